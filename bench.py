@@ -1,0 +1,364 @@
+"""Benchmark: exact-DBSCAN points/sec on one GB300 (replicas on N GPUs).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload zipf2d_10m|aniso3d_20m|blobs2d_100k]
+                  [--precision fp64|fp32band]
+
+Default workload: 10,000,000 2D float64 points (500 Zipf-sized Gaussian blobs +
+5% uniform noise), eps=0.3, minpts=8, every distance test in float64 -- the
+single-instance GPU configuration the headline metric is quoted on.
+
+A step is one full exact-DBSCAN pass (index build, core flags, union-find,
+cluster numbering, borders, labels in caller order) over the whole point set.
+  value  points/s with the points already in HBM (CUDA events on the stream the
+         library launches on, L2 flushed between steps with a 512 MiB write)
+  e2e    points/s through gd_dbscan with pinned HOST input and output: the
+         host->device copy of the points and the device->host copy of the
+         labels are inside the timed region
+The JSON line also carries a float32-band run of the same workload, per-phase
+device times, the roofline of the pipeline, the CPU baseline (the CPU
+restatement of the reference's exact DBSCAN on this host's cores, bounded
+sample) and the SM clocks sampled during the timed region.
+
+--impl reference times the reference's exact CPU DBSCAN path on this host: the
+reference's own R-tree program (oracle/_ref) where it was built, otherwise the
+CPU restatement (oracle/), with all host threads, on a bounded sample per step.
+Multi-GPU: the path does not shard across GPUs here; --gpus N runs N
+independent replicas (one per rank) and reports their aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+PKG = "fast-cuda-gpu-dbscan_gb300"
+
+ALGO_BYTES_PER_POINT = {2: 8 * 2 + 4, 3: 8 * 3 + 4}   # f64 coordinates in + int32 label out
+METRIC = "points/sec at exact labels"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if len(r) > 2 + i and r[2 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def make_workload(name: str):
+    ds = importlib.import_module(PKG + ".datasets")
+    return getattr(ds, name)(seed=0)
+
+
+def cpu_baseline(name: str, target_s: float = 12.0):
+    """The CPU restatement of the reference's exact DBSCAN on all host cores,
+    on a bounded sample of the same workload (density-preserving scale-down)."""
+    from oracle import oracle
+    ds = importlib.import_module(PKG + ".datasets")
+    cores = os.cpu_count() or 1
+    scale = 0.01
+    while True:
+        inst = getattr(ds, name)(seed=0, scale=scale)
+        t0 = time.perf_counter()
+        oracle.oracle_dbscan(inst.points, inst.eps, inst.minpts, nthreads=cores)
+        dt = time.perf_counter() - t0
+        if dt * 3 > target_s or scale >= 1.0:
+            break
+        scale = min(1.0, scale * max(2.0, min(8.0, target_s / max(dt, 1e-3) / 2)))
+    return {"value": inst.n / dt, "unit": "points/s", "cores": cores, "kind": "port",
+            "sample": f"{name} scale {scale:g}: {inst.n} points, one full run, {dt:.2f} s"}
+
+
+def run_reference(args, rank):
+    """--impl reference: the reference's exact CPU DBSCAN on this host."""
+    if rank != 0:
+        return None
+    from oracle import build as obuild
+    from oracle import oracle
+    ds = importlib.import_module(PKG + ".datasets")
+    cores = os.cpu_count() or 1
+    use_ref = os.path.exists(obuild.REF_RTREE_SO)
+    wl = args.workload
+    dim = 3 if wl.startswith("aniso3d") else 2
+    if use_ref and dim != 2:
+        use_ref = False
+    # bounded sample: grow the scale until one run takes ~6 s
+    scale, inst, dt = 0.002, None, 0.0
+    while True:
+        inst = getattr(ds, wl)(seed=0, scale=scale)
+        t0 = time.perf_counter()
+        if use_ref:
+            oracle.ref_rtree_dbscan(inst.points, inst.eps, inst.minpts)
+        else:
+            oracle.oracle_dbscan(inst.points, inst.eps, inst.minpts, nthreads=cores)
+        dt = time.perf_counter() - t0
+        if dt > 2.0 or scale >= 1.0:
+            break
+        scale = min(1.0, scale * 4)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        if use_ref:
+            oracle.ref_rtree_dbscan(inst.points, inst.eps, inst.minpts)
+        else:
+            oracle.oracle_dbscan(inst.points, inst.eps, inst.minpts, nthreads=cores)
+        times.append(time.perf_counter() - t0)
+    t = sum(times)
+    value = inst.n * len(times) / t
+    kind = "reference" if use_ref else "port"
+    return {
+        "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": wl, "points": inst.n, "eps": inst.eps, "minpts": inst.minpts,
+                   "sample_scale": scale},
+        "cpu_baseline": {"value": value, "unit": "points/s", "cores": 1 if use_ref else cores,
+                         "kind": kind,
+                         "sample": f"{wl} scale {scale:g} ({inst.n} points) per step"},
+        "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="zipf2d_10m",
+                    choices=["zipf2d_10m", "aniso3d_20m", "blobs2d_100k"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32band"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+
+    if args.impl == "reference":
+        line = run_reference(args, rank)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    import torch
+    gdm = importlib.import_module(PKG)
+    gdm.load_library()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    inst = make_workload(args.workload)
+    n, dim = inst.n, inst.dim
+    prec = gdm.GD_PREC_FP64 if args.precision == "fp64" else gdm.GD_PREC_FP32_BAND
+
+    stream = torch.cuda.current_stream(dev)
+    ctx = gdm.Context(local, precision=prec)
+    ctx.set_stream(stream.cuda_stream)
+    pts_dev = torch.from_numpy(inst.points).to(dev)
+    lab_dev = torch.empty(n, dtype=torch.int32, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.int32, device=dev)
+
+    def step_device():
+        ctx.index_build(pts_dev, inst.eps)
+        ctx.expand(inst.minpts)
+        ctx.get_result(out=lab_dev)
+
+    def timed_device(k, w, sampler=None):
+        for _ in range(w):
+            step_device()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        evs = []
+        phases = []
+        for _ in range(k):
+            flush.fill_(1)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step_device()
+            b.record(stream)
+            evs.append((a, b))
+            phases.append(ctx.stats())
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        ms = [a.elapsed_time(b) for a, b in evs]
+        return ms, phases
+
+    # headline: device-resident input, chosen precision
+    with ClockSampler(local) as clk:
+        ms, phases = timed_device(args.steps, args.warmup)
+    clocks = clk.summary()
+    t_step = sum(ms) / len(ms)
+    if dist:
+        t = torch.tensor([t_step], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_step = float(t.item())
+    value = world * n / (t_step / 1e3)
+    st = phases[-1]
+    ref_labels = lab_dev.cpu().numpy()
+
+    # the other precision on the same workload (labels must agree bit for bit)
+    other = gdm.GD_PREC_FP32_BAND if prec == gdm.GD_PREC_FP64 else gdm.GD_PREC_FP64
+    ctx.set_precision(other)
+    ms2, ph2 = timed_device(max(3, args.steps // 2), 1)
+    other_labels_equal = bool(np.array_equal(lab_dev.cpu().numpy(), ref_labels))
+    ctx.set_precision(prec)
+
+    # end to end through gd_dbscan: pinned host points in, pinned host labels out
+    host_pts = torch.from_numpy(inst.points).pin_memory().numpy()
+    host_lab = torch.empty(n, dtype=torch.int32).pin_memory().numpy()
+    ctx2 = gdm.Context(local, precision=prec)
+    import ctypes
+    api = importlib.import_module(PKG + ".api")
+    gp = api.GdPoints(host_pts.ctypes.data, n, dim, 0)
+    gst = api.GdStats()
+
+    def step_e2e():
+        api._check(ctx2._lib.gd_dbscan(ctx2._ctx, ctypes.byref(gp), inst.eps, inst.minpts,
+                                       host_lab.ctypes.data, ctypes.byref(gst)))
+
+    for _ in range(args.warmup):
+        step_e2e()
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step_e2e()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_times) / len(e2e_times)
+    if dist:
+        t = torch.tensor([e2e_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_equal = bool(np.array_equal(host_lab, ref_labels))
+    ctx2.close()
+
+    peak, peak_kind = peaks()
+    algo = ALGO_BYTES_PER_POINT[dim] * n
+    achieved = algo / (t_step / 1e3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", f"traffic_{args.workload}_{args.precision}.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            traffic = json.load(f).get("dram_bytes_per_step")
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args.workload)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == gdm.GD_PREC_FP64 else "f32+f64band", "data": "synthetic",
+        "config": {"workload": args.workload, "points": n, "dim": dim, "eps": inst.eps,
+                   "minpts": inst.minpts, "precision": args.precision,
+                   "parallelism": f"replicas{world}",
+                   "l2": "512 MiB flush write between timed steps; inputs 160+ MB > L2"},
+        "e2e": {"value": world * n / e2e_s, "unit": "points/s",
+                "h2d_bytes_per_step": n * dim * 8, "d2h_bytes_per_step": n * 4,
+                "ms_per_step": e2e_s * 1e3, "labels_equal_device_run": e2e_equal},
+        "gpu_launches": int(st["launches"]) * args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "kernel": "whole single-instance pipeline (one step)",
+                     "algorithmic_bytes": algo},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "phases_ms": {k: st[k] for k in ("ms_index", "ms_core", "ms_union", "ms_label",
+                                          "ms_total")},
+        "counts": {k: st[k] for k in ("n_clusters", "n_noise", "n_core", "n_border", "n_cells",
+                                      "n_dense_cells", "tests_fp64", "tests_fp32",
+                                      "band_retests", "asym_pairs", "key_bits")},
+        "other_precision": {"precision": "fp32band" if other == gdm.GD_PREC_FP32_BAND else "fp64",
+                            "value": world * n / (sum(ms2) / len(ms2) / 1e3),
+                            "ms_per_step": sum(ms2) / len(ms2),
+                            "labels_identical": other_labels_equal,
+                            "tests_fp32": ph2[-1]["tests_fp32"],
+                            "tests_fp64": ph2[-1]["tests_fp64"],
+                            "band_retests": ph2[-1]["band_retests"],
+                            "band_hit_rate": ph2[-1]["band_retests"] / max(1, ph2[-1]["tests_fp32"])},
+    }
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,153 @@
+// gd_internal.cuh -- device-side declarations shared by the gbdbscan kernels.
+//
+// Data layout in HBM for one clustering instance of n points in d dimensions
+// (d = 2 or 3), after the index build:
+//   keys[n]   u32   fine-cell key of each point, sorted ascending
+//   ids[n]    u32   original point index of each sorted position
+//   X[k][n]   f64   coordinate k of each sorted position (structure of arrays)
+//   start[C+1] i32  dense cell table: points of cell c are start[c]..start[c+1]
+//   reps[M+1] i32   sorted position of the first point of every non-empty cell
+// Per non-empty cell, indexed by its first sorted position b ("rep"):
+//   cellcore[b]  number of core points in the cell
+//   cellmin[b]   smallest original index among the cell's core points
+//   parent[b]    union-find parent (a rep position)
+//   cellcid[b]   cluster id of the cell's core points
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gd {
+
+constexpr int kNoise = -2;            // common.h:8 NOISE
+constexpr int kWarp = 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+// Grid and predicate parameters, computed on the device from the bounding box.
+struct DevParams {
+  double lo[3];        // per-dimension minimum (grid origin)
+  double hi[3];        // per-dimension maximum
+  double centre[3];    // bounding-box centre (origin of the float32 copy)
+  double f;            // fine cell side
+  double inv_f;        // 1 / f
+  double eps;          // epsilon
+  double eps2;         // fl(eps * eps), the reference's threshold
+  double eps2_in;      // float64 d2 <= eps2_in implies the box test passes
+  float eps2_lo32;     // float32 d2 below this: certainly a neighbour
+  float eps2_hi32;     // float32 d2 above this: certainly not a neighbour
+  int64_t G[3];        // cells per dimension
+  uint64_t C;          // total cells (G0*G1[*G2])
+  int32_t dim;
+  int32_t minpts;
+  int32_t key_bits;
+  int32_t flags;       // kFlag*
+};
+
+constexpr int kFlagNonFinite = 1;     // NaN or Inf coordinate
+constexpr int kFlagGridTooLarge = 2;  // cell table would exceed the limit
+constexpr int kFlagNoShortcut = 4;    // |x| too large relative to eps for the
+                                      // box-test shortcut / float32 filter
+
+// Device counters (u64), zeroed per run.
+enum Counter {
+  kCtrCells = 0,        // M, number of non-empty cells
+  kCtrTests64,          // float64 distance evaluations
+  kCtrTests32,          // float32 distance evaluations
+  kCtrBand,             // float32 evaluations that fell in the re-test band
+  kCtrAsym,             // core pairs that are neighbours in one direction only
+  kCtrClusters,         // K
+  kCtrCore,             // core points
+  kCtrNoise,            // noise points
+  kCtrDenseCells,       // cells with >= minpts points
+  kCtrCount = 16
+};
+
+// ---- float64 predicate, bit-exact with the reference's CPU DBSCAN ----------
+// Neighbour test with centre p and candidate q: the query box
+// [fl(p-eps), fl(p+eps)] with inclusive bounds (cpu-dbscan/Rtree.h:1573-1588)
+// and fl(fl(dx*dx) + fl(dy*dy) [+ fl(dz*dz)]) <= fl(eps*eps), dx = fl(p - q)
+// (cpu-dbscan/dbscan_rtree_exp.cpp:351-358, 431-432).  The _rn intrinsics keep
+// the compiler from fusing multiply-adds, which would change the bits.
+template <int D>
+__device__ __forceinline__ double dist2_f64(const double* p, const double* q) {
+  double a = __dsub_rn(p[0], q[0]);
+  double s = __dmul_rn(a, a);
+  double b = __dsub_rn(p[1], q[1]);
+  s = __dadd_rn(s, __dmul_rn(b, b));
+  if (D == 3) {
+    double c = __dsub_rn(p[2], q[2]);
+    s = __dadd_rn(s, __dmul_rn(c, c));
+  }
+  return s;
+}
+
+template <int D>
+__device__ __forceinline__ bool box_f64(const double* p, const double* q, double eps) {
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    double lo = __dsub_rn(p[k], eps);
+    double hi = __dadd_rn(p[k], eps);
+    if (lo > q[k] || q[k] > hi) return false;
+  }
+  return true;
+}
+
+// Full predicate given d2 = dist2_f64(p, q).
+template <int D>
+__device__ __forceinline__ bool pred_from_d2(double d2, const double* p, const double* q,
+                                             const DevParams& P) {
+  if (d2 <= P.eps2_in) return true;
+  if (!(d2 <= P.eps2)) return false;
+  return box_f64<D>(p, q, P.eps);
+}
+
+// ---- union-find over cell reps (lock-free, hooks by (cellmin, position)) ---
+__device__ __forceinline__ int uf_find(int* parent, int x) {
+  volatile int* par = parent;
+  int p = par[x];
+  while (p != x) {
+    int gp = par[p];
+    if (gp != p) par[x] = gp;
+    x = p;
+    p = gp;
+  }
+  return x;
+}
+
+__device__ __forceinline__ bool uf_less(const int* cellmin, int a, int b) {
+  int wa = cellmin[a], wb = cellmin[b];
+  return wa < wb || (wa == wb && a < b);
+}
+
+__device__ __forceinline__ void uf_union(int* parent, const int* cellmin, int a, int b) {
+  while (true) {
+    a = uf_find(parent, a);
+    b = uf_find(parent, b);
+    if (a == b) return;
+    if (uf_less(cellmin, b, a)) { int t = a; a = b; b = t; }
+    // hook b (the heavier root) under a
+    int old = atomicCAS(parent + b, b, a);
+    if (old == b) return;
+    b = old;
+  }
+}
+
+}  // namespace gd
+
+// ---- host-side primitive launchers (gd_prims.cu) ---------------------------
+namespace gdprim {
+// temp bytes needed by exclusive_scan_u32 for n elements
+size_t scan_temp_bytes(int64_t n);
+// out[i] = sum_{j<i} in[i]; in == out allowed.  Returns the total in *total_dev
+// (device pointer, may be null).
+void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, void* temp,
+                        uint32_t* total_dev, cudaStream_t s);
+// temp bytes needed by radix_sort_pairs for n elements
+size_t sort_temp_bytes(int64_t n);
+// Stable LSD radix sort of (key, value) pairs on the low `bits` key bits.
+// keys/vals: ping-pong buffers [0] and [1]; input in [0].  If vals_in_is_iota,
+// vals[0] is not read and the values are taken as 0..n-1.  Returns the index
+// (0 or 1) of the buffer that holds the result.
+int radix_sort_pairs(uint32_t* keys[2], uint32_t* vals[2], int64_t n, int bits,
+                     bool vals_in_is_iota, void* temp, cudaStream_t s);
+}  // namespace gdprim

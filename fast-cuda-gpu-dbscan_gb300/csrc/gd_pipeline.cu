@@ -1,0 +1,815 @@
+// gd_pipeline.cu -- the exact-DBSCAN kernels for one instance.
+//
+// Replaces, in the reference (CUDA-DClust+):
+//   host bbox + bin widths        main.cu:166-207           -> k_bbox_partial, k_params
+//   INDEXING_STRUCTURE/insertData indexing.cu:54-118        -> k_keys (cell keys)
+//   thrust::sort_by_key           main.cu:332               -> gdprim::radix_sort_pairs
+//   INDEXING_ADJUSTMENT           indexing.cu:23-51         -> k_run_flags/k_run_scatter/
+//                                                              k_cell_counts + scan (cell table)
+//   DBSCAN kernel + searchPoints  dbscan.cu:254-474         -> k_core (core flags)
+//   MarkAsCandidate + host merge  dbscan.cu:189-222, 25-187 -> k_union (device union-find)
+//   GetDbscanResult               dbscan.cu:225-251         -> k_roots, k_label, k_border,
+//                                                              k_scatter_labels
+//
+// Grid: fine cells of side f = eps * m, m = 0.5 * (1 + 2^-16) by default, keyed
+// x-major.  Two points of one cell are always neighbours (cell diagonal
+// <= 0.87 eps), and every neighbour of a point lies within +-2 cells per axis.
+// A cell holding >= minpts points is therefore all core ("dense") without a
+// single distance evaluation, and all core points of a cell are in one cluster.
+//
+// Precision modes (template flag F32):
+//   F32 = false: every pair decision is the float64 predicate (gd_internal.cuh).
+//   F32 = true : the pair is first measured in float32 on bbox-centred
+//                coordinates; only pairs whose float32 d2 falls inside a proven
+//                rounding band around eps^2 are re-tested with the float64
+//                predicate.  Outside the band the float32 decision provably
+//                equals the float64 one, so labels stay bit-exact.
+#include <cfloat>
+#include <climits>
+
+#include "gd_internal.cuh"
+
+namespace gd {
+
+// ------------------------------------------------------------------ bbox
+constexpr int kBboxThreads = 256;
+
+template <int D>
+__global__ void __launch_bounds__(kBboxThreads)
+k_bbox_partial(const double* __restrict__ pts, int64_t n, double* __restrict__ partial,
+               int* __restrict__ flags) {
+  double lo[D], hi[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) { lo[k] = DBL_MAX; hi[k] = -DBL_MAX; }
+  bool bad = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      double v = pts[i * D + k];
+      bad |= !isfinite(v);
+      lo[k] = fmin(lo[k], v);
+      hi[k] = fmax(hi[k], v);
+    }
+  }
+  __shared__ double s[2 * D][kBboxThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[k] = fmin(lo[k], __shfl_xor_sync(kFull, lo[k], o));
+      hi[k] = fmax(hi[k], __shfl_xor_sync(kFull, hi[k], o));
+    }
+    if (lane == 0) { s[k][w] = lo[k]; s[D + k][w] = hi[k]; }
+  }
+  if (__any_sync(kFull, bad) && lane == 0) atomicOr(flags, kFlagNonFinite);
+  __syncthreads();
+  if (threadIdx.x < 2 * D) {
+    const int k = threadIdx.x;
+    double v = s[k][0];
+    for (int j = 1; j < kBboxThreads / 32; ++j) v = k < D ? fmin(v, s[k][j]) : fmax(v, s[k][j]);
+    partial[blockIdx.x * 2 * D + k] = v;
+  }
+}
+
+// One thread: finish the reduction, derive the grid and the float32 band.
+template <int D>
+__global__ void k_params(const double* __restrict__ partial, int nblocks, DevParams* P,
+                         double eps, int minpts, double cell_mult, uint64_t max_cells,
+                         const int* __restrict__ flags) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  DevParams p;
+  int fl = *flags;
+  for (int k = 0; k < 3; ++k) { p.lo[k] = 0; p.hi[k] = 0; p.centre[k] = 0; p.G[k] = 1; }
+  for (int k = 0; k < D; ++k) {
+    double lo = DBL_MAX, hi = -DBL_MAX;
+    for (int b = 0; b < nblocks; ++b) {
+      lo = fmin(lo, partial[b * 2 * D + k]);
+      hi = fmax(hi, partial[b * 2 * D + k + D]);
+    }
+    p.lo[k] = lo;
+    p.hi[k] = hi;
+    p.centre[k] = 0.5 * lo + 0.5 * hi;
+  }
+  p.dim = D;
+  p.minpts = minpts;
+  p.eps = eps;
+  p.eps2 = __dmul_rn(eps, eps);
+  p.f = __dmul_rn(eps, cell_mult);
+  p.inv_f = 1.0 / p.f;
+  double cells = 1.0;
+  uint64_t C = 1;
+  for (int k = 0; k < D; ++k) {
+    double t = floor(__dmul_rn(__dsub_rn(p.hi[k], p.lo[k]), p.inv_f)) + 1.0;
+    if (!(t < 4294967296.0)) { fl |= kFlagGridTooLarge; t = 1.0; }
+    p.G[k] = (int64_t)t;
+    cells *= t;
+    C *= (uint64_t)p.G[k];
+  }
+  if (cells > (double)max_cells || C > max_cells) fl |= kFlagGridTooLarge;
+  p.C = C;
+  int bits = 0;
+  while (bits < 63 && (C - 1) >> bits) ++bits;
+  p.key_bits = bits;
+  // box-test shortcut and float32 filter need every |x| <= eps * 2^30
+  double maxabs = 0, R = 0;
+  for (int k = 0; k < D; ++k) {
+    maxabs = fmax(maxabs, fmax(fabs(p.lo[k]), fabs(p.hi[k])));
+    R = fmax(R, fmax(p.hi[k] - p.centre[k], p.centre[k] - p.lo[k]));
+  }
+  if (maxabs <= eps * 1073741824.0) {
+    p.eps2_in = __dmul_rn(p.eps2, 1.0 - 1.0 / 524288.0);    // 1 - 2^-19
+  } else {
+    p.eps2_in = -1.0;
+    fl |= kFlagNoShortcut;
+  }
+  // float32 band: see the derivation in the file header of gd_api.cu
+  {
+    const double u32 = 1.0 / 16777216.0;               // 2^-24
+    R = R * (1.0 + 1e-12) + 1e-300;
+    const double ea = R * u32 * (1.0 + 1e-8);          // |fl32(x - c) - (x - c)|
+    const double e2 = p.eps2;
+    const double rs = sqrt(2.0 * e2) * sqrt((double)D);
+    double bmax = (2.0 * e2 + 4.0 * ea * rs + 4.0 * D * ea * ea) * (D + 3) * u32
+                  + 4.0 * ea * rs + 4.0 * D * ea * ea;
+    bmax *= 1.5;
+    const double L = e2 * (1.0 - 1.0 / 131072.0) - bmax;   // 2^-17
+    const double H = e2 * (1.0 + 1.0 / 131072.0) + bmax;
+    const bool ok = !(fl & kFlagNoShortcut) && e2 > 1e-30 && R < 1e30 && L > 0.25 * e2 &&
+                    H < 4.0 * e2;
+    p.eps2_lo32 = ok ? __double2float_rd(L) : -1.0f;
+    p.eps2_hi32 = ok ? __double2float_ru(H) : -1.0f;
+  }
+  p.flags = fl;
+  *P = p;
+}
+
+// ------------------------------------------------------------------ keys
+template <int D>
+__global__ void k_keys(const double* __restrict__ pts, int64_t n, const DevParams* __restrict__ Pp,
+                       uint32_t* __restrict__ keys) {
+  const DevParams P = *Pp;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint64_t key = 0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      double t = __dmul_rn(__dsub_rn(pts[i * D + k], P.lo[k]), P.inv_f);
+      int64_t g = (int64_t)floor(t);
+      g = g < 0 ? 0 : (g >= P.G[k] ? P.G[k] - 1 : g);
+      key = key * (uint64_t)P.G[k] + (uint64_t)g;
+    }
+    keys[i] = (uint32_t)key;
+  }
+}
+
+// sorted structure-of-arrays copy (+ float32 centred copy)
+template <int D, bool F32>
+__global__ void k_gather(const double* __restrict__ pts, const uint32_t* __restrict__ ids,
+                         int64_t n, const DevParams* __restrict__ Pp, double* __restrict__ X,
+                         float* __restrict__ Xf) {
+  double c[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) c[k] = Pp->centre[k];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = ids[i];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      double v = pts[j * D + k];
+      X[k * n + i] = v;
+      if (F32) Xf[k * n + i] = __double2float_rn(__dsub_rn(v, c[k]));
+    }
+  }
+}
+
+__global__ void k_run_flags(const uint32_t* __restrict__ keys, int64_t n, uint32_t* __restrict__ fl) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    fl[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
+}
+
+__global__ void k_run_scatter(const uint32_t* __restrict__ fl, const uint32_t* __restrict__ pos,
+                              int64_t n, int* __restrict__ reps, const uint32_t* __restrict__ Mdev,
+                              unsigned long long* ctr) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    if (fl[i]) reps[pos[i]] = (int)i;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    reps[*Mdev] = (int)n;
+    ctr[kCtrCells] = *Mdev;
+  }
+}
+
+__global__ void k_cell_counts(const uint32_t* __restrict__ keys, const int* __restrict__ reps,
+                              const uint32_t* __restrict__ Mdev, uint32_t* __restrict__ table) {
+  const int64_t M = *Mdev;
+  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
+       m += (int64_t)gridDim.x * blockDim.x) {
+    int b = reps[m], e = reps[m + 1];
+    table[keys[b]] = (uint32_t)(e - b);
+  }
+}
+
+// ------------------------------------------------------------- cell helpers
+template <int D>
+struct CellXYZ {
+  int64_t c[3];
+};
+
+template <int D>
+__device__ __forceinline__ CellXYZ<D> decompose(uint32_t key, const DevParams& P) {
+  CellXYZ<D> r;
+  uint64_t k = key;
+  if (D == 3) {
+    r.c[2] = (int64_t)(k % (uint64_t)P.G[2]);
+    k /= (uint64_t)P.G[2];
+  } else {
+    r.c[2] = 0;
+  }
+  r.c[1] = (int64_t)(k % (uint64_t)P.G[1]);
+  r.c[0] = (int64_t)(k / (uint64_t)P.G[1]);
+  return r;
+}
+
+// key of cell (c + o), or -1 when outside the grid
+template <int D>
+__device__ __forceinline__ int64_t offset_key(const CellXYZ<D>& c, int ox, int oy, int oz,
+                                              const DevParams& P) {
+  int64_t x = c.c[0] + ox, y = c.c[1] + oy;
+  if (x < 0 || x >= P.G[0] || y < 0 || y >= P.G[1]) return -1;
+  int64_t k = x * P.G[1] + y;
+  if (D == 3) {
+    int64_t z = c.c[2] + oz;
+    if (z < 0 || z >= P.G[2]) return -1;
+    k = k * P.G[2] + z;
+  }
+  return k;
+}
+
+__constant__ int kRowOrder[5] = {0, -1, 1, -2, 2};
+
+// Loads one candidate (sorted position q) in the layout the mode tests with.
+template <int D, bool F32>
+struct Cand {
+  double x[D];
+  float f[D];
+};
+
+template <int D, bool F32>
+__device__ __forceinline__ void load_cand(Cand<D, F32>& c, const double* __restrict__ X,
+                                          const float* __restrict__ Xf, int64_t n, int64_t q) {
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    if (F32) c.f[k] = Xf[k * n + q];
+    else c.x[k] = X[k * n + q];
+  }
+}
+
+// Per-warp staging of up to 32 "A" points (the points of the cell in work).
+template <int D>
+struct WarpStage {
+  double x[32][D];
+  float f[32][D];
+};
+
+struct Tally {
+  uint32_t t64 = 0, t32 = 0, band = 0, asym = 0;
+};
+
+// float32 distance (centred copies); FMA-rounded as the band derivation assumes
+template <int D>
+__device__ __forceinline__ float dist2_f32(const float* a, const float* b) {
+  float u = __fsub_rn(a[0], b[0]);
+  float s = __fmul_rn(u, u);
+  float v = __fsub_rn(a[1], b[1]);
+  s = __fmaf_rn(v, v, s);
+  if (D == 3) {
+    float w = __fsub_rn(a[2], b[2]);
+    s = __fmaf_rn(w, w, s);
+  }
+  return s;
+}
+
+// Directed test "cand is a neighbour of centre".  One side is a staged point
+// (coords in smem), the other a candidate (coords in registers / memory).
+// stage_is_centre selects which is the centre of the query box.
+template <int D, bool F32>
+__device__ __forceinline__ bool pair_test(const double* sx, const float* sf, const Cand<D, F32>& c,
+                                          const double* __restrict__ X, int64_t n, int64_t q,
+                                          bool stage_is_centre, const DevParams& P, Tally& t) {
+  if (F32) {
+    ++t.t32;
+    float s = dist2_f32<D>(sf, c.f);
+    if (s < P.eps2_lo32) return true;
+    if (s > P.eps2_hi32) return false;
+    ++t.band;
+    double qx[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) qx[k] = X[k * n + q];
+    ++t.t64;
+    double d2 = dist2_f64<D>(sx, qx);
+    return stage_is_centre ? pred_from_d2<D>(d2, sx, qx, P) : pred_from_d2<D>(d2, qx, sx, P);
+  } else {
+    ++t.t64;
+    double d2 = dist2_f64<D>(sx, c.x);
+    return stage_is_centre ? pred_from_d2<D>(d2, sx, c.x, P) : pred_from_d2<D>(d2, c.x, sx, P);
+  }
+}
+
+// Symmetric test for core-core links: true when the pair is a neighbour in both
+// directions; counts pairs that are neighbours in exactly one direction.
+template <int D, bool F32>
+__device__ __forceinline__ bool link_test(const double* sx, const float* sf, const Cand<D, F32>& c,
+                                          const double* __restrict__ X, int64_t n, int64_t q,
+                                          const DevParams& P, Tally& t) {
+  double qx[D];
+  if (F32) {
+    ++t.t32;
+    float s = dist2_f32<D>(sf, c.f);
+    if (s < P.eps2_lo32) return true;
+    if (s > P.eps2_hi32) return false;
+    ++t.band;
+#pragma unroll
+    for (int k = 0; k < D; ++k) qx[k] = X[k * n + q];
+  } else {
+#pragma unroll
+    for (int k = 0; k < D; ++k) qx[k] = c.x[k];
+  }
+  ++t.t64;
+  double d2 = dist2_f64<D>(sx, qx);
+  if (d2 <= P.eps2_in) return true;
+  if (!(d2 <= P.eps2)) return false;
+  bool f = box_f64<D>(sx, qx, P.eps), b = box_f64<D>(qx, sx, P.eps);
+  if (f != b) ++t.asym;
+  return f && b;
+}
+
+__device__ __forceinline__ void flush_tally(const Tally& t, unsigned long long* ctr) {
+  // one atomic per warp per counter
+  unsigned long long a = t.t64, b = t.t32, c = t.band, d = t.asym;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(kFull, a, o);
+    b += __shfl_xor_sync(kFull, b, o);
+    c += __shfl_xor_sync(kFull, c, o);
+    d += __shfl_xor_sync(kFull, d, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (a) atomicAdd(ctr + kCtrTests64, a);
+    if (b) atomicAdd(ctr + kCtrTests32, b);
+    if (c) atomicAdd(ctr + kCtrBand, c);
+    if (d) atomicAdd(ctr + kCtrAsym, d);
+  }
+}
+
+__device__ __forceinline__ int warp_min_i32(int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(kFull, v, o));
+  return v;
+}
+
+constexpr int kWarpsPerBlock = 8;
+constexpr int kCellThreads = kWarpsPerBlock * 32;
+
+// ------------------------------------------------------------- core flags
+// One warp per non-empty cell.  Dense cells are all core.  Otherwise every point
+// p of the cell counts its neighbours: the warp streams the candidate rows (the
+// 5 cells along the last axis, merged into one contiguous range) 32 at a time,
+// one candidate per lane, and each staged p gets __ballot_sync + __popc of the
+// lanes that hold a neighbour.  Stops as soon as every p has reached minpts.
+template <int D, bool F32>
+__global__ void __launch_bounds__(kCellThreads)
+k_core(const DevParams* __restrict__ Pp, const uint32_t* __restrict__ keys,
+       const int* __restrict__ reps, const uint32_t* __restrict__ Mdev,
+       const uint32_t* __restrict__ start, const double* __restrict__ X,
+       const float* __restrict__ Xf, int64_t n, const uint32_t* __restrict__ ids,
+       uint8_t* __restrict__ core, int* __restrict__ cellcore, int* __restrict__ cellmin,
+       unsigned long long* ctr) {
+  __shared__ DevParams sP;
+  __shared__ WarpStage<D> stage[kWarpsPerBlock];
+  if (threadIdx.x == 0) sP = *Pp;
+  __syncthreads();
+  const DevParams& P = sP;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  WarpStage<D>& S = stage[w];
+  const int64_t M = *Mdev;
+  const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
+  Tally t;
+  unsigned long long dense = 0;
+  for (int64_t m = (int64_t)blockIdx.x * kWarpsPerBlock + w; m < M; m += W) {
+    const int b = reps[m], e = reps[m + 1], sz = e - b;
+    if (sz >= P.minpts) {
+      int mn = INT_MAX;
+      for (int i = b + lane; i < e; i += 32) {
+        core[i] = 1;
+        mn = min(mn, (int)ids[i]);
+      }
+      mn = warp_min_i32(mn);
+      if (lane == 0) { cellcore[b] = sz; cellmin[b] = mn; ++dense; }
+      continue;
+    }
+    const CellXYZ<D> cc = decompose<D>(keys[b], P);
+    const int64_t Gl = P.G[D - 1];
+    const int64_t cl = cc.c[D - 1];
+    const int64_t l0 = cl - 2 < 0 ? 0 : cl - 2;
+    const int64_t l1 = cl + 2 >= Gl ? Gl - 1 : cl + 2;
+    int ncore = 0, mn = INT_MAX;
+    for (int c0 = 0; c0 < sz; c0 += 32) {
+      const int na = min(32, sz - c0);
+      if (lane < na) {
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+          S.x[lane][k] = X[k * n + b + c0 + lane];
+          if (F32) S.f[lane][k] = Xf[k * n + b + c0 + lane];
+        }
+      }
+      __syncwarp();
+      int mycnt = 0;
+      bool done = false;
+      const int nrows = D == 3 ? 25 : 5;
+      for (int r = 0; r < nrows && !done; ++r) {
+        const int ox = kRowOrder[D == 3 ? r / 5 : r];
+        const int oy = D == 3 ? kRowOrder[r % 5] : 0;
+        int64_t rowkey = offset_key<D>(cc, ox, D == 3 ? oy : 0, 0, P);
+        if (rowkey < 0) continue;
+        rowkey -= cl;  // key of the row's first cell
+        const int64_t qlo = start[rowkey + l0];
+        const int64_t qhi = start[rowkey + l1 + 1];
+        for (int64_t qb = qlo; qb < qhi && !done; qb += 32) {
+          const int64_t q = qb + lane;
+          const bool valid = q < qhi;
+          Cand<D, F32> c;
+          if (valid) load_cand<D, F32>(c, X, Xf, n, q);
+          for (int j = 0; j < na; ++j) {
+            bool hit = valid && pair_test<D, F32>(S.x[j], S.f[j], c, X, n, q, true, P, t);
+            unsigned bal = __ballot_sync(kFull, hit);
+            if (lane == j) mycnt += __popc(bal);
+          }
+          done = __all_sync(kFull, lane >= na || mycnt >= P.minpts);
+        }
+      }
+      const bool isc = lane < na && mycnt >= P.minpts;
+      if (lane < na) core[b + c0 + lane] = isc ? 1 : 0;
+      if (isc) mn = min(mn, (int)ids[b + c0 + lane]);
+      ncore += __popc(__ballot_sync(kFull, isc));
+      __syncwarp();
+    }
+    mn = warp_min_i32(mn);
+    if (lane == 0) { cellcore[b] = ncore; cellmin[b] = mn; }
+  }
+  flush_tally(t, ctr);
+  if (lane == 0 && dense) atomicAdd(ctr + kCtrDenseCells, dense);
+}
+
+// ------------------------------------------------------------- union-find
+__global__ void k_parent_init(const int* __restrict__ reps, const uint32_t* __restrict__ Mdev,
+                              int* __restrict__ parent) {
+  const int64_t M = *Mdev;
+  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
+       m += (int64_t)gridDim.x * blockDim.x) {
+    int b = reps[m];
+    parent[b] = b;
+  }
+}
+
+// Half stencil of cell offsets (o > 0 lexicographically).  PASS 0: offsets with
+// every |o_k| <= 1; PASS 1: the others.  Running the near pass first lets most
+// far pairs be skipped because their cells are already in one component.
+template <int D>
+__device__ __forceinline__ bool half_offset(int t, int pass, int& ox, int& oy, int& oz) {
+  if (D == 2) {
+    ox = t / 5 - 2; oy = t % 5 - 2; oz = 0;
+  } else {
+    ox = t / 25 - 2; oy = (t / 5) % 5 - 2; oz = t % 5 - 2;
+  }
+  bool pos = ox > 0 || (ox == 0 && (oy > 0 || (oy == 0 && oz > 0)));
+  if (!pos) return false;
+  bool near = abs(ox) <= 1 && abs(oy) <= 1 && abs(oz) <= 1;
+  return (pass == 0) == near;
+}
+
+// One warp per cell A with core points; for each half-stencil neighbour cell B
+// with core points in another component, look for one core-core pair that are
+// neighbours both ways (lanes over B's points, A's points broadcast) and unite.
+template <int D, bool F32>
+__global__ void __launch_bounds__(kCellThreads)
+k_union(const DevParams* __restrict__ Pp, int pass, const uint32_t* __restrict__ keys,
+        const int* __restrict__ reps, const uint32_t* __restrict__ Mdev,
+        const uint32_t* __restrict__ start, const double* __restrict__ X,
+        const float* __restrict__ Xf, int64_t n, const uint8_t* __restrict__ core,
+        const int* __restrict__ cellcore, const int* __restrict__ cellmin, int* parent,
+        unsigned long long* ctr) {
+  __shared__ DevParams sP;
+  if (threadIdx.x == 0) sP = *Pp;
+  __syncthreads();
+  const DevParams& P = sP;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t M = *Mdev;
+  const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
+  constexpr int NT = D == 3 ? 125 : 25;
+  Tally t;
+  for (int64_t m = (int64_t)blockIdx.x * kWarpsPerBlock + w; m < M; m += W) {
+    const int b = reps[m];
+    if (cellcore[b] == 0) continue;
+    const int e = reps[m + 1];
+    const CellXYZ<D> cc = decompose<D>(keys[b], P);
+    for (int tt = 0; tt < NT; ++tt) {
+      int ox, oy, oz;
+      if (!half_offset<D>(tt, pass, ox, oy, oz)) continue;
+      const int64_t kb = offset_key<D>(cc, ox, oy, oz, P);
+      if (kb < 0) continue;
+      const int bB = (int)start[kb], eB = (int)start[kb + 1];
+      if (bB == eB || cellcore[bB] == 0) continue;
+      if (uf_find(parent, b) == uf_find(parent, bB)) continue;
+      bool found = false;
+      for (int qb = bB; qb < eB && !found; qb += 32) {
+        const int q = qb + lane;
+        const bool valid = q < eB && core[q];
+        Cand<D, F32> c;
+        if (valid) load_cand<D, F32>(c, X, Xf, n, q);
+        for (int a = b; a < e && !found; ++a) {
+          if (!core[a]) continue;
+          double ax[D];
+          float af[D];
+#pragma unroll
+          for (int k = 0; k < D; ++k) {
+            ax[k] = X[k * n + a];
+            if (F32) af[k] = Xf[k * n + a];
+          }
+          bool hit = valid && link_test<D, F32>(ax, af, c, X, n, q, P, t);
+          found = __any_sync(kFull, hit);
+        }
+      }
+      if (found && lane == 0) uf_union(parent, cellmin, b, bB);
+      __syncwarp();
+    }
+  }
+  flush_tally(t, ctr);
+}
+
+// parent[b] <- root; roots flag their component's smallest core index
+__global__ void k_roots(const int* __restrict__ reps, const uint32_t* __restrict__ Mdev,
+                        const int* __restrict__ cellcore, const int* __restrict__ cellmin,
+                        int* parent, uint32_t* __restrict__ Fmark) {
+  const int64_t M = *Mdev;
+  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
+       m += (int64_t)gridDim.x * blockDim.x) {
+    const int b = reps[m];
+    if (cellcore[b] == 0) continue;
+    const int r = uf_find(parent, b);
+    if (r == b) Fmark[cellmin[b]] = 1u;
+  }
+}
+
+__global__ void k_compress(const int* __restrict__ reps, const uint32_t* __restrict__ Mdev,
+                           const int* __restrict__ cellcore, int* parent) {
+  const int64_t M = *Mdev;
+  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
+       m += (int64_t)gridDim.x * blockDim.x) {
+    const int b = reps[m];
+    if (cellcore[b] == 0) continue;
+    parent[b] = uf_find(parent, b);
+  }
+}
+
+// Cluster id of every cell with core points (ordered by smallest core index:
+// Fscan is the exclusive scan of the root marks over original indices), and the
+// provisional label of every point: its cluster if core, NOISE otherwise.
+__global__ void k_label(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ start,
+                        int64_t n, const uint8_t* __restrict__ core,
+                        const int* __restrict__ cellcore, const int* __restrict__ cellmin,
+                        const int* __restrict__ parent, const uint32_t* __restrict__ Fscan,
+                        int* __restrict__ cellcid, int* __restrict__ lab) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int b = (int)start[keys[i]];
+    int cl = INT_MAX;
+    if (cellcore[b] > 0) cl = (int)Fscan[cellmin[parent[b]]];
+    if (i == b) cellcid[b] = cl;
+    lab[i] = core[i] ? cl : kNoise;
+  }
+}
+
+// Border points: one warp per cell with non-core points (only non-dense cells
+// have any).  Each staged non-core point takes the smallest cluster id among
+// the cells whose core points have it in their neighbourhood (centre = the core
+// point, as the reference's expansion queries from the core point).
+template <int D, bool F32>
+__global__ void __launch_bounds__(kCellThreads)
+k_border(const DevParams* __restrict__ Pp, const uint32_t* __restrict__ keys,
+         const int* __restrict__ reps, const uint32_t* __restrict__ Mdev,
+         const uint32_t* __restrict__ start, const double* __restrict__ X,
+         const float* __restrict__ Xf, int64_t n, const uint8_t* __restrict__ core,
+         const int* __restrict__ cellcore, const int* __restrict__ cellcid,
+         int* __restrict__ lab, unsigned long long* ctr) {
+  __shared__ DevParams sP;
+  __shared__ WarpStage<D> stage[kWarpsPerBlock];
+  __shared__ int sIdx[kWarpsPerBlock][32];
+  if (threadIdx.x == 0) sP = *Pp;
+  __syncthreads();
+  const DevParams& P = sP;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  WarpStage<D>& S = stage[w];
+  const int64_t M = *Mdev;
+  const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
+  constexpr int NT = D == 3 ? 125 : 25;
+  Tally t;
+  for (int64_t m = (int64_t)blockIdx.x * kWarpsPerBlock + w; m < M; m += W) {
+    const int b = reps[m], e = reps[m + 1];
+    if (cellcore[b] == e - b) continue;  // no non-core point here
+    const CellXYZ<D> cc = decompose<D>(keys[b], P);
+    for (int c0 = b; c0 < e; c0 += 32) {
+      // stage this chunk's non-core points
+      const int i = c0 + lane;
+      const bool nc = i < e && !core[i];
+      const unsigned ncm = __ballot_sync(kFull, nc);
+      const int na = __popc(ncm);
+      if (na == 0) continue;
+      if (nc) {
+        const int slot = __popc(ncm & ((1u << lane) - 1u));
+        sIdx[w][slot] = i;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+          S.x[slot][k] = X[k * n + i];
+          if (F32) S.f[slot][k] = Xf[k * n + i];
+        }
+      }
+      __syncwarp();
+      int best = INT_MAX;  // lane j < na: best cluster of staged point j
+      for (int tt = 0; tt < NT; ++tt) {
+        int ox, oy, oz;
+        if (D == 2) { ox = tt / 5 - 2; oy = tt % 5 - 2; oz = 0; }
+        else { ox = tt / 25 - 2; oy = (tt / 5) % 5 - 2; oz = tt % 5 - 2; }
+        const int64_t kb = offset_key<D>(cc, ox, oy, oz, P);
+        if (kb < 0) continue;
+        const int bB = (int)start[kb], eB = (int)start[kb + 1];
+        if (bB == eB || cellcore[bB] == 0) continue;
+        const int cB = cellcid[bB];
+        // can any staged point still improve?
+        const bool want = lane < na && cB < best;
+        unsigned wantm = __ballot_sync(kFull, want);
+        if (!wantm) continue;
+        for (int qb = bB; qb < eB && wantm; qb += 32) {
+          const int q = qb + lane;
+          const bool valid = q < eB && core[q];
+          Cand<D, F32> c;
+          if (valid) load_cand<D, F32>(c, X, Xf, n, q);
+          unsigned pending = wantm;
+          while (pending) {
+            const int j = __ffs(pending) - 1;
+            pending &= pending - 1;
+            bool hit = valid && pair_test<D, F32>(S.x[j], S.f[j], c, X, n, q, false, P, t);
+            if (__any_sync(kFull, hit)) {
+              if (lane == j) best = cB;
+              wantm &= ~(1u << j);
+            }
+          }
+        }
+      }
+      if (lane < na) lab[sIdx[w][lane]] = best == INT_MAX ? kNoise : best;
+      __syncwarp();
+    }
+  }
+  flush_tally(t, ctr);
+}
+
+// labels back to the caller's point order; counts
+__global__ void k_scatter_labels(const int* __restrict__ lab, const uint8_t* __restrict__ core,
+                                 const uint32_t* __restrict__ ids, int64_t n,
+                                 int* __restrict__ out, uint8_t* __restrict__ core_out,
+                                 unsigned long long* ctr) {
+  unsigned long long nn = 0, nc = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t j = ids[i];
+    const int l = lab[i];
+    out[j] = l;
+    if (core_out) core_out[j] = core[i];
+    nn += l == kNoise;
+    nc += core[i];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    nn += __shfl_xor_sync(kFull, nn, o);
+    nc += __shfl_xor_sync(kFull, nc, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (nn) atomicAdd(ctr + kCtrNoise, nn);
+    if (nc) atomicAdd(ctr + kCtrCore, nc);
+  }
+}
+
+}  // namespace gd
+
+// ------------------------------------------------------------------ launchers
+#include "gd_launch.h"
+
+namespace gdl {
+
+using namespace gd;
+
+static int grid_for(int64_t work, int threads, int sms, int per_sm) {
+  int64_t g = (work + threads - 1) / threads;
+  int64_t cap = (int64_t)sms * per_sm;
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  return (int)g;
+}
+
+void bbox(const double* pts, int64_t n, int dim, double* partial, int nblocks, int* flags,
+          cudaStream_t s) {
+  if (dim == 2) k_bbox_partial<2><<<nblocks, kBboxThreads, 0, s>>>(pts, n, partial, flags);
+  else k_bbox_partial<3><<<nblocks, kBboxThreads, 0, s>>>(pts, n, partial, flags);
+}
+
+void params(const double* partial, int nblocks, int dim, DevParams* P, double eps, int minpts,
+            double cell_mult, uint64_t max_cells, const int* flags, cudaStream_t s) {
+  if (dim == 2) k_params<2><<<1, 32, 0, s>>>(partial, nblocks, P, eps, minpts, cell_mult, max_cells, flags);
+  else k_params<3><<<1, 32, 0, s>>>(partial, nblocks, P, eps, minpts, cell_mult, max_cells, flags);
+}
+
+void keys(const double* pts, int64_t n, int dim, const DevParams* P, uint32_t* keys, int sms,
+          cudaStream_t s) {
+  int g = grid_for(n, 256, sms, 8);
+  if (dim == 2) k_keys<2><<<g, 256, 0, s>>>(pts, n, P, keys);
+  else k_keys<3><<<g, 256, 0, s>>>(pts, n, P, keys);
+}
+
+void gather(const double* pts, const uint32_t* ids, int64_t n, int dim, bool f32,
+            const DevParams* P, double* X, float* Xf, int sms, cudaStream_t s) {
+  int g = grid_for(n, 256, sms, 8);
+  if (dim == 2) {
+    if (f32) k_gather<2, true><<<g, 256, 0, s>>>(pts, ids, n, P, X, Xf);
+    else k_gather<2, false><<<g, 256, 0, s>>>(pts, ids, n, P, X, Xf);
+  } else {
+    if (f32) k_gather<3, true><<<g, 256, 0, s>>>(pts, ids, n, P, X, Xf);
+    else k_gather<3, false><<<g, 256, 0, s>>>(pts, ids, n, P, X, Xf);
+  }
+}
+
+void run_flags(const uint32_t* keys, int64_t n, uint32_t* fl, int sms, cudaStream_t s) {
+  k_run_flags<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(keys, n, fl);
+}
+
+void run_scatter(const uint32_t* fl, const uint32_t* pos, int64_t n, int* reps,
+                 const uint32_t* Mdev, unsigned long long* ctr, int sms, cudaStream_t s) {
+  k_run_scatter<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(fl, pos, n, reps, Mdev, ctr);
+}
+
+void cell_counts(const uint32_t* keys, const int* reps, const uint32_t* Mdev, int64_t n,
+                 uint32_t* table, int sms, cudaStream_t s) {
+  k_cell_counts<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(keys, reps, Mdev, table);
+}
+
+#define GD_DISPATCH(dim, f32, KERNEL, GRID, ...)                                   \
+  do {                                                                           \
+    if (dim == 2) {                                                              \
+      if (f32) KERNEL<2, true><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);       \
+      else KERNEL<2, false><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);          \
+    } else {                                                                     \
+      if (f32) KERNEL<3, true><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);       \
+      else KERNEL<3, false><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);          \
+    }                                                                            \
+  } while (0)
+
+void core(const Bufs& B, int64_t n, int dim, bool f32, int sms, cudaStream_t s) {
+  int g = sms * 8;
+  GD_DISPATCH(dim, f32, k_core, g, B.P, B.keys, B.reps, B.M, B.start, B.X, B.Xf, n, B.ids,
+              B.core, B.cellcore, B.cellmin, B.ctr);
+}
+
+void unite(const Bufs& B, int64_t n, int dim, bool f32, int sms, cudaStream_t s) {
+  k_parent_init<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B.reps, B.M, B.parent);
+  int g = sms * 8;
+  for (int pass = 0; pass < 2; ++pass)
+    GD_DISPATCH(dim, f32, k_union, g, B.P, pass, B.keys, B.reps, B.M, B.start, B.X, B.Xf, n,
+                B.core, B.cellcore, B.cellmin, B.parent, B.ctr);
+  k_compress<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B.reps, B.M, B.cellcore, B.parent);
+}
+
+void roots(const Bufs& B, int64_t n, int sms, cudaStream_t s) {
+  k_roots<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B.reps, B.M, B.cellcore, B.cellmin,
+                                                   B.parent, B.Fmark);
+}
+
+void label(const Bufs& B, int64_t n, int sms, cudaStream_t s) {
+  k_label<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B.keys, B.start, n, B.core, B.cellcore,
+                                                   B.cellmin, B.parent, B.Fmark, B.cellcid,
+                                                   B.lab);
+}
+
+void border(const Bufs& B, int64_t n, int dim, bool f32, int sms, cudaStream_t s) {
+  int g = sms * 8;
+  GD_DISPATCH(dim, f32, k_border, g, B.P, B.keys, B.reps, B.M, B.start, B.X, B.Xf, n, B.core,
+              B.cellcore, B.cellcid, B.lab, B.ctr);
+}
+
+void scatter_labels(const Bufs& B, int64_t n, int* out, uint8_t* core_out, int sms,
+                    cudaStream_t s) {
+  k_scatter_labels<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B.lab, B.core, B.ids, n, out,
+                                                            core_out, B.ctr);
+}
+
+}  // namespace gdl

@@ -1,0 +1,296 @@
+// gd_prims.cu -- device primitives: exclusive scan and a stable LSD radix sort.
+//
+// Both are reduce-then-scan designs: no kernel waits on another block, so no
+// spin loop exists anywhere in them.
+//
+// Scan (u32): tiles of 4096 elements (512 threads x 8 contiguous items).
+//   k_scan_reduce    tile sums                       reads 4 B/elem
+//   k_scan_partials  one block scans the tile sums
+//   k_scan_down      tile-local scan + tile offset   reads 4 B, writes 4 B/elem
+// Radix sort (u32 key, u32 value), 8-bit digits, tiles of 4096 pairs
+// (256 threads x 16 items; each warp owns a contiguous 512-element segment so
+// warp-local ranking in item order is stable):
+//   k_rs_upsweep     per-tile digit histograms       reads 4 B/pair
+//   exclusive scan over the [digit][tile] histogram
+//   k_rs_downsweep   rank in tile, regroup in shared memory, scatter
+//                                                    reads 8 B, writes 8 B/pair
+// This replaces thrust::sort_by_key (main.cu:332).
+#include "gd_internal.cuh"
+
+namespace gdprim {
+
+namespace {
+
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(gd::kFull, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
+
+// exclusive scan of one value per thread across a block of NT threads
+template <int NT>
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp,
+                                                    uint32_t* block_total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  constexpr int NW = NT / 32;
+  uint32_t inc = warp_incl_scan(v, lane);
+  if (lane == 31) s_warp[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t t = lane < NW ? s_warp[lane] : 0u;
+    uint32_t ti = warp_incl_scan(t, lane);
+    if (lane < NW) s_warp[lane] = ti - t;
+    if (lane == NW - 1 && block_total) *block_total = ti;
+  }
+  __syncthreads();
+  uint32_t r = s_warp[w] + inc - v;
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_reduce(const uint32_t* __restrict__ in, int64_t n, uint32_t* __restrict__ partial) {
+  __shared__ uint32_t s_warp[32];
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  uint32_t sum = 0;
+  if (base + kScanItems <= n) {
+    const uint4* p = reinterpret_cast<const uint4*>(in + base);
+    uint4 a = p[0], b = p[1];
+    sum = a.x + a.y + a.z + a.w + b.x + b.y + b.z + b.w;
+  } else {
+    for (int i = 0; i < kScanItems; ++i)
+      if (base + i < n) sum += in[base + i];
+  }
+  // block reduction
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(gd::kFull, sum, o);
+  if (lane == 0) s_warp[w] = sum;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t t = lane < kScanThreads / 32 ? s_warp[lane] : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(gd::kFull, t, o);
+    if (lane == 0) partial[blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(1024)
+k_scan_partials(uint32_t* partial, int64_t T, uint32_t* total_dev) {
+  __shared__ uint32_t s_warp[32];
+  __shared__ uint32_t s_total;
+  uint32_t carry = 0;
+  for (int64_t base = 0; base < T; base += 1024) {
+    int64_t i = base + threadIdx.x;
+    uint32_t v = i < T ? partial[i] : 0u;
+    uint32_t ex = block_excl_scan<1024>(v, s_warp, &s_total);
+    if (i < T) partial[i] = carry + ex;
+    __syncthreads();
+    carry += s_total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && total_dev) *total_dev = carry;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_down(const uint32_t* in, uint32_t* out, int64_t n, const uint32_t* __restrict__ partial) {
+  __shared__ uint32_t s_warp[32];
+  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  const bool full = base + kScanItems <= n;
+  if (full) {
+    const uint4* p = reinterpret_cast<const uint4*>(in + base);
+    uint4 a = p[0], b = p[1];
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+  } else {
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i) v[i] = base + i < n ? in[base + i] : 0u;
+  }
+  uint32_t s = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) s += v[i];
+  uint32_t ex = block_excl_scan<kScanThreads>(s, s_warp, nullptr) + partial[blockIdx.x];
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    uint32_t t = v[i];
+    v[i] = ex;
+    ex += t;
+  }
+  if (full) {
+    uint4* p = reinterpret_cast<uint4*>(out + base);
+    p[0] = make_uint4(v[0], v[1], v[2], v[3]);
+    p[1] = make_uint4(v[4], v[5], v[6], v[7]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < kScanItems; ++i)
+      if (base + i < n) out[base + i] = v[i];
+  }
+}
+
+// ---------------------------------------------------------------- radix sort
+constexpr int kRsThreads = 256;
+constexpr int kRsItems = 16;
+constexpr int kRsWarps = kRsThreads / 32;
+constexpr int kRsSeg = 32 * kRsItems;            // 512 elements per warp
+constexpr int kRsTile = kRsThreads * kRsItems;   // 4096 elements per tile
+constexpr int kRsBins = 256;
+
+__global__ void __launch_bounds__(kRsThreads)
+k_rs_upsweep(const uint32_t* __restrict__ keys, int64_t n, int shift,
+             uint32_t* __restrict__ hist, int64_t T) {
+  __shared__ uint32_t h[kRsBins];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t seg = (int64_t)blockIdx.x * kRsTile + w * kRsSeg;
+#pragma unroll 4
+  for (int i = 0; i < kRsItems; ++i) {
+    int64_t e = seg + i * 32 + lane;
+    bool valid = e < n;
+    uint32_t d = valid ? (__ldg(keys + e) >> shift) & 0xffu : 0x100u;
+    unsigned peers = __match_any_sync(gd::kFull, d);
+    if (valid && lane == __ffs(peers) - 1) atomicAdd(&h[d], (uint32_t)__popc(peers));
+  }
+  __syncthreads();
+  hist[(int64_t)threadIdx.x * T + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kRsThreads)
+k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+               uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, int64_t n,
+               int shift, const uint32_t* __restrict__ goff, int64_t T) {
+  __shared__ uint32_t s_keys[kRsTile];
+  __shared__ uint32_t s_vals[kRsTile];
+  __shared__ uint32_t s_cnt[kRsWarps][kRsBins];
+  __shared__ uint32_t s_dstart[kRsBins];
+  __shared__ int32_t s_gbase[kRsBins];
+  __shared__ uint32_t s_warp[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t base = (int64_t)blockIdx.x * kRsTile;
+  const int valid_count = (int)min((int64_t)kRsTile, n - base);
+  for (int i = lane; i < kRsBins; i += 32) s_cnt[w][i] = 0;
+  __syncwarp();
+  const unsigned lt_mask = (1u << lane) - 1u;
+  uint32_t k[kRsItems], v[kRsItems], r[kRsItems];
+  const int64_t seg = base + w * kRsSeg;
+#pragma unroll
+  for (int i = 0; i < kRsItems; ++i) {
+    int64_t e = seg + i * 32 + lane;
+    if (e < n) {
+      k[i] = __ldg(kin + e);
+      v[i] = vin ? __ldg(vin + e) : (uint32_t)e;
+    } else {
+      k[i] = 0xffffffffu;
+      v[i] = 0;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < kRsItems; ++i) {
+    uint32_t d = (k[i] >> shift) & 0xffu;
+    unsigned peers = __match_any_sync(gd::kFull, d);
+    uint32_t b = s_cnt[w][d];
+    __syncwarp();
+    if (lane == __ffs(peers) - 1) s_cnt[w][d] = b + (uint32_t)__popc(peers);
+    __syncwarp();
+    r[i] = b + (uint32_t)__popc(peers & lt_mask);
+  }
+  __syncthreads();
+  {
+    const int d = threadIdx.x;
+    uint32_t tot = 0;
+#pragma unroll
+    for (int ww = 0; ww < kRsWarps; ++ww) {
+      uint32_t c = s_cnt[ww][d];
+      s_cnt[ww][d] = tot;
+      tot += c;
+    }
+    uint32_t ex = block_excl_scan<kRsThreads>(tot, s_warp, nullptr);
+    s_dstart[d] = ex;
+    s_gbase[d] = (int32_t)goff[(int64_t)d * T + blockIdx.x] - (int32_t)ex;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < kRsItems; ++i) {
+    uint32_t d = (k[i] >> shift) & 0xffu;
+    uint32_t pos = s_dstart[d] + s_cnt[w][d] + r[i];
+    s_keys[pos] = k[i];
+    s_vals[pos] = v[i];
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < valid_count; j += kRsThreads) {
+    uint32_t key = s_keys[j];
+    uint32_t d = (key >> shift) & 0xffu;
+    int64_t g = (int64_t)s_gbase[d] + j;
+    kout[g] = key;
+    vout[g] = s_vals[j];
+  }
+}
+
+__global__ void k_iota(uint32_t* v, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    v[i] = (uint32_t)i;
+}
+
+inline size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+size_t scan_temp_bytes(int64_t n) {
+  int64_t T = (n + kScanTile - 1) / kScanTile;
+  return align_up((size_t)(T + 1) * sizeof(uint32_t));
+}
+
+void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, void* temp,
+                        uint32_t* total_dev, cudaStream_t s) {
+  if (n <= 0) {
+    if (total_dev) cudaMemsetAsync(total_dev, 0, sizeof(uint32_t), s);
+    return;
+  }
+  int64_t T = (n + kScanTile - 1) / kScanTile;
+  uint32_t* partial = static_cast<uint32_t*>(temp);
+  k_scan_reduce<<<(unsigned)T, kScanThreads, 0, s>>>(in, n, partial);
+  k_scan_partials<<<1, 1024, 0, s>>>(partial, T, total_dev);
+  k_scan_down<<<(unsigned)T, kScanThreads, 0, s>>>(in, out, n, partial);
+}
+
+size_t sort_temp_bytes(int64_t n) {
+  int64_t T = (n + kRsTile - 1) / kRsTile;
+  int64_t h = T * kRsBins;
+  return align_up((size_t)h * sizeof(uint32_t)) + scan_temp_bytes(h);
+}
+
+int radix_sort_pairs(uint32_t* keys[2], uint32_t* vals[2], int64_t n, int bits,
+                     bool vals_in_is_iota, void* temp, cudaStream_t s) {
+  if (n <= 0) return 0;
+  int passes = (bits + 7) / 8;
+  if (passes == 0) {
+    if (vals_in_is_iota) k_iota<<<1024, 256, 0, s>>>(vals[0], n);
+    return 0;
+  }
+  int64_t T = (n + kRsTile - 1) / kRsTile;
+  int64_t h = T * kRsBins;
+  uint32_t* hist = static_cast<uint32_t*>(temp);
+  void* scan_temp = static_cast<char*>(temp) + align_up((size_t)h * sizeof(uint32_t));
+  int cur = 0;
+  for (int p = 0; p < passes; ++p) {
+    int shift = 8 * p;
+    k_rs_upsweep<<<(unsigned)T, kRsThreads, 0, s>>>(keys[cur], n, shift, hist, T);
+    exclusive_scan_u32(hist, hist, h, scan_temp, nullptr, s);
+    const uint32_t* vin = (p == 0 && vals_in_is_iota) ? nullptr : vals[cur];
+    k_rs_downsweep<<<(unsigned)T, kRsThreads, 0, s>>>(keys[cur], vin, keys[cur ^ 1],
+                                                      vals[cur ^ 1], n, shift, hist, T);
+    cur ^= 1;
+  }
+  return cur;
+}
+
+}  // namespace gdprim

@@ -1,0 +1,162 @@
+/* gbdbscan.h -- C ABI of the GB300-native exact DBSCAN library (libgbdbscan.so).
+ *
+ * Drop-in for the DBSCAN pipeline of CUDA-DClust+ (l3lackcurtains/fast-cuda-gpu-dbscan).
+ * The reference has no library API: it is one program (main.cu) that imports a
+ * CSV, builds a grid-tree index on the GPU, expands clusters block by block and
+ * merges them on the host, with its configuration fixed at compile time in
+ * common.h.  Each entry point below names the reference code it replaces.
+ *
+ * Conventions kept from the reference:
+ *   - points are float64, row-major [n][dim] (main.cu:48-49, 137-139);
+ *   - eps and minpts mean what EPS and MINPTS mean in common.h:21-22: a point q
+ *     is a neighbour of p when |p - q|^2 <= eps^2 (p itself included), and p is
+ *     a core point when it has at least minpts neighbours;
+ *   - NOISE = -2 (common.h:8).
+ * Changed on purpose:
+ *   - labels are per point (the reference writes a sorted unique label list,
+ *     dbscan.cu:233-247) and dense: clusters are 0..K-1, numbered in the order of
+ *     their smallest core point index, border points take the smallest adjacent
+ *     cluster.  The labels equal those of the reference's exact CPU DBSCAN
+ *     (cpu-dbscan/dbscan_rtree_exp.cpp) with -1 -> -2 and k -> k-1;
+ *   - errors are returned as gd_status codes; nothing calls exit()
+ *     (the reference exits in gpuErrchk, common.h:31-40, and on a bin narrower
+ *     than eps, main.cu:204-207 -- that restriction does not exist here).
+ *
+ * Threading: a context is used by one host thread at a time.  Calls are
+ * synchronous with respect to the host (they return when results are ready)
+ * and run on the context's CUDA stream.
+ */
+#ifndef GBDBSCAN_H
+#define GBDBSCAN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GD_NOISE (-2)       /* common.h:8 */
+#define GD_ABI_VERSION 1
+
+typedef enum gd_status {
+  GD_OK = 0,
+  GD_EINVAL = 1,    /* bad argument: n < 0, dim not 2/3, eps <= 0 or not finite,
+                       minpts < 1, NaN/Inf coordinate, NULL pointer */
+  GD_ENOMEM = 2,    /* device or host allocation failed */
+  GD_ECUDA = 3,     /* CUDA runtime error (message in gd_last_error) */
+  GD_ERANGE = 4,    /* the eps-cell grid of this input exceeds the cell-table limit */
+  GD_ETIMEOUT = 5,  /* a bounded wait gave up */
+  GD_EIO = 6,       /* file could not be opened / parsed */
+  GD_ENODEV = 7,    /* no CUDA device, or the device is not sm_103 */
+  GD_ESTATE = 8     /* call out of order (e.g. gd_expand before gd_index_build) */
+} gd_status;
+
+typedef enum gd_precision {
+  GD_PREC_FP64 = 0,      /* every distance test in float64 */
+  GD_PREC_FP32_BAND = 1  /* float32 test, float64 re-test inside the proven rounding
+                            band; labels identical to GD_PREC_FP64 */
+} gd_precision;
+
+typedef struct gd_ctx gd_ctx;
+
+typedef struct gd_points {
+  const double* coords; /* n x dim float64, row-major */
+  int64_t n;
+  int32_t dim;          /* 2 or 3 (common.h:10 DIMENSION) */
+  int32_t on_device;    /* 0: host memory; 1: device memory of the context's GPU */
+} gd_points;
+
+typedef struct gd_stats {
+  int64_t n_points;
+  int64_t n_clusters;
+  int64_t n_noise;
+  int64_t n_core;
+  int64_t n_border;
+  int64_t n_cells;          /* non-empty grid cells */
+  int64_t n_dense_cells;    /* cells with >= minpts points (all core, no test) */
+  int64_t tests_fp64;       /* float64 pair evaluations */
+  int64_t tests_fp32;       /* float32 pair evaluations */
+  int64_t band_retests;     /* float32 evaluations re-tested in float64 */
+  int64_t asym_pairs;       /* core pairs that are neighbours in one direction only
+                               (possible only at the last bit of eps; see DESIGN) */
+  int64_t grid_cells;       /* cells of the dense cell table */
+  int32_t precision_used;   /* gd_precision actually run */
+  int32_t key_bits;         /* radix-sort key width */
+  int32_t launches;         /* kernel launches of the last pipeline run */
+  int32_t reserved;
+  double ms_index;          /* device time: bbox, keys, sort, cell table */
+  double ms_core;           /* device time: core flags */
+  double ms_union;          /* device time: union-find */
+  double ms_label;          /* device time: cluster ids, borders, output order */
+  double ms_total;          /* device time of the whole pipeline (without host copies) */
+  double ms_h2d;            /* host->device copy of the points (0 if on device) */
+  double ms_d2h;            /* device->host copy of the labels (0 if on device) */
+} gd_stats;
+
+/* ---- context ------------------------------------------------------------ */
+gd_status gd_ctx_create(int32_t device, gd_ctx** out);
+void gd_ctx_destroy(gd_ctx* ctx);
+/* stream: a cudaStream_t of the context's device; NULL restores the context's own */
+gd_status gd_ctx_set_stream(gd_ctx* ctx, void* stream);
+gd_status gd_ctx_set_precision(gd_ctx* ctx, int32_t precision);
+/* grid cell side = eps * mult; 0 restores the default 0.5*(1+2^-16).
+   Allowed range: (0.5, 1/sqrt(dim)) -- cells stay smaller than eps/sqrt(dim) so
+   a cell's points are mutual neighbours, and larger than eps/2 so neighbours
+   stay within +-2 cells. */
+gd_status gd_ctx_set_cell_mult(gd_ctx* ctx, double mult);
+/* Frees the context's cached device buffers (they regrow on the next call). */
+gd_status gd_ctx_trim(gd_ctx* ctx);
+
+/* ---- the pipeline, stage by stage ---------------------------------------- */
+/* Replaces main.cu:166-338: host min/max + bin widths (main.cu:166-207), the
+   per-node tree allocation (main.cu:264-305), INDEXING_STRUCTURE
+   (indexing.cu:54-118), thrust::sort_by_key (main.cu:332) and
+   INDEXING_ADJUSTMENT (indexing.cu:23-51).  Builds the eps-cell grid of the
+   points on the device; the points must stay valid until gd_expand returns. */
+gd_status gd_index_build(gd_ctx* ctx, const gd_points* pts, double eps);
+
+/* Replaces the expansion loop main.cu:369-403: MonitorSeedPoints
+   (dbscan.cu:25-187), the DBSCAN kernel (dbscan.cu:254-387) and
+   MarkAsCandidate (dbscan.cu:189-222).  Core flags, device union-find over
+   core-core links, cluster numbering and border assignment, all on the GPU. */
+gd_status gd_expand(gd_ctx* ctx, int32_t minpts);
+
+/* Replaces GetDbscanResult (dbscan.cu:225-251).  Writes per-point labels in the
+   caller's point order (host or device memory as on_device says), optional
+   per-point core flags (is_core may be NULL), and the counts the reference
+   prints (main.cu:423-424).  cluster_count / noise_count may be NULL. */
+gd_status gd_get_result(gd_ctx* ctx, int32_t* labels, uint8_t* is_core, int32_t on_device,
+                        int64_t* cluster_count, int64_t* noise_count);
+
+/* The whole pipeline in one call (main.cu:35-459 without the CSV import):
+   labels has pts->n entries in the same memory space as pts->coords.
+   stats may be NULL. */
+gd_status gd_dbscan(gd_ctx* ctx, const gd_points* pts, double eps, int32_t minpts,
+                    int32_t* labels, gd_stats* stats);
+
+/* Statistics of the last gd_expand / gd_dbscan on this context. */
+gd_status gd_get_stats(gd_ctx* ctx, gd_stats* stats);
+
+/* ---- dataset files ------------------------------------------------------- */
+/* Replaces ImportDataset (main.cu:469-498): reads a headerless CSV with dim
+   comma-separated values per line (max_points <= 0: no limit; the reference
+   stops at DATASET_COUNT).  A file ending in ".f64" is read as raw float64
+   row-major data instead.  *out is allocated here; release with gd_free. */
+gd_status gd_import_dataset(const char* path, int32_t dim, int64_t max_points, double** out,
+                            int64_t* n);
+/* Writes one label per line (the per-point form of dbscan.cu:242-247). */
+gd_status gd_write_labels(const char* path, const int32_t* labels, int64_t n);
+void gd_free(void* p);
+
+/* ---- errors -------------------------------------------------------------- */
+const char* gd_status_string(gd_status s);
+/* Message of the last failure on the calling thread ("" if none). */
+const char* gd_last_error(void);
+int32_t gd_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBDBSCAN_H */

@@ -1,0 +1,73 @@
+"""The oracle (CPU restatement) against the reference's own answers."""
+import numpy as np
+import pytest
+
+from conftest import brute_dbscan, golden_cases
+
+
+def test_ex_txt_known_answer(oracle):
+    # test-datasets/ex.txt with common.h (EPS 1.5, MINPTS 3): three collinear trios
+    ex = np.array([[1, 1], [2, 2], [3, 3], [10, 10], [11, 11], [12, 12],
+                   [20, 20], [21, 21], [22, 22]], dtype=np.float64)
+    lab, core, c = oracle.oracle_dbscan(ex, 1.5, 3)
+    assert lab.tolist() == [0, 0, 0, 1, 1, 1, 2, 2, 2]
+    assert core.tolist() == [False, True, False] * 3
+    assert c["clusters"] == 3 and c["noise"] == 0 and c["border"] == 6
+
+
+def test_oracle_matches_reference_golden(oracle):
+    n = 0
+    for name, pts, eps, mp, want in golden_cases():
+        lab, _, _ = oracle.oracle_dbscan(pts, eps, mp)
+        assert np.array_equal(lab, want), name
+        n += 1
+    assert n >= 50
+
+
+def test_one_directional_pair_uses_sequential_relabel(oracle):
+    X = [[1e-20, 0.0], [0.1, 0.0], [0.2, 0.0]]
+    Y = [[-0.3, 0.0], [-0.4, 0.0], [-0.5, 0.0]]
+    assert oracle.oracle_pred(np.array(X[0]), np.array(Y[0]), 0.3)
+    assert not oracle.oracle_pred(np.array(Y[0]), np.array(X[0]), 0.3)
+    lab, _, c = oracle.oracle_dbscan(np.array(X + Y), 0.3, 3)
+    assert lab.tolist() == [0] * 6 and c["asym_pairs"] > 0 and c["sequential"] == 1
+    lab, _, c = oracle.oracle_dbscan(np.array(Y + X), 0.3, 3)
+    assert lab.tolist() == [0, 0, 0, 1, 1, 1]
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_oracle_3d_and_2d_vs_bruteforce(oracle, seed):
+    rng = np.random.default_rng(100 + seed)
+    for d in (2, 3):
+        n = int(rng.integers(20, 300))
+        pts = np.concatenate([rng.normal(0, 0.4, (n // 2, d)), rng.uniform(-2, 2, (n - n // 2, d))])
+        if seed % 2:
+            pts = np.round(pts * 4) / 4  # many exact ties on the eps boundary
+        eps = float(rng.choice([0.25, 0.3, 0.5]))
+        mp = int(rng.integers(1, 10))
+        lab, _, _ = oracle.oracle_dbscan(pts, eps, mp)
+        assert np.array_equal(lab, brute_dbscan(pts, eps, mp)), (d, n, eps, mp)
+
+
+def test_oracle_rejects_bad_input(oracle):
+    with pytest.raises(ValueError):
+        oracle.oracle_dbscan(np.array([[0.0, np.nan]]), 1.0, 1)
+    with pytest.raises(ValueError):
+        oracle.oracle_dbscan(np.zeros((3, 2)), 0.0, 1)
+    with pytest.raises(ValueError):
+        oracle.oracle_dbscan(np.zeros((3, 2)), 1.0, 0)
+
+
+def test_oracle_vs_live_reference(oracle):
+    """When the reference checkout is present, compare on fresh random inputs."""
+    if not oracle.ref_available():
+        pytest.skip("reference checkout not present")
+    rng = np.random.default_rng(777)
+    for _ in range(40):
+        n = int(rng.integers(10, 3000))
+        pts = rng.normal(0, 1, (n, 2)) * 10 ** rng.uniform(-2, 2)
+        eps = float(np.std(pts) * rng.uniform(0.02, 0.3))
+        mp = int(rng.integers(1, 16))
+        lab, _, _ = oracle.oracle_dbscan(pts, eps, mp)
+        ref, _ = oracle.ref_rtree_dbscan(pts, eps, mp)
+        assert np.array_equal(lab, ref)
