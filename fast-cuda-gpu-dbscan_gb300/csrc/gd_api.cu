@@ -64,7 +64,8 @@ struct gd_ctx {
   double cell_mult = 0.0;
 
   DevBuf pts, keys0, keys1, vals0, vals1, X, Xf, table, reps, runfl, runpos, core, cellcore,
-      cellmin, parent, Fmark, cellcid, lab, out, coreout, sorttemp, scantemp, partial, small;
+      cellmin, parent, Fmark, cellcid, lab, out, coreout, sorttemp, scantemp, partial, small,
+      asym, hkeys, hvals;
 
   // state of the current instance
   int stage = 0;  // 0: nothing, 1: indexed, 2: expanded
@@ -75,8 +76,10 @@ struct gd_ctx {
   bool f32 = false;
   gd::DevParams hp{};
   const double* dpts = nullptr;
-  uint32_t* skeys = nullptr;
+  void* skeys = nullptr;
   uint32_t* sids = nullptr;
+  bool sparse = false;
+  uint32_t hmask = 0;
   cudaEvent_t ev[8] = {};
   gd_stats st{};
   int bbox_blocks = 0;
@@ -100,7 +103,8 @@ struct gd_ctx {
   void free_all() {
     DevBuf* all[] = {&pts, &keys0, &keys1, &vals0, &vals1, &X, &Xf, &table, &reps, &runfl,
                      &runpos, &core, &cellcore, &cellmin, &parent, &Fmark, &cellcid, &lab,
-                     &out, &coreout, &sorttemp, &scantemp, &partial, &small};
+                     &out, &coreout, &sorttemp, &scantemp, &partial, &small, &asym, &hkeys,
+                     &hvals};
     for (DevBuf* b : all) {
       if (b->p) cudaFree(b->p);
       b->p = nullptr;
@@ -124,7 +128,12 @@ struct gd_ctx {
     B.ids = sids;
     B.reps = static_cast<int*>(reps.p);
     B.M = dM();
+    B.runfl = static_cast<uint32_t*>(runfl.p);
+    B.runpos = static_cast<uint32_t*>(runpos.p);
     B.start = static_cast<uint32_t*>(table.p);
+    B.hkeys = static_cast<unsigned long long*>(hkeys.p);
+    B.hvals = static_cast<uint32_t*>(hvals.p);
+    B.hmask = hmask;
     B.X = static_cast<double*>(X.p);
     B.Xf = static_cast<float*>(Xf.p);
     B.core = static_cast<uint8_t*>(core.p);
@@ -134,6 +143,7 @@ struct gd_ctx {
     B.Fmark = static_cast<uint32_t*>(Fmark.p);
     B.cellcid = static_cast<int*>(cellcid.p);
     B.lab = static_cast<int*>(lab.p);
+    B.asym = static_cast<int*>(asym.p);
     B.ctr = dCtr();
     return B;
   }
@@ -292,58 +302,83 @@ gd_status gd_index_build(gd_ctx* ctx, const gd_points* pts, double eps) {
   if (ctx->hp.flags & gd::kFlagNonFinite)
     return fail(GD_EINVAL, "gd_index_build: input has NaN or Inf coordinates");
   if (ctx->hp.flags & gd::kFlagGridTooLarge) {
-    char buf[256];
-    snprintf(buf, sizeof buf,
-             "gd_index_build: eps-cell grid too large (extent/eps too big for the dense "
-             "cell table, limit %llu cells)",
-             (unsigned long long)max_cells);
-    return fail(GD_ERANGE, buf);
+    return fail(GD_ERANGE,
+                "gd_index_build: eps-cell grid too large (extent/eps beyond 2^31 cells per "
+                "axis or 2^62 cells in all)");
   }
   ctx->f32 = ctx->precision == GD_PREC_FP32_BAND && ctx->hp.eps2_lo32 > 0.0f;
+  ctx->sparse = ctx->hp.sparse != 0;
   const uint64_t C = ctx->hp.C;
+  const size_t kw = ctx->sparse ? 8 : 4;  // key width
   // buffers
-  if ((st = ctx->ensure(ctx->keys0, n * 4, "keys")) != GD_OK) return st;
-  if ((st = ctx->ensure(ctx->keys1, n * 4, "keys")) != GD_OK) return st;
+  if ((st = ctx->ensure(ctx->keys0, n * kw, "keys")) != GD_OK) return st;
+  if ((st = ctx->ensure(ctx->keys1, n * kw, "keys")) != GD_OK) return st;
   if ((st = ctx->ensure(ctx->vals0, n * 4, "ids")) != GD_OK) return st;
   if ((st = ctx->ensure(ctx->vals1, n * 4, "ids")) != GD_OK) return st;
   if ((st = ctx->ensure(ctx->X, (size_t)n * D * 8, "sorted coordinates")) != GD_OK) return st;
   if (ctx->f32 && (st = ctx->ensure(ctx->Xf, (size_t)n * D * 4, "f32 coordinates")) != GD_OK)
     return st;
-  if ((st = ctx->ensure(ctx->table, (C + 1) * 4, "cell table")) != GD_OK) return st;
+  uint64_t hcap = 1024;
+  if (ctx->sparse) {
+    while (hcap < 2 * (uint64_t)n) hcap <<= 1;
+    ctx->hmask = (uint32_t)(hcap - 1);
+    if ((st = ctx->ensure(ctx->hkeys, hcap * 8, "cell hash keys")) != GD_OK) return st;
+    if ((st = ctx->ensure(ctx->hvals, hcap * 4, "cell hash values")) != GD_OK) return st;
+  } else {
+    if ((st = ctx->ensure(ctx->table, (C + 1) * 4, "cell table")) != GD_OK) return st;
+  }
   if ((st = ctx->ensure(ctx->reps, (n + 1) * 4, "cell reps")) != GD_OK) return st;
   if ((st = ctx->ensure(ctx->runfl, n * 4, "run flags")) != GD_OK) return st;
   if ((st = ctx->ensure(ctx->runpos, n * 4, "run positions")) != GD_OK) return st;
   if ((st = ctx->ensure(ctx->sorttemp, gdprim::sort_temp_bytes(n), "sort temp")) != GD_OK)
     return st;
-  size_t sc = std::max(gdprim::scan_temp_bytes(n), gdprim::scan_temp_bytes((int64_t)C + 1));
+  size_t sc = gdprim::scan_temp_bytes(n);
+  if (!ctx->sparse) sc = std::max(sc, gdprim::scan_temp_bytes((int64_t)C + 1));
   if ((st = ctx->ensure(ctx->scantemp, sc, "scan temp")) != GD_OK) return st;
   // keys and sort
-  uint32_t* kb[2] = {static_cast<uint32_t*>(ctx->keys0.p), static_cast<uint32_t*>(ctx->keys1.p)};
+  int r;
+  gdl::keys(ctx->dpts, n, D, ctx->sparse, ctx->dP(), ctx->keys0.p, ctx->sms, s);
   uint32_t* vb[2] = {static_cast<uint32_t*>(ctx->vals0.p), static_cast<uint32_t*>(ctx->vals1.p)};
-  gdl::keys(ctx->dpts, n, D, ctx->dP(), kb[0], ctx->sms, s);
-  int r = gdprim::radix_sort_pairs(kb, vb, n, ctx->hp.key_bits, true, ctx->sorttemp.p, s);
-  ctx->skeys = kb[r];
+  if (ctx->sparse) {
+    using U64 = unsigned long long;
+    U64* kb[2] = {static_cast<U64*>(ctx->keys0.p), static_cast<U64*>(ctx->keys1.p)};
+    r = gdprim::radix_sort_pairs<U64>(kb, vb, n, ctx->hp.key_bits, true, ctx->sorttemp.p, s);
+    ctx->skeys = kb[r];
+  } else {
+    uint32_t* kb[2] = {static_cast<uint32_t*>(ctx->keys0.p), static_cast<uint32_t*>(ctx->keys1.p)};
+    r = gdprim::radix_sort_pairs<uint32_t>(kb, vb, n, ctx->hp.key_bits, true, ctx->sorttemp.p, s);
+    ctx->skeys = kb[r];
+  }
   ctx->sids = vb[r];
   gdl::gather(ctx->dpts, ctx->sids, n, D, ctx->f32, ctx->dP(), static_cast<double*>(ctx->X.p),
               static_cast<float*>(ctx->Xf.p), ctx->sms, s);
-  // cell runs and the dense cell table
+  // cell runs and the cell lookup (dense table or hash of occupied cells)
   uint32_t* fl = static_cast<uint32_t*>(ctx->runfl.p);
   uint32_t* pos = static_cast<uint32_t*>(ctx->runpos.p);
-  gdl::run_flags(ctx->skeys, n, fl, ctx->sms, s);
+  gdl::run_flags(ctx->skeys, ctx->sparse, n, fl, ctx->sms, s);
   gdprim::exclusive_scan_u32(fl, pos, n, ctx->scantemp.p, ctx->dM(), s);
   gdl::run_scatter(fl, pos, n, static_cast<int*>(ctx->reps.p), ctx->dM(), ctx->dCtr(), ctx->sms, s);
-  GD_CUDA(cudaMemsetAsync(ctx->table.p, 0, (C + 1) * 4, s), "clear cell table");
-  gdl::cell_counts(ctx->skeys, static_cast<int*>(ctx->reps.p), ctx->dM(), n,
-                   static_cast<uint32_t*>(ctx->table.p), ctx->sms, s);
-  gdprim::exclusive_scan_u32(static_cast<uint32_t*>(ctx->table.p),
-                             static_cast<uint32_t*>(ctx->table.p), (int64_t)C + 1,
-                             ctx->scantemp.p, nullptr, s);
+  if (ctx->sparse) {
+    GD_CUDA(cudaMemsetAsync(ctx->hkeys.p, 0xff, hcap * 8, s), "clear cell hash");
+    gdl::hash_insert(static_cast<const unsigned long long*>(ctx->skeys),
+                     static_cast<int*>(ctx->reps.p), ctx->dM(), n,
+                     static_cast<unsigned long long*>(ctx->hkeys.p),
+                     static_cast<uint32_t*>(ctx->hvals.p), ctx->hmask, ctx->sms, s);
+  } else {
+    GD_CUDA(cudaMemsetAsync(ctx->table.p, 0, (C + 1) * 4, s), "clear cell table");
+    gdl::cell_counts(static_cast<const uint32_t*>(ctx->skeys), static_cast<int*>(ctx->reps.p),
+                     ctx->dM(), n, static_cast<uint32_t*>(ctx->table.p), ctx->sms, s);
+    gdprim::exclusive_scan_u32(static_cast<uint32_t*>(ctx->table.p),
+                               static_cast<uint32_t*>(ctx->table.p), (int64_t)C + 1,
+                               ctx->scantemp.p, nullptr, s);
+  }
   cudaEventRecord(ctx->ev[2], s);
   GD_CUDA(cudaGetLastError(), "index build launch");
   {
     const int passes = (ctx->hp.key_bits + 7) / 8;
     // bbox, params, keys, sort, gather, run flags, scan, run scatter, counts, scan
-    ctx->launches = 3 + (passes ? passes * 5 : 1) + 1 + 1 + 3 + 1 + 1 + 3;
+    // bbox, params, keys, sort, gather, run flags, scan, run scatter, table or hash
+    ctx->launches = 3 + (passes ? passes * 5 : 1) + 1 + 1 + 3 + 1 + (ctx->sparse ? 1 : 4);
   }
   ctx->st.grid_cells = (int64_t)C;
   ctx->st.key_bits = ctx->hp.key_bits;
@@ -371,6 +406,7 @@ gd_status gd_expand(gd_ctx* ctx, int32_t minpts) {
   if ((st = ctx->ensure(ctx->Fmark, n * 4, "cluster marks")) != GD_OK) return st;
   if ((st = ctx->ensure(ctx->cellcid, n * 4, "cell cluster ids")) != GD_OK) return st;
   if ((st = ctx->ensure(ctx->lab, n * 4, "labels")) != GD_OK) return st;
+  if ((st = ctx->ensure(ctx->asym, gd::kAsymCap * 8, "one-directional links")) != GD_OK) return st;
   size_t sc = gdprim::scan_temp_bytes(n);
   if ((st = ctx->ensure(ctx->scantemp, std::max(sc, ctx->scantemp.bytes), "scan temp")) != GD_OK)
     return st;
@@ -382,18 +418,18 @@ gd_status gd_expand(gd_ctx* ctx, int32_t minpts) {
   gdl::Bufs B = ctx->bufs();
   const int D = ctx->dim;
   cudaEventRecord(ctx->ev[3], s);
-  gdl::core(B, n, D, ctx->f32, ctx->sms, s);
+  gdl::core(B, n, D, ctx->f32, ctx->sparse, ctx->sms, s);
   cudaEventRecord(ctx->ev[4], s);
-  gdl::unite(B, n, D, ctx->f32, ctx->sms, s);
+  gdl::unite(B, n, D, ctx->f32, ctx->sparse, ctx->sms, s);
   cudaEventRecord(ctx->ev[5], s);
   GD_CUDA(cudaMemsetAsync(B.Fmark, 0, n * 4, s), "clear marks");
   gdl::roots(B, n, ctx->sms, s);
   gdprim::exclusive_scan_u32(B.Fmark, B.Fmark, n, ctx->scantemp.p, ctx->dK(), s);
   gdl::label(B, n, ctx->sms, s);
-  gdl::border(B, n, D, ctx->f32, ctx->sms, s);
+  gdl::border(B, n, D, ctx->f32, ctx->sparse, ctx->sms, s);
   GD_CUDA(cudaGetLastError(), "expand launch");
-  // core, parent init, 2 union passes, compress, roots, scan, label, border
-  ctx->launches += 1 + 1 + 2 + 1 + 1 + 3 + 1 + 1;
+  // core, parent init, 2 union passes, compress, merge replay, roots, scan, label, border
+  ctx->launches += 1 + 1 + 2 + 1 + 1 + 1 + 3 + 1 + 1;
   ctx->stage = 2;
   return GD_OK;
 }
@@ -450,6 +486,11 @@ gd_status gd_get_result(gd_ctx* ctx, int32_t* labels, uint8_t* is_core, int32_t 
   S.tests_fp32 = (int64_t)ctr[gd::kCtrTests32];
   S.band_retests = (int64_t)ctr[gd::kCtrBand];
   S.asym_pairs = (int64_t)ctr[gd::kCtrAsym];
+  if (ctr[gd::kCtrAsymEdges] > (unsigned long long)gd::kAsymCap) {
+    ctx->stage = 1;
+    return fail(GD_ERANGE, "more one-directional core neighbour pairs than the merge replay "
+                           "holds (2048)");
+  }
   S.precision_used = ctx->f32 ? GD_PREC_FP32_BAND : GD_PREC_FP64;
   S.launches = ctx->launches;
   float ms = 0;

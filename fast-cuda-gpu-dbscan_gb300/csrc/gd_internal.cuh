@@ -2,10 +2,13 @@
 //
 // Data layout in HBM for one clustering instance of n points in d dimensions
 // (d = 2 or 3), after the index build:
-//   keys[n]   u32   fine-cell key of each point, sorted ascending
+//   keys[n]   u32   fine-cell key of each point, sorted ascending (u64 for
+//                   sparse grids)
 //   ids[n]    u32   original point index of each sorted position
 //   X[k][n]   f64   coordinate k of each sorted position (structure of arrays)
 //   start[C+1] i32  dense cell table: points of cell c are start[c]..start[c+1]
+//                   (grids up to max(2^26, 8n) cells), or, for larger (sparse)
+//                   grids, a hash of the occupied cells' 64-bit keys -> m
 //   reps[M+1] i32   sorted position of the first point of every non-empty cell
 // Per non-empty cell, indexed by its first sorted position b ("rep"):
 //   cellcore[b]  number of core points in the cell
@@ -41,10 +44,12 @@ struct DevParams {
   int32_t minpts;
   int32_t key_bits;
   int32_t flags;       // kFlag*
+  int32_t sparse;      // 1: hash of occupied cells (64-bit keys); 0: dense table
+  int32_t pad;
 };
 
 constexpr int kFlagNonFinite = 1;     // NaN or Inf coordinate
-constexpr int kFlagGridTooLarge = 2;  // cell table would exceed the limit
+constexpr int kFlagGridTooLarge = 2;  // keys would not fit 62 bits
 constexpr int kFlagNoShortcut = 4;    // |x| too large relative to eps for the
                                       // box-test shortcut / float32 filter
 
@@ -59,8 +64,18 @@ enum Counter {
   kCtrCore,             // core points
   kCtrNoise,            // noise points
   kCtrDenseCells,       // cells with >= minpts points
+  kCtrAsymEdges,        // one-directional core pairs recorded for the merge replay
   kCtrCount = 16
 };
+
+// Capacity of the list of one-directional core-core pairs (see k_asym_resolve).
+constexpr int kAsymCap = 2048;
+
+// Hash of occupied cells (sparse grids): open addressing, linear probing.
+constexpr unsigned long long kHashEmpty = ~0ull;
+__host__ __device__ __forceinline__ uint32_t hash_key(unsigned long long k) {
+  return (uint32_t)((k * 0x9E3779B97F4A7C15ull) >> 32);
+}
 
 // ---- float64 predicate, bit-exact with the reference's CPU DBSCAN ----------
 // Neighbour test with centre p and candidate q: the query box
@@ -142,12 +157,14 @@ size_t scan_temp_bytes(int64_t n);
 // (device pointer, may be null).
 void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, void* temp,
                         uint32_t* total_dev, cudaStream_t s);
-// temp bytes needed by radix_sort_pairs for n elements
+// temp bytes needed by radix_sort_pairs for n elements (either key width)
 size_t sort_temp_bytes(int64_t n);
-// Stable LSD radix sort of (key, value) pairs on the low `bits` key bits.
-// keys/vals: ping-pong buffers [0] and [1]; input in [0].  If vals_in_is_iota,
-// vals[0] is not read and the values are taken as 0..n-1.  Returns the index
-// (0 or 1) of the buffer that holds the result.
-int radix_sort_pairs(uint32_t* keys[2], uint32_t* vals[2], int64_t n, int bits,
-                     bool vals_in_is_iota, void* temp, cudaStream_t s);
+// Stable LSD radix sort of (key, value) pairs on the low `bits` key bits,
+// K = uint32_t or unsigned long long.  keys/vals: ping-pong buffers [0] and
+// [1]; input in [0].  If vals_in_is_iota, vals[0] is not read and the values
+// are taken as 0..n-1.  Returns the index (0 or 1) of the buffer that holds the
+// result.
+template <class K>
+int radix_sort_pairs(K* keys[2], uint32_t* vals[2], int64_t n, int bits, bool vals_in_is_iota,
+                     void* temp, cudaStream_t s);
 }  // namespace gdprim

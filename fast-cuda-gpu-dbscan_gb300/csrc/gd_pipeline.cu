@@ -28,6 +28,7 @@
 #include <climits>
 
 #include "gd_internal.cuh"
+#include "gd_launch.h"
 
 namespace gd {
 
@@ -102,12 +103,14 @@ __global__ void k_params(const double* __restrict__ partial, int nblocks, DevPar
   uint64_t C = 1;
   for (int k = 0; k < D; ++k) {
     double t = floor(__dmul_rn(__dsub_rn(p.hi[k], p.lo[k]), p.inv_f)) + 1.0;
-    if (!(t < 4294967296.0)) { fl |= kFlagGridTooLarge; t = 1.0; }
+    if (!(t < 2147483648.0)) { fl |= kFlagGridTooLarge; t = 1.0; }
     p.G[k] = (int64_t)t;
     cells *= t;
     C *= (uint64_t)p.G[k];
   }
-  if (cells > (double)max_cells || C > max_cells) fl |= kFlagGridTooLarge;
+  // keys must fit 62 bits; a grid beyond the dense-table limit uses the hash
+  if (!(cells < 4.0e18)) fl |= kFlagGridTooLarge;
+  p.sparse = (cells > (double)max_cells || C > max_cells) ? 1 : 0;
   p.C = C;
   int bits = 0;
   while (bits < 63 && (C - 1) >> bits) ++bits;
@@ -124,7 +127,18 @@ __global__ void k_params(const double* __restrict__ partial, int nblocks, DevPar
     p.eps2_in = -1.0;
     fl |= kFlagNoShortcut;
   }
-  // float32 band: see the derivation in the file header of gd_api.cu
+  // float32 band.  a_k = fl32(x_k - c_k) is off from x_k - c_k by at most
+  // ea = R 2^-24 (R bounds |x_k - c_k|).  For a pair with true squared distance
+  // S, the float32 value s = fl(fl(u0^2) + ...), u_k = fl32(a_pk - a_qk), obeys
+  //   |s - S| <= (S + 4 ea sqrt(D S) + 4 D ea^2)(D + 3) 2^-24
+  //              + 4 ea sqrt(D S) + 4 D ea^2  =: B(S)
+  // (coordinate error, one rounding per subtraction, D roundings in the FMA
+  // chain).  Evaluated at S = 2 eps^2 and padded by 1.5 this is bmax.  Then
+  //   s < L = eps^2 (1 - 2^-17) - bmax  =>  S < eps^2 (1 - 2^-17)
+  //        =>  float64 d2 <= eps2_in  =>  neighbour both ways (box test passes);
+  //   s > H = eps^2 (1 + 2^-17) + bmax  =>  float64 d2 > eps2  =>  not a neighbour.
+  // L is rounded down and H up to float32.  Pairs with L <= s <= H take the
+  // float64 predicate.  The filter is off (fp64 only) when the bound is not small.
   {
     const double u32 = 1.0 / 16777216.0;               // 2^-24
     R = R * (1.0 + 1e-12) + 1e-300;
@@ -146,9 +160,9 @@ __global__ void k_params(const double* __restrict__ partial, int nblocks, DevPar
 }
 
 // ------------------------------------------------------------------ keys
-template <int D>
+template <int D, class Key>
 __global__ void k_keys(const double* __restrict__ pts, int64_t n, const DevParams* __restrict__ Pp,
-                       uint32_t* __restrict__ keys) {
+                       Key* __restrict__ keys) {
   const DevParams P = *Pp;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -160,7 +174,7 @@ __global__ void k_keys(const double* __restrict__ pts, int64_t n, const DevParam
       g = g < 0 ? 0 : (g >= P.G[k] ? P.G[k] - 1 : g);
       key = key * (uint64_t)P.G[k] + (uint64_t)g;
     }
-    keys[i] = (uint32_t)key;
+    keys[i] = (Key)key;
   }
 }
 
@@ -184,7 +198,8 @@ __global__ void k_gather(const double* __restrict__ pts, const uint32_t* __restr
   }
 }
 
-__global__ void k_run_flags(const uint32_t* __restrict__ keys, int64_t n, uint32_t* __restrict__ fl) {
+template <class Key>
+__global__ void k_run_flags(const Key* __restrict__ keys, int64_t n, uint32_t* __restrict__ fl) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     fl[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
@@ -212,6 +227,27 @@ __global__ void k_cell_counts(const uint32_t* __restrict__ keys, const int* __re
   }
 }
 
+// sparse grids: hash of the occupied cells, key -> cell index m
+__global__ void k_hash_insert(const unsigned long long* __restrict__ keys,
+                              const int* __restrict__ reps, const uint32_t* __restrict__ Mdev,
+                              unsigned long long* __restrict__ hkeys, uint32_t* __restrict__ hvals,
+                              uint32_t mask) {
+  const int64_t M = *Mdev;
+  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
+       m += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned long long k = keys[reps[m]];
+    uint32_t h = hash_key(k) & mask;
+    for (uint32_t probe = 0; probe <= mask; ++probe) {
+      unsigned long long prev = atomicCAS(hkeys + h, kHashEmpty, k);
+      if (prev == kHashEmpty || prev == k) {
+        hvals[h] = (uint32_t)m;
+        break;
+      }
+      h = (h + 1) & mask;
+    }
+  }
+}
+
 // ------------------------------------------------------------- cell helpers
 template <int D>
 struct CellXYZ {
@@ -219,7 +255,7 @@ struct CellXYZ {
 };
 
 template <int D>
-__device__ __forceinline__ CellXYZ<D> decompose(uint32_t key, const DevParams& P) {
+__device__ __forceinline__ CellXYZ<D> decompose(uint64_t key, const DevParams& P) {
   CellXYZ<D> r;
   uint64_t k = key;
   if (D == 3) {
@@ -322,8 +358,9 @@ __device__ __forceinline__ bool pair_test(const double* sx, const float* sf, con
 // directions; counts pairs that are neighbours in exactly one direction.
 template <int D, bool F32>
 __device__ __forceinline__ bool link_test(const double* sx, const float* sf, const Cand<D, F32>& c,
-                                          const double* __restrict__ X, int64_t n, int64_t q,
-                                          const DevParams& P, Tally& t) {
+                                          const double* __restrict__ X, int64_t n, int a, int q,
+                                          const DevParams& P, Tally& t,
+                                          int* __restrict__ asym_list, unsigned long long* ctr) {
   double qx[D];
   if (F32) {
     ++t.t32;
@@ -342,7 +379,16 @@ __device__ __forceinline__ bool link_test(const double* sx, const float* sf, con
   if (d2 <= P.eps2_in) return true;
   if (!(d2 <= P.eps2)) return false;
   bool f = box_f64<D>(sx, qx, P.eps), b = box_f64<D>(qx, sx, P.eps);
-  if (f != b) ++t.asym;
+  if (f != b) {
+    // q is a neighbour of a but not a of q (f), or the reverse: a directed
+    // link that the merge replay (k_asym_resolve) needs.
+    ++t.asym;
+    unsigned long long slot = atomicAdd(ctr + kCtrAsymEdges, 1ull);
+    if (slot < (unsigned long long)kAsymCap) {
+      asym_list[2 * slot] = f ? a : q;
+      asym_list[2 * slot + 1] = f ? q : a;
+    }
+  }
   return f && b;
 }
 
@@ -373,44 +419,101 @@ __device__ __forceinline__ int warp_min_i32(int v) {
 constexpr int kWarpsPerBlock = 8;
 constexpr int kCellThreads = kWarpsPerBlock * 32;
 
+// Cell lookup.  Dense grids: the cell table gives every cell's point range.
+// Sparse grids: a hash of the occupied cells' keys gives the cell index m, and
+// reps[m]..reps[m+1] its points.  The probe loop is bounded by the table size.
+template <bool SPARSE>
+struct GridView {
+  const uint32_t* start;
+  const unsigned long long* hkeys;
+  const uint32_t* hvals;
+  const int* reps;
+  uint32_t hmask;
+
+  __device__ __forceinline__ int find(uint64_t k) const {
+    uint32_t h = hash_key(k) & hmask;
+    for (uint32_t probe = 0; probe <= hmask; ++probe) {
+      unsigned long long kk = hkeys[h];
+      if (kk == k) return (int)hvals[h];
+      if (kk == kHashEmpty) return -1;
+      h = (h + 1) & hmask;
+    }
+    return -1;
+  }
+  // points of cell k: [x, y)
+  __device__ __forceinline__ int2 cell(uint64_t k) const {
+    if (!SPARSE) return make_int2((int)start[k], (int)start[k + 1]);
+    int m = find(k);
+    return m < 0 ? make_int2(0, 0) : make_int2(reps[m], reps[m + 1]);
+  }
+  // points of the cells k0..k1 (consecutive keys along one row): one contiguous
+  // range, because no other key sorts between them
+  __device__ __forceinline__ int2 span(uint64_t k0, uint64_t k1) const {
+    if (!SPARSE) return make_int2((int)start[k0], (int)start[k1 + 1]);
+    int lo = INT_MAX, hi = 0;
+    for (uint64_t k = k0; k <= k1; ++k) {
+      int m = find(k);
+      if (m >= 0) {
+        lo = min(lo, reps[m]);
+        hi = max(hi, reps[m + 1]);
+      }
+    }
+    return lo == INT_MAX ? make_int2(0, 0) : make_int2(lo, hi);
+  }
+};
+
+template <bool SPARSE>
+__host__ __device__ __forceinline__ GridView<SPARSE> view_of(const gdl::Bufs& B) {
+  return GridView<SPARSE>{B.start, B.hkeys, B.hvals, B.reps, B.hmask};
+}
+
+template <bool SPARSE>
+__device__ __forceinline__ uint64_t key_at(const gdl::Bufs& B, int64_t i) {
+  if (SPARSE) return static_cast<const unsigned long long*>(B.keys)[i];
+  return static_cast<const uint32_t*>(B.keys)[i];
+}
+
+// first sorted position (rep) of the cell holding sorted position i
+__device__ __forceinline__ int rep_of(const gdl::Bufs& B, int64_t i) {
+  return B.reps[B.runpos[i] + B.runfl[i] - 1];
+}
+
+
 // ------------------------------------------------------------- core flags
 // One warp per non-empty cell.  Dense cells are all core.  Otherwise every point
 // p of the cell counts its neighbours: the warp streams the candidate rows (the
-// 5 cells along the last axis, merged into one contiguous range) 32 at a time,
-// one candidate per lane, and each staged p gets __ballot_sync + __popc of the
+// 5 cells along the last axis, one contiguous range) 32 at a time, one
+// candidate per lane, and each staged p gets __ballot_sync + __popc of the
 // lanes that hold a neighbour.  Stops as soon as every p has reached minpts.
-template <int D, bool F32>
-__global__ void __launch_bounds__(kCellThreads)
-k_core(const DevParams* __restrict__ Pp, const uint32_t* __restrict__ keys,
-       const int* __restrict__ reps, const uint32_t* __restrict__ Mdev,
-       const uint32_t* __restrict__ start, const double* __restrict__ X,
-       const float* __restrict__ Xf, int64_t n, const uint32_t* __restrict__ ids,
-       uint8_t* __restrict__ core, int* __restrict__ cellcore, int* __restrict__ cellmin,
-       unsigned long long* ctr) {
+template <int D, bool F32, bool SPARSE>
+__global__ void __launch_bounds__(kCellThreads) k_core(const gdl::Bufs B, int64_t n) {
   __shared__ DevParams sP;
   __shared__ WarpStage<D> stage[kWarpsPerBlock];
-  if (threadIdx.x == 0) sP = *Pp;
+  if (threadIdx.x == 0) sP = *B.P;
   __syncthreads();
   const DevParams& P = sP;
+  const GridView<SPARSE> gv = view_of<SPARSE>(B);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   WarpStage<D>& S = stage[w];
-  const int64_t M = *Mdev;
+  const double* __restrict__ X = B.X;
+  const float* __restrict__ Xf = B.Xf;
+  const int64_t M = *B.M;
   const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
   Tally t;
   unsigned long long dense = 0;
   for (int64_t m = (int64_t)blockIdx.x * kWarpsPerBlock + w; m < M; m += W) {
-    const int b = reps[m], e = reps[m + 1], sz = e - b;
+    const int b = B.reps[m], e = B.reps[m + 1], sz = e - b;
     if (sz >= P.minpts) {
       int mn = INT_MAX;
       for (int i = b + lane; i < e; i += 32) {
-        core[i] = 1;
-        mn = min(mn, (int)ids[i]);
+        B.core[i] = 1;
+        mn = min(mn, (int)B.ids[i]);
       }
       mn = warp_min_i32(mn);
-      if (lane == 0) { cellcore[b] = sz; cellmin[b] = mn; ++dense; }
+      if (lane == 0) { B.cellcore[b] = sz; B.cellmin[b] = mn; ++dense; }
       continue;
     }
-    const CellXYZ<D> cc = decompose<D>(keys[b], P);
+    const CellXYZ<D> cc = decompose<D>(key_at<SPARSE>(B, b), P);
     const int64_t Gl = P.G[D - 1];
     const int64_t cl = cc.c[D - 1];
     const int64_t l0 = cl - 2 < 0 ? 0 : cl - 2;
@@ -432,14 +535,13 @@ k_core(const DevParams* __restrict__ Pp, const uint32_t* __restrict__ keys,
       for (int r = 0; r < nrows && !done; ++r) {
         const int ox = kRowOrder[D == 3 ? r / 5 : r];
         const int oy = D == 3 ? kRowOrder[r % 5] : 0;
-        int64_t rowkey = offset_key<D>(cc, ox, D == 3 ? oy : 0, 0, P);
+        int64_t rowkey = offset_key<D>(cc, ox, oy, 0, P);
         if (rowkey < 0) continue;
         rowkey -= cl;  // key of the row's first cell
-        const int64_t qlo = start[rowkey + l0];
-        const int64_t qhi = start[rowkey + l1 + 1];
-        for (int64_t qb = qlo; qb < qhi && !done; qb += 32) {
+        const int2 rg = gv.span((uint64_t)(rowkey + l0), (uint64_t)(rowkey + l1));
+        for (int64_t qb = rg.x; qb < rg.y && !done; qb += 32) {
           const int64_t q = qb + lane;
-          const bool valid = q < qhi;
+          const bool valid = q < rg.y;
           Cand<D, F32> c;
           if (valid) load_cand<D, F32>(c, X, Xf, n, q);
           for (int j = 0; j < na; ++j) {
@@ -451,26 +553,25 @@ k_core(const DevParams* __restrict__ Pp, const uint32_t* __restrict__ keys,
         }
       }
       const bool isc = lane < na && mycnt >= P.minpts;
-      if (lane < na) core[b + c0 + lane] = isc ? 1 : 0;
-      if (isc) mn = min(mn, (int)ids[b + c0 + lane]);
+      if (lane < na) B.core[b + c0 + lane] = isc ? 1 : 0;
+      if (isc) mn = min(mn, (int)B.ids[b + c0 + lane]);
       ncore += __popc(__ballot_sync(kFull, isc));
       __syncwarp();
     }
     mn = warp_min_i32(mn);
-    if (lane == 0) { cellcore[b] = ncore; cellmin[b] = mn; }
+    if (lane == 0) { B.cellcore[b] = ncore; B.cellmin[b] = mn; }
   }
-  flush_tally(t, ctr);
-  if (lane == 0 && dense) atomicAdd(ctr + kCtrDenseCells, dense);
+  flush_tally(t, B.ctr);
+  if (lane == 0 && dense) atomicAdd(B.ctr + kCtrDenseCells, dense);
 }
 
 // ------------------------------------------------------------- union-find
-__global__ void k_parent_init(const int* __restrict__ reps, const uint32_t* __restrict__ Mdev,
-                              int* __restrict__ parent) {
-  const int64_t M = *Mdev;
+__global__ void k_parent_init(const gdl::Bufs B) {
+  const int64_t M = *B.M;
   for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
        m += (int64_t)gridDim.x * blockDim.x) {
-    int b = reps[m];
-    parent[b] = b;
+    int b = B.reps[m];
+    B.parent[b] = b;
   }
 }
 
@@ -493,44 +594,42 @@ __device__ __forceinline__ bool half_offset(int t, int pass, int& ox, int& oy, i
 // One warp per cell A with core points; for each half-stencil neighbour cell B
 // with core points in another component, look for one core-core pair that are
 // neighbours both ways (lanes over B's points, A's points broadcast) and unite.
-template <int D, bool F32>
-__global__ void __launch_bounds__(kCellThreads)
-k_union(const DevParams* __restrict__ Pp, int pass, const uint32_t* __restrict__ keys,
-        const int* __restrict__ reps, const uint32_t* __restrict__ Mdev,
-        const uint32_t* __restrict__ start, const double* __restrict__ X,
-        const float* __restrict__ Xf, int64_t n, const uint8_t* __restrict__ core,
-        const int* __restrict__ cellcore, const int* __restrict__ cellmin, int* parent,
-        unsigned long long* ctr) {
+template <int D, bool F32, bool SPARSE>
+__global__ void __launch_bounds__(kCellThreads) k_union(const gdl::Bufs B, int64_t n, int pass) {
   __shared__ DevParams sP;
-  if (threadIdx.x == 0) sP = *Pp;
+  if (threadIdx.x == 0) sP = *B.P;
   __syncthreads();
   const DevParams& P = sP;
+  const GridView<SPARSE> gv = view_of<SPARSE>(B);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t M = *Mdev;
+  const double* __restrict__ X = B.X;
+  const float* __restrict__ Xf = B.Xf;
+  const int64_t M = *B.M;
   const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
   constexpr int NT = D == 3 ? 125 : 25;
   Tally t;
   for (int64_t m = (int64_t)blockIdx.x * kWarpsPerBlock + w; m < M; m += W) {
-    const int b = reps[m];
-    if (cellcore[b] == 0) continue;
-    const int e = reps[m + 1];
-    const CellXYZ<D> cc = decompose<D>(keys[b], P);
+    const int b = B.reps[m];
+    if (B.cellcore[b] == 0) continue;
+    const int e = B.reps[m + 1];
+    const CellXYZ<D> cc = decompose<D>(key_at<SPARSE>(B, b), P);
     for (int tt = 0; tt < NT; ++tt) {
       int ox, oy, oz;
       if (!half_offset<D>(tt, pass, ox, oy, oz)) continue;
       const int64_t kb = offset_key<D>(cc, ox, oy, oz, P);
       if (kb < 0) continue;
-      const int bB = (int)start[kb], eB = (int)start[kb + 1];
-      if (bB == eB || cellcore[bB] == 0) continue;
-      if (uf_find(parent, b) == uf_find(parent, bB)) continue;
+      const int2 cb = gv.cell((uint64_t)kb);
+      const int bB = cb.x, eB = cb.y;
+      if (bB == eB || B.cellcore[bB] == 0) continue;
+      if (uf_find(B.parent, b) == uf_find(B.parent, bB)) continue;
       bool found = false;
       for (int qb = bB; qb < eB && !found; qb += 32) {
         const int q = qb + lane;
-        const bool valid = q < eB && core[q];
+        const bool valid = q < eB && B.core[q];
         Cand<D, F32> c;
         if (valid) load_cand<D, F32>(c, X, Xf, n, q);
         for (int a = b; a < e && !found; ++a) {
-          if (!core[a]) continue;
+          if (!B.core[a]) continue;
           double ax[D];
           float af[D];
 #pragma unroll
@@ -538,57 +637,125 @@ k_union(const DevParams* __restrict__ Pp, int pass, const uint32_t* __restrict__
             ax[k] = X[k * n + a];
             if (F32) af[k] = Xf[k * n + a];
           }
-          bool hit = valid && link_test<D, F32>(ax, af, c, X, n, q, P, t);
+          bool hit = valid && link_test<D, F32>(ax, af, c, X, n, a, q, P, t, B.asym, B.ctr);
           found = __any_sync(kFull, hit);
         }
       }
-      if (found && lane == 0) uf_union(parent, cellmin, b, bB);
+      if (found && lane == 0) uf_union(B.parent, B.cellmin, b, bB);
       __syncwarp();
     }
   }
-  flush_tally(t, ctr);
+  flush_tally(t, B.ctr);
 }
 
-// parent[b] <- root; roots flag their component's smallest core index
-__global__ void k_roots(const int* __restrict__ reps, const uint32_t* __restrict__ Mdev,
-                        const int* __restrict__ cellcore, const int* __restrict__ cellmin,
-                        int* parent, uint32_t* __restrict__ Fmark) {
-  const int64_t M = *Mdev;
+// Merge replay for one-directional core links.  Components of the symmetric
+// core graph are what the reference's sequential expansion produces when every
+// core-core neighbour relation is mutual.  When core a has core b in its
+// neighbourhood but not the reverse (the query box and the distance test can
+// disagree in the last bit), the reference's scan (dbscan_rtree_exp.cpp:363-404)
+// lets the cluster that expands a swallow b's component if that component is
+// still unvisited -- which depends on the order clusters open.  This kernel
+// replays exactly that order over the few components touched by such links:
+// components in order of their smallest core index; each unassigned one opens
+// a cluster that absorbs every unassigned component reachable along directed
+// links.  Absorbed roots are re-parented under the opening root.  One thread;
+// the list holds at most kAsymCap links (more is reported as an error).
+__global__ void k_asym_resolve(const gdl::Bufs B) {
+  const int* __restrict__ cellmin = B.cellmin;
+  int* parent = B.parent;
+  const int* __restrict__ asym_list = B.asym;
+  unsigned long long* ctr = B.ctr;
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  unsigned long long E = ctr[kCtrAsymEdges];
+  if (E == 0) return;
+  if (E > (unsigned long long)kAsymCap) return;  // reported by the host
+  __shared__ int from[kAsymCap], to[kAsymCap];
+  __shared__ int node[2 * kAsymCap], assigned[2 * kAsymCap];
+  int ne = 0, nv = 0;
+  for (unsigned long long i = 0; i < E; ++i) {
+    int a = asym_list[2 * i], b = asym_list[2 * i + 1];
+    int ra = uf_find(parent, rep_of(B, a));
+    int rb = uf_find(parent, rep_of(B, b));
+    if (ra == rb) continue;
+    from[ne] = ra;
+    to[ne] = rb;
+    ++ne;
+    int r2[2] = {ra, rb};
+    for (int k = 0; k < 2; ++k) {
+      bool seen = false;
+      for (int v = 0; v < nv && !seen; ++v) seen = node[v] == r2[k];
+      if (!seen) node[nv++] = r2[k];
+    }
+  }
+  // order the components by smallest core index (insertion sort, small)
+  for (int i = 1; i < nv; ++i) {
+    int x = node[i], j = i - 1;
+    while (j >= 0 && cellmin[node[j]] > cellmin[x]) { node[j + 1] = node[j]; --j; }
+    node[j + 1] = x;
+  }
+  // links as indices into the ordered node list
+  for (int e = 0; e < ne; ++e) {
+    int fi = 0, ti = 0;
+    for (int u = 0; u < nv; ++u) {
+      if (node[u] == from[e]) fi = u;
+      if (node[u] == to[e]) ti = u;
+    }
+    from[e] = fi;
+    to[e] = ti;
+  }
+  for (int v = 0; v < nv; ++v) assigned[v] = -1;
+  for (int v = 0; v < nv; ++v) {
+    if (assigned[v] >= 0) continue;
+    assigned[v] = node[v];
+    // grow the opened cluster along directed links until nothing changes
+    bool grew = true;
+    while (grew) {
+      grew = false;
+      for (int e = 0; e < ne; ++e) {
+        if (assigned[from[e]] == node[v] && assigned[to[e]] < 0) {
+          assigned[to[e]] = node[v];
+          grew = true;
+        }
+      }
+    }
+  }
+  for (int v = 0; v < nv; ++v)
+    if (assigned[v] != node[v]) parent[node[v]] = assigned[v];
+}
+
+// parent[b] <- root (full path compression)
+__global__ void k_compress(const gdl::Bufs B) {
+  const int64_t M = *B.M;
   for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
        m += (int64_t)gridDim.x * blockDim.x) {
-    const int b = reps[m];
-    if (cellcore[b] == 0) continue;
-    const int r = uf_find(parent, b);
-    if (r == b) Fmark[cellmin[b]] = 1u;
+    const int b = B.reps[m];
+    if (B.cellcore[b] == 0) continue;
+    B.parent[b] = uf_find(B.parent, b);
   }
 }
 
-__global__ void k_compress(const int* __restrict__ reps, const uint32_t* __restrict__ Mdev,
-                           const int* __restrict__ cellcore, int* parent) {
-  const int64_t M = *Mdev;
+// every root flags its component's smallest core index
+__global__ void k_roots(const gdl::Bufs B) {
+  const int64_t M = *B.M;
   for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
        m += (int64_t)gridDim.x * blockDim.x) {
-    const int b = reps[m];
-    if (cellcore[b] == 0) continue;
-    parent[b] = uf_find(parent, b);
+    const int b = B.reps[m];
+    if (B.cellcore[b] == 0) continue;
+    if (uf_find(B.parent, b) == b) B.Fmark[B.cellmin[b]] = 1u;
   }
 }
 
 // Cluster id of every cell with core points (ordered by smallest core index:
-// Fscan is the exclusive scan of the root marks over original indices), and the
-// provisional label of every point: its cluster if core, NOISE otherwise.
-__global__ void k_label(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ start,
-                        int64_t n, const uint8_t* __restrict__ core,
-                        const int* __restrict__ cellcore, const int* __restrict__ cellmin,
-                        const int* __restrict__ parent, const uint32_t* __restrict__ Fscan,
-                        int* __restrict__ cellcid, int* __restrict__ lab) {
+// Fmark now holds the exclusive scan of the root marks over original indices),
+// and the provisional label of every point: its cluster if core, NOISE otherwise.
+__global__ void k_label(const gdl::Bufs B, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const int b = (int)start[keys[i]];
+    const int b = rep_of(B, i);
     int cl = INT_MAX;
-    if (cellcore[b] > 0) cl = (int)Fscan[cellmin[parent[b]]];
-    if (i == b) cellcid[b] = cl;
-    lab[i] = core[i] ? cl : kNoise;
+    if (B.cellcore[b] > 0) cl = (int)B.Fmark[B.cellmin[uf_find(B.parent, b)]];
+    if (i == b) B.cellcid[b] = cl;
+    B.lab[i] = B.core[i] ? cl : kNoise;
   }
 }
 
@@ -596,34 +763,31 @@ __global__ void k_label(const uint32_t* __restrict__ keys, const uint32_t* __res
 // have any).  Each staged non-core point takes the smallest cluster id among
 // the cells whose core points have it in their neighbourhood (centre = the core
 // point, as the reference's expansion queries from the core point).
-template <int D, bool F32>
-__global__ void __launch_bounds__(kCellThreads)
-k_border(const DevParams* __restrict__ Pp, const uint32_t* __restrict__ keys,
-         const int* __restrict__ reps, const uint32_t* __restrict__ Mdev,
-         const uint32_t* __restrict__ start, const double* __restrict__ X,
-         const float* __restrict__ Xf, int64_t n, const uint8_t* __restrict__ core,
-         const int* __restrict__ cellcore, const int* __restrict__ cellcid,
-         int* __restrict__ lab, unsigned long long* ctr) {
+template <int D, bool F32, bool SPARSE>
+__global__ void __launch_bounds__(kCellThreads) k_border(const gdl::Bufs B, int64_t n) {
   __shared__ DevParams sP;
   __shared__ WarpStage<D> stage[kWarpsPerBlock];
   __shared__ int sIdx[kWarpsPerBlock][32];
-  if (threadIdx.x == 0) sP = *Pp;
+  if (threadIdx.x == 0) sP = *B.P;
   __syncthreads();
   const DevParams& P = sP;
+  const GridView<SPARSE> gv = view_of<SPARSE>(B);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   WarpStage<D>& S = stage[w];
-  const int64_t M = *Mdev;
+  const double* __restrict__ X = B.X;
+  const float* __restrict__ Xf = B.Xf;
+  const int64_t M = *B.M;
   const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
   constexpr int NT = D == 3 ? 125 : 25;
   Tally t;
   for (int64_t m = (int64_t)blockIdx.x * kWarpsPerBlock + w; m < M; m += W) {
-    const int b = reps[m], e = reps[m + 1];
-    if (cellcore[b] == e - b) continue;  // no non-core point here
-    const CellXYZ<D> cc = decompose<D>(keys[b], P);
+    const int b = B.reps[m], e = B.reps[m + 1];
+    if (B.cellcore[b] == e - b) continue;  // no non-core point here
+    const CellXYZ<D> cc = decompose<D>(key_at<SPARSE>(B, b), P);
     for (int c0 = b; c0 < e; c0 += 32) {
       // stage this chunk's non-core points
       const int i = c0 + lane;
-      const bool nc = i < e && !core[i];
+      const bool nc = i < e && !B.core[i];
       const unsigned ncm = __ballot_sync(kFull, nc);
       const int na = __popc(ncm);
       if (na == 0) continue;
@@ -644,16 +808,17 @@ k_border(const DevParams* __restrict__ Pp, const uint32_t* __restrict__ keys,
         else { ox = tt / 25 - 2; oy = (tt / 5) % 5 - 2; oz = tt % 5 - 2; }
         const int64_t kb = offset_key<D>(cc, ox, oy, oz, P);
         if (kb < 0) continue;
-        const int bB = (int)start[kb], eB = (int)start[kb + 1];
-        if (bB == eB || cellcore[bB] == 0) continue;
-        const int cB = cellcid[bB];
+        const int2 cb = gv.cell((uint64_t)kb);
+        const int bB = cb.x, eB = cb.y;
+        if (bB == eB || B.cellcore[bB] == 0) continue;
+        const int cB = B.cellcid[bB];
         // can any staged point still improve?
         const bool want = lane < na && cB < best;
         unsigned wantm = __ballot_sync(kFull, want);
         if (!wantm) continue;
         for (int qb = bB; qb < eB && wantm; qb += 32) {
           const int q = qb + lane;
-          const bool valid = q < eB && core[q];
+          const bool valid = q < eB && B.core[q];
           Cand<D, F32> c;
           if (valid) load_cand<D, F32>(c, X, Xf, n, q);
           unsigned pending = wantm;
@@ -668,27 +833,26 @@ k_border(const DevParams* __restrict__ Pp, const uint32_t* __restrict__ keys,
           }
         }
       }
-      if (lane < na) lab[sIdx[w][lane]] = best == INT_MAX ? kNoise : best;
+      if (lane < na) B.lab[sIdx[w][lane]] = best == INT_MAX ? kNoise : best;
       __syncwarp();
     }
   }
-  flush_tally(t, ctr);
+  flush_tally(t, B.ctr);
 }
 
 // labels back to the caller's point order; counts
-__global__ void k_scatter_labels(const int* __restrict__ lab, const uint8_t* __restrict__ core,
-                                 const uint32_t* __restrict__ ids, int64_t n,
-                                 int* __restrict__ out, uint8_t* __restrict__ core_out,
-                                 unsigned long long* ctr) {
+__global__ void k_scatter_labels(const gdl::Bufs B, int64_t n, int* __restrict__ out,
+                                 uint8_t* __restrict__ core_out) {
   unsigned long long nn = 0, nc = 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t j = ids[i];
-    const int l = lab[i];
+    const uint32_t j = B.ids[i];
+    const int l = B.lab[i];
+    const uint8_t c = B.core[i];
     out[j] = l;
-    if (core_out) core_out[j] = core[i];
+    if (core_out) core_out[j] = c;
     nn += l == kNoise;
-    nc += core[i];
+    nc += c;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -696,16 +860,14 @@ __global__ void k_scatter_labels(const int* __restrict__ lab, const uint8_t* __r
     nc += __shfl_xor_sync(kFull, nc, o);
   }
   if ((threadIdx.x & 31) == 0) {
-    if (nn) atomicAdd(ctr + kCtrNoise, nn);
-    if (nc) atomicAdd(ctr + kCtrCore, nc);
+    if (nn) atomicAdd(B.ctr + kCtrNoise, nn);
+    if (nc) atomicAdd(B.ctr + kCtrCore, nc);
   }
 }
 
 }  // namespace gd
 
 // ------------------------------------------------------------------ launchers
-#include "gd_launch.h"
-
 namespace gdl {
 
 using namespace gd;
@@ -726,15 +888,23 @@ void bbox(const double* pts, int64_t n, int dim, double* partial, int nblocks, i
 
 void params(const double* partial, int nblocks, int dim, DevParams* P, double eps, int minpts,
             double cell_mult, uint64_t max_cells, const int* flags, cudaStream_t s) {
-  if (dim == 2) k_params<2><<<1, 32, 0, s>>>(partial, nblocks, P, eps, minpts, cell_mult, max_cells, flags);
-  else k_params<3><<<1, 32, 0, s>>>(partial, nblocks, P, eps, minpts, cell_mult, max_cells, flags);
+  if (dim == 2)
+    k_params<2><<<1, 32, 0, s>>>(partial, nblocks, P, eps, minpts, cell_mult, max_cells, flags);
+  else
+    k_params<3><<<1, 32, 0, s>>>(partial, nblocks, P, eps, minpts, cell_mult, max_cells, flags);
 }
 
-void keys(const double* pts, int64_t n, int dim, const DevParams* P, uint32_t* keys, int sms,
-          cudaStream_t s) {
+void keys(const double* pts, int64_t n, int dim, bool sparse, const DevParams* P, void* keys,
+          int sms, cudaStream_t s) {
   int g = grid_for(n, 256, sms, 8);
-  if (dim == 2) k_keys<2><<<g, 256, 0, s>>>(pts, n, P, keys);
-  else k_keys<3><<<g, 256, 0, s>>>(pts, n, P, keys);
+  using U64 = unsigned long long;
+  if (dim == 2) {
+    if (sparse) k_keys<2, U64><<<g, 256, 0, s>>>(pts, n, P, static_cast<U64*>(keys));
+    else k_keys<2, uint32_t><<<g, 256, 0, s>>>(pts, n, P, static_cast<uint32_t*>(keys));
+  } else {
+    if (sparse) k_keys<3, U64><<<g, 256, 0, s>>>(pts, n, P, static_cast<U64*>(keys));
+    else k_keys<3, uint32_t><<<g, 256, 0, s>>>(pts, n, P, static_cast<uint32_t*>(keys));
+  }
 }
 
 void gather(const double* pts, const uint32_t* ids, int64_t n, int dim, bool f32,
@@ -749,8 +919,13 @@ void gather(const double* pts, const uint32_t* ids, int64_t n, int dim, bool f32
   }
 }
 
-void run_flags(const uint32_t* keys, int64_t n, uint32_t* fl, int sms, cudaStream_t s) {
-  k_run_flags<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(keys, n, fl);
+void run_flags(const void* keys, bool sparse, int64_t n, uint32_t* fl, int sms, cudaStream_t s) {
+  int g = grid_for(n, 256, sms, 8);
+  if (sparse)
+    k_run_flags<unsigned long long><<<g, 256, 0, s>>>(
+        static_cast<const unsigned long long*>(keys), n, fl);
+  else
+    k_run_flags<uint32_t><<<g, 256, 0, s>>>(static_cast<const uint32_t*>(keys), n, fl);
 }
 
 void run_scatter(const uint32_t* fl, const uint32_t* pos, int64_t n, int* reps,
@@ -763,53 +938,62 @@ void cell_counts(const uint32_t* keys, const int* reps, const uint32_t* Mdev, in
   k_cell_counts<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(keys, reps, Mdev, table);
 }
 
-#define GD_DISPATCH(dim, f32, KERNEL, GRID, ...)                                   \
-  do {                                                                           \
-    if (dim == 2) {                                                              \
-      if (f32) KERNEL<2, true><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);       \
-      else KERNEL<2, false><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);          \
-    } else {                                                                     \
-      if (f32) KERNEL<3, true><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);       \
-      else KERNEL<3, false><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);          \
-    }                                                                            \
-  } while (0)
-
-void core(const Bufs& B, int64_t n, int dim, bool f32, int sms, cudaStream_t s) {
-  int g = sms * 8;
-  GD_DISPATCH(dim, f32, k_core, g, B.P, B.keys, B.reps, B.M, B.start, B.X, B.Xf, n, B.ids,
-              B.core, B.cellcore, B.cellmin, B.ctr);
+void hash_insert(const unsigned long long* keys, const int* reps, const uint32_t* Mdev, int64_t n,
+                 unsigned long long* hkeys, uint32_t* hvals, uint32_t mask, int sms,
+                 cudaStream_t s) {
+  k_hash_insert<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(keys, reps, Mdev, hkeys, hvals, mask);
 }
 
-void unite(const Bufs& B, int64_t n, int dim, bool f32, int sms, cudaStream_t s) {
-  k_parent_init<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B.reps, B.M, B.parent);
+#define GD_DISPATCH(dim, f32, sparse, KERNEL, GRID, ...)                                    \
+  do {                                                                                      \
+    if (dim == 2) {                                                                         \
+      if (f32) {                                                                            \
+        if (sparse) KERNEL<2, true, true><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);       \
+        else KERNEL<2, true, false><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);             \
+      } else {                                                                              \
+        if (sparse) KERNEL<2, false, true><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);      \
+        else KERNEL<2, false, false><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);            \
+      }                                                                                     \
+    } else {                                                                                \
+      if (f32) {                                                                            \
+        if (sparse) KERNEL<3, true, true><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);       \
+        else KERNEL<3, true, false><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);             \
+      } else {                                                                              \
+        if (sparse) KERNEL<3, false, true><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);      \
+        else KERNEL<3, false, false><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);            \
+      }                                                                                     \
+    }                                                                                       \
+  } while (0)
+
+void core(const Bufs& B, int64_t n, int dim, bool f32, bool sparse, int sms, cudaStream_t s) {
   int g = sms * 8;
-  for (int pass = 0; pass < 2; ++pass)
-    GD_DISPATCH(dim, f32, k_union, g, B.P, pass, B.keys, B.reps, B.M, B.start, B.X, B.Xf, n,
-                B.core, B.cellcore, B.cellmin, B.parent, B.ctr);
-  k_compress<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B.reps, B.M, B.cellcore, B.parent);
+  GD_DISPATCH(dim, f32, sparse, k_core, g, B, n);
+}
+
+void unite(const Bufs& B, int64_t n, int dim, bool f32, bool sparse, int sms, cudaStream_t s) {
+  k_parent_init<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
+  int g = sms * 8;
+  for (int pass = 0; pass < 2; ++pass) GD_DISPATCH(dim, f32, sparse, k_union, g, B, n, pass);
+  k_compress<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
+  k_asym_resolve<<<1, 32, 0, s>>>(B);
 }
 
 void roots(const Bufs& B, int64_t n, int sms, cudaStream_t s) {
-  k_roots<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B.reps, B.M, B.cellcore, B.cellmin,
-                                                   B.parent, B.Fmark);
+  k_roots<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
 }
 
 void label(const Bufs& B, int64_t n, int sms, cudaStream_t s) {
-  k_label<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B.keys, B.start, n, B.core, B.cellcore,
-                                                   B.cellmin, B.parent, B.Fmark, B.cellcid,
-                                                   B.lab);
+  k_label<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
 }
 
-void border(const Bufs& B, int64_t n, int dim, bool f32, int sms, cudaStream_t s) {
+void border(const Bufs& B, int64_t n, int dim, bool f32, bool sparse, int sms, cudaStream_t s) {
   int g = sms * 8;
-  GD_DISPATCH(dim, f32, k_border, g, B.P, B.keys, B.reps, B.M, B.start, B.X, B.Xf, n, B.core,
-              B.cellcore, B.cellcid, B.lab, B.ctr);
+  GD_DISPATCH(dim, f32, sparse, k_border, g, B, n);
 }
 
 void scatter_labels(const Bufs& B, int64_t n, int* out, uint8_t* core_out, int sms,
                     cudaStream_t s) {
-  k_scatter_labels<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B.lab, B.core, B.ids, n, out,
-                                                            core_out, B.ctr);
+  k_scatter_labels<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n, out, core_out);
 }
 
 }  // namespace gdl

@@ -137,25 +137,28 @@ k_scan_down(const uint32_t* in, uint32_t* out, int64_t n, const uint32_t* __rest
 
 // ---------------------------------------------------------------- radix sort
 constexpr int kRsThreads = 256;
-constexpr int kRsItems = 16;
 constexpr int kRsWarps = kRsThreads / 32;
-constexpr int kRsSeg = 32 * kRsItems;            // 512 elements per warp
-constexpr int kRsTile = kRsThreads * kRsItems;   // 4096 elements per tile
 constexpr int kRsBins = 256;
+// items per thread: 16 for 32-bit keys (4096-pair tiles), 8 for 64-bit keys
+template <class K>
+constexpr int rs_items() { return sizeof(K) == 4 ? 16 : 8; }
+constexpr int kRsMinTile = kRsThreads * 8;
 
+template <class K, int ITEMS>
 __global__ void __launch_bounds__(kRsThreads)
-k_rs_upsweep(const uint32_t* __restrict__ keys, int64_t n, int shift,
-             uint32_t* __restrict__ hist, int64_t T) {
+k_rs_upsweep(const K* __restrict__ keys, int64_t n, int shift, uint32_t* __restrict__ hist,
+             int64_t T) {
+  constexpr int SEG = 32 * ITEMS, TILE = kRsThreads * ITEMS;
   __shared__ uint32_t h[kRsBins];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   h[threadIdx.x] = 0;
   __syncthreads();
-  const int64_t seg = (int64_t)blockIdx.x * kRsTile + w * kRsSeg;
+  const int64_t seg = (int64_t)blockIdx.x * TILE + w * SEG;
 #pragma unroll 4
-  for (int i = 0; i < kRsItems; ++i) {
+  for (int i = 0; i < ITEMS; ++i) {
     int64_t e = seg + i * 32 + lane;
     bool valid = e < n;
-    uint32_t d = valid ? (__ldg(keys + e) >> shift) & 0xffu : 0x100u;
+    uint32_t d = valid ? (uint32_t)(__ldg(keys + e) >> shift) & 0xffu : 0x100u;
     unsigned peers = __match_any_sync(gd::kFull, d);
     if (valid && lane == __ffs(peers) - 1) atomicAdd(&h[d], (uint32_t)__popc(peers));
   }
@@ -163,38 +166,41 @@ k_rs_upsweep(const uint32_t* __restrict__ keys, int64_t n, int shift,
   hist[(int64_t)threadIdx.x * T + blockIdx.x] = h[threadIdx.x];
 }
 
+template <class K, int ITEMS>
 __global__ void __launch_bounds__(kRsThreads)
-k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
-               uint32_t* __restrict__ kout, uint32_t* __restrict__ vout, int64_t n,
+k_rs_downsweep(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
+               K* __restrict__ kout, uint32_t* __restrict__ vout, int64_t n,
                int shift, const uint32_t* __restrict__ goff, int64_t T) {
-  __shared__ uint32_t s_keys[kRsTile];
-  __shared__ uint32_t s_vals[kRsTile];
+  constexpr int SEG = 32 * ITEMS, TILE = kRsThreads * ITEMS;
+  __shared__ K s_keys[TILE];
+  __shared__ uint32_t s_vals[TILE];
   __shared__ uint32_t s_cnt[kRsWarps][kRsBins];
   __shared__ uint32_t s_dstart[kRsBins];
   __shared__ int32_t s_gbase[kRsBins];
   __shared__ uint32_t s_warp[32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int64_t base = (int64_t)blockIdx.x * kRsTile;
-  const int valid_count = (int)min((int64_t)kRsTile, n - base);
+  const int64_t base = (int64_t)blockIdx.x * TILE;
+  const int valid_count = (int)min((int64_t)TILE, n - base);
   for (int i = lane; i < kRsBins; i += 32) s_cnt[w][i] = 0;
   __syncwarp();
   const unsigned lt_mask = (1u << lane) - 1u;
-  uint32_t k[kRsItems], v[kRsItems], r[kRsItems];
-  const int64_t seg = base + w * kRsSeg;
+  K k[ITEMS];
+  uint32_t v[ITEMS], r[ITEMS];
+  const int64_t seg = base + w * SEG;
 #pragma unroll
-  for (int i = 0; i < kRsItems; ++i) {
+  for (int i = 0; i < ITEMS; ++i) {
     int64_t e = seg + i * 32 + lane;
     if (e < n) {
       k[i] = __ldg(kin + e);
       v[i] = vin ? __ldg(vin + e) : (uint32_t)e;
     } else {
-      k[i] = 0xffffffffu;
+      k[i] = ~(K)0;
       v[i] = 0;
     }
   }
 #pragma unroll
-  for (int i = 0; i < kRsItems; ++i) {
-    uint32_t d = (k[i] >> shift) & 0xffu;
+  for (int i = 0; i < ITEMS; ++i) {
+    uint32_t d = (uint32_t)(k[i] >> shift) & 0xffu;
     unsigned peers = __match_any_sync(gd::kFull, d);
     uint32_t b = s_cnt[w][d];
     __syncwarp();
@@ -218,16 +224,16 @@ k_rs_downsweep(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vi
   }
   __syncthreads();
 #pragma unroll
-  for (int i = 0; i < kRsItems; ++i) {
-    uint32_t d = (k[i] >> shift) & 0xffu;
+  for (int i = 0; i < ITEMS; ++i) {
+    uint32_t d = (uint32_t)(k[i] >> shift) & 0xffu;
     uint32_t pos = s_dstart[d] + s_cnt[w][d] + r[i];
     s_keys[pos] = k[i];
     s_vals[pos] = v[i];
   }
   __syncthreads();
   for (int j = threadIdx.x; j < valid_count; j += kRsThreads) {
-    uint32_t key = s_keys[j];
-    uint32_t d = (key >> shift) & 0xffu;
+    K key = s_keys[j];
+    uint32_t d = (uint32_t)(key >> shift) & 0xffu;
     int64_t g = (int64_t)s_gbase[d] + j;
     kout[g] = key;
     vout[g] = s_vals[j];
@@ -263,34 +269,42 @@ void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, void* temp
 }
 
 size_t sort_temp_bytes(int64_t n) {
-  int64_t T = (n + kRsTile - 1) / kRsTile;
+  int64_t T = (n + kRsMinTile - 1) / kRsMinTile;
   int64_t h = T * kRsBins;
   return align_up((size_t)h * sizeof(uint32_t)) + scan_temp_bytes(h);
 }
 
-int radix_sort_pairs(uint32_t* keys[2], uint32_t* vals[2], int64_t n, int bits,
-                     bool vals_in_is_iota, void* temp, cudaStream_t s) {
+template <class K>
+int radix_sort_pairs(K* keys[2], uint32_t* vals[2], int64_t n, int bits, bool vals_in_is_iota,
+                     void* temp, cudaStream_t s) {
   if (n <= 0) return 0;
   int passes = (bits + 7) / 8;
   if (passes == 0) {
     if (vals_in_is_iota) k_iota<<<1024, 256, 0, s>>>(vals[0], n);
     return 0;
   }
-  int64_t T = (n + kRsTile - 1) / kRsTile;
+  constexpr int ITEMS = rs_items<K>();
+  constexpr int TILE = kRsThreads * ITEMS;
+  int64_t T = (n + TILE - 1) / TILE;
   int64_t h = T * kRsBins;
   uint32_t* hist = static_cast<uint32_t*>(temp);
   void* scan_temp = static_cast<char*>(temp) + align_up((size_t)h * sizeof(uint32_t));
   int cur = 0;
   for (int p = 0; p < passes; ++p) {
     int shift = 8 * p;
-    k_rs_upsweep<<<(unsigned)T, kRsThreads, 0, s>>>(keys[cur], n, shift, hist, T);
+    k_rs_upsweep<K, ITEMS><<<(unsigned)T, kRsThreads, 0, s>>>(keys[cur], n, shift, hist, T);
     exclusive_scan_u32(hist, hist, h, scan_temp, nullptr, s);
     const uint32_t* vin = (p == 0 && vals_in_is_iota) ? nullptr : vals[cur];
-    k_rs_downsweep<<<(unsigned)T, kRsThreads, 0, s>>>(keys[cur], vin, keys[cur ^ 1],
-                                                      vals[cur ^ 1], n, shift, hist, T);
+    k_rs_downsweep<K, ITEMS><<<(unsigned)T, kRsThreads, 0, s>>>(keys[cur], vin, keys[cur ^ 1],
+                                                                vals[cur ^ 1], n, shift, hist, T);
     cur ^= 1;
   }
   return cur;
 }
+
+template int radix_sort_pairs<uint32_t>(uint32_t* [2], uint32_t* [2], int64_t, int, bool, void*,
+                                        cudaStream_t);
+template int radix_sort_pairs<unsigned long long>(unsigned long long* [2], uint32_t* [2], int64_t,
+                                                  int, bool, void*, cudaStream_t);
 
 }  // namespace gdprim

@@ -166,3 +166,21 @@ def test_cli_end_to_end(built_lib, tmp_path, ds, oracle):
     assert f"Final cluster after merging: {c['clusters']}" in r.stdout
     assert f"Number of noises: {c['noise']}" in r.stdout
     assert np.array_equal(np.loadtxt(str(out), dtype=np.int32), olab)
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+@pytest.mark.parametrize("d", [2, 3])
+def test_sparse_grid_vs_oracle(gpu_ctx, oracle, prec, d):
+    """Far-apart blobs: the eps-cell grid exceeds the dense table and the
+    occupied cells are looked up through the hash (64-bit keys)."""
+    rng = np.random.default_rng(31 + d)
+    centres = rng.uniform(-1e5, 1e5, (6, d))
+    pts = np.concatenate([c + rng.normal(0, 0.2, (3000, d)) for c in centres] +
+                         [rng.uniform(-1e5, 1e5, (500, d))])
+    pts = pts[rng.permutation(len(pts))]
+    lab, core = run(gpu_ctx, pts, 0.05, 6, prec)
+    st = gpu_ctx.stats()
+    assert st["grid_cells"] > 10 ** 9 or st["key_bits"] > 32
+    olab, ocore, _ = oracle.oracle_dbscan(pts, 0.05, 6)
+    assert np.array_equal(core, ocore)
+    assert np.array_equal(lab, olab)
