@@ -174,9 +174,9 @@ def test_sparse_grid_vs_oracle(gpu_ctx, oracle, prec, d):
     """Far-apart blobs: the eps-cell grid exceeds the dense table and the
     occupied cells are looked up through the hash (64-bit keys)."""
     rng = np.random.default_rng(31 + d)
-    centres = rng.uniform(-1e5, 1e5, (6, d))
+    centres = rng.uniform(-1e4, 1e4, (6, d))
     pts = np.concatenate([c + rng.normal(0, 0.2, (3000, d)) for c in centres] +
-                         [rng.uniform(-1e5, 1e5, (500, d))])
+                         [rng.uniform(-1e4, 1e4, (500, d))])
     pts = pts[rng.permutation(len(pts))]
     lab, core = run(gpu_ctx, pts, 0.05, 6, prec)
     st = gpu_ctx.stats()
