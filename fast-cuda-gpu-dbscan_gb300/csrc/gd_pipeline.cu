@@ -35,32 +35,44 @@ namespace gd {
 // ------------------------------------------------------------------ bbox
 constexpr int kBboxThreads = 256;
 
+// Doubles ordered as int64 (monotone for non-NaN values): min/max run on the
+// integer pipe instead of the much slower float64 pipe of this GPU.
+__device__ __forceinline__ long long ord_of(double v) {
+  long long b = __double_as_longlong(v);
+  return b >= 0 ? b : b ^ 0x7fffffffffffffffLL;
+}
+__device__ __forceinline__ double dbl_of(long long o) {
+  return __longlong_as_double(o >= 0 ? o : o ^ 0x7fffffffffffffffLL);
+}
+
 template <int D>
 __global__ void __launch_bounds__(kBboxThreads)
-k_bbox_partial(const double* __restrict__ pts, int64_t n, double* __restrict__ partial,
+k_bbox_partial(const double* __restrict__ pts, int64_t n, long long* __restrict__ partial,
                int* __restrict__ flags) {
-  double lo[D], hi[D];
+  long long lo[D], hi[D];
 #pragma unroll
-  for (int k = 0; k < D; ++k) { lo[k] = DBL_MAX; hi[k] = -DBL_MAX; }
+  for (int k = 0; k < D; ++k) { lo[k] = LLONG_MAX; hi[k] = LLONG_MIN; }
   bool bad = false;
+  const long long* __restrict__ bits = reinterpret_cast<const long long*>(pts);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
 #pragma unroll
     for (int k = 0; k < D; ++k) {
-      double v = pts[i * D + k];
-      bad |= !isfinite(v);
-      lo[k] = fmin(lo[k], v);
-      hi[k] = fmax(hi[k], v);
+      long long bv = bits[i * D + k];
+      bad |= (bv & 0x7ff0000000000000LL) == 0x7ff0000000000000LL;
+      long long o = bv >= 0 ? bv : bv ^ 0x7fffffffffffffffLL;
+      lo[k] = min(lo[k], o);
+      hi[k] = max(hi[k], o);
     }
   }
-  __shared__ double s[2 * D][kBboxThreads / 32];
+  __shared__ long long s[2 * D][kBboxThreads / 32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < D; ++k) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      lo[k] = fmin(lo[k], __shfl_xor_sync(kFull, lo[k], o));
-      hi[k] = fmax(hi[k], __shfl_xor_sync(kFull, hi[k], o));
+      lo[k] = min(lo[k], __shfl_xor_sync(kFull, lo[k], o));
+      hi[k] = max(hi[k], __shfl_xor_sync(kFull, hi[k], o));
     }
     if (lane == 0) { s[k][w] = lo[k]; s[D + k][w] = hi[k]; }
   }
@@ -68,30 +80,48 @@ k_bbox_partial(const double* __restrict__ pts, int64_t n, double* __restrict__ p
   __syncthreads();
   if (threadIdx.x < 2 * D) {
     const int k = threadIdx.x;
-    double v = s[k][0];
-    for (int j = 1; j < kBboxThreads / 32; ++j) v = k < D ? fmin(v, s[k][j]) : fmax(v, s[k][j]);
+    long long v = s[k][0];
+    for (int j = 1; j < kBboxThreads / 32; ++j) v = k < D ? min(v, s[k][j]) : max(v, s[k][j]);
     partial[blockIdx.x * 2 * D + k] = v;
   }
 }
 
-// One thread: finish the reduction, derive the grid and the float32 band.
+// One block: reduce the partial boxes; thread 0 derives the grid and the
+// float32 band.
 template <int D>
-__global__ void k_params(const double* __restrict__ partial, int nblocks, DevParams* P,
-                         double eps, int minpts, double cell_mult, uint64_t max_cells,
-                         const int* __restrict__ flags) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__global__ void __launch_bounds__(256)
+k_params(const long long* __restrict__ partial, int nblocks, DevParams* P, double eps, int minpts,
+         double cell_mult, uint64_t max_cells, const int* __restrict__ flags) {
+  __shared__ long long s[2 * D][256];
+  long long lo[D], hi[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) { lo[k] = LLONG_MAX; hi[k] = LLONG_MIN; }
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      lo[k] = min(lo[k], partial[b * 2 * D + k]);
+      hi[k] = max(hi[k], partial[b * 2 * D + k + D]);
+    }
+#pragma unroll
+  for (int k = 0; k < D; ++k) { s[k][threadIdx.x] = lo[k]; s[D + k][threadIdx.x] = hi[k]; }
+  __syncthreads();
+  for (int st = 128; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+#pragma unroll
+      for (int k = 0; k < D; ++k) {
+        s[k][threadIdx.x] = min(s[k][threadIdx.x], s[k][threadIdx.x + st]);
+        s[D + k][threadIdx.x] = max(s[D + k][threadIdx.x], s[D + k][threadIdx.x + st]);
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
   DevParams p;
   int fl = *flags;
   for (int k = 0; k < 3; ++k) { p.lo[k] = 0; p.hi[k] = 0; p.centre[k] = 0; p.G[k] = 1; }
   for (int k = 0; k < D; ++k) {
-    double lo = DBL_MAX, hi = -DBL_MAX;
-    for (int b = 0; b < nblocks; ++b) {
-      lo = fmin(lo, partial[b * 2 * D + k]);
-      hi = fmax(hi, partial[b * 2 * D + k + D]);
-    }
-    p.lo[k] = lo;
-    p.hi[k] = hi;
-    p.centre[k] = 0.5 * lo + 0.5 * hi;
+    p.lo[k] = dbl_of(s[k][0]);
+    p.hi[k] = dbl_of(s[D + k][0]);
+    p.centre[k] = 0.5 * p.lo[k] + 0.5 * p.hi[k];
   }
   p.dim = D;
   p.minpts = minpts;
@@ -284,7 +314,6 @@ __device__ __forceinline__ int64_t offset_key(const CellXYZ<D>& c, int ox, int o
   return k;
 }
 
-__constant__ int kRowOrder[5] = {0, -1, 1, -2, 2};
 
 // Loads one candidate (sorted position q) in the layout the mode tests with.
 template <int D, bool F32>
@@ -416,9 +445,6 @@ __device__ __forceinline__ int warp_min_i32(int v) {
   return v;
 }
 
-constexpr int kWarpsPerBlock = 8;
-constexpr int kCellThreads = kWarpsPerBlock * 32;
-
 // Cell lookup.  Dense grids: the cell table gives every cell's point range.
 // Sparse grids: a hash of the occupied cells' keys gives the cell index m, and
 // reps[m]..reps[m+1] its points.  The probe loop is bounded by the table size.
@@ -479,22 +505,136 @@ __device__ __forceinline__ int rep_of(const gdl::Bufs& B, int64_t i) {
 }
 
 
+// ------------------------------------------------------------ stencil tables
+// Offsets within +-2 cells, built at compile time.  kRows: the (ox, oy) rows a
+// core count scans, own row first.  kHalf[d][pass]: the half stencil (o > 0
+// lexicographically) split into near offsets (all |o_k| <= 1, pass 0) and the
+// rest (pass 1).  kFull[d]: all offsets (border search).
+struct OffTab {
+  signed char o[128][3];
+  int n;
+};
+
+constexpr OffTab make_rows(int D) {
+  OffTab t{};
+  const int order[5] = {0, -1, 1, -2, 2};
+  for (int a = 0; a < 5; ++a)
+    for (int b = 0; b < (D == 3 ? 5 : 1); ++b) {
+      t.o[t.n][0] = (signed char)order[a];
+      t.o[t.n][1] = (signed char)(D == 3 ? order[b] : 0);
+      t.o[t.n][2] = 0;
+      ++t.n;
+    }
+  return t;
+}
+
+constexpr OffTab make_half(int D, int pass) {
+  OffTab t{};
+  const int zr = D == 3 ? 2 : 0;
+  for (int x = -2; x <= 2; ++x)
+    for (int y = -2; y <= 2; ++y)
+      for (int z = -zr; z <= zr; ++z) {
+        bool pos = x > 0 || (x == 0 && (y > 0 || (y == 0 && z > 0)));
+        bool near = x >= -1 && x <= 1 && y >= -1 && y <= 1 && z >= -1 && z <= 1;
+        if (!pos || (pass == 0) != near) continue;
+        t.o[t.n][0] = (signed char)x;
+        t.o[t.n][1] = (signed char)y;
+        t.o[t.n][2] = (signed char)z;
+        ++t.n;
+      }
+  return t;
+}
+
+constexpr OffTab make_full(int D) {
+  OffTab t{};
+  const int zr = D == 3 ? 2 : 0;
+  for (int x = -2; x <= 2; ++x)
+    for (int y = -2; y <= 2; ++y)
+      for (int z = -zr; z <= zr; ++z) {
+        t.o[t.n][0] = (signed char)x;
+        t.o[t.n][1] = (signed char)y;
+        t.o[t.n][2] = (signed char)z;
+        ++t.n;
+      }
+  return t;
+}
+
+__constant__ OffTab kRows[2] = {make_rows(2), make_rows(3)};
+__constant__ OffTab kHalf[2][2] = {{make_half(2, 0), make_half(2, 1)},
+                                   {make_half(3, 0), make_half(3, 1)}};
+__constant__ OffTab kFullSt[2] = {make_full(2), make_full(3)};
+
+// Per-warp list of candidate rows: row r holds the points lo[r] .. lo[r]+len,
+// and pre[r] is the exclusive prefix of the lengths (rows concatenated in
+// table order).  Lane r looks its row up, so all lookups are in flight at once.
+struct RowList {
+  int lo[32];
+  int pre[32];
+};
+
+template <int D, bool SPARSE>
+__device__ __forceinline__ int build_rows(RowList& RL, const GridView<SPARSE>& gv,
+                                          const CellXYZ<D>& cc, const DevParams& P, int lane) {
+  const OffTab& T = kRows[D - 2];
+  const int64_t Gl = P.G[D - 1];
+  const int64_t cl = cc.c[D - 1];
+  const int64_t l0 = cl - 2 < 0 ? 0 : cl - 2;
+  const int64_t l1 = cl + 2 >= Gl ? Gl - 1 : cl + 2;
+  int lo = 0, len = 0;
+  if (lane < T.n) {
+    int64_t rowkey = offset_key<D>(cc, T.o[lane][0], T.o[lane][1], 0, P);
+    if (rowkey >= 0) {
+      rowkey -= cl;
+      const int2 rg = gv.span((uint64_t)(rowkey + l0), (uint64_t)(rowkey + l1));
+      lo = rg.x;
+      len = rg.y - rg.x;
+    }
+  }
+  int inc = len;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int v = __shfl_up_sync(kFull, inc, o);
+    if (lane >= o) inc += v;
+  }
+  RL.lo[lane] = lo;
+  RL.pre[lane] = inc - len;
+  __syncwarp();
+  return __shfl_sync(kFull, inc, 31);
+}
+
+// sorted position of concatenated candidate c (0 <= c < total)
+__device__ __forceinline__ int row_pos(const RowList& RL, int nrows, int c) {
+  int r = 0;
+#pragma unroll
+  for (int step = 16; step; step >>= 1)
+    if (r + step < nrows && RL.pre[r + step] <= c) r += step;
+  return RL.lo[r] + (c - RL.pre[r]);
+}
+
+constexpr int kWarpsPerBlock = 8;
+constexpr int kCellThreads = kWarpsPerBlock * 32;
+
 // ------------------------------------------------------------- core flags
-// One warp per non-empty cell.  Dense cells are all core.  Otherwise every point
-// p of the cell counts its neighbours: the warp streams the candidate rows (the
-// 5 cells along the last axis, one contiguous range) 32 at a time, one
-// candidate per lane, and each staged p gets __ballot_sync + __popc of the
-// lanes that hold a neighbour.  Stops as soon as every p has reached minpts.
+// One warp per non-empty cell.  Dense cells are all core.  Otherwise the warp
+// looks up its candidate rows (5 cells along the last axis each, 5 rows in 2D,
+// 25 in 3D; one lane per row), concatenates them, and streams the candidates
+// 32 at a time, one per lane.  Each staged point p of the cell gets
+// __ballot_sync + __popc of the lanes holding a neighbour.  The warp stops as
+// soon as every staged p has reached minpts (own row first, so dense
+// neighbourhoods stop after one tile).
 template <int D, bool F32, bool SPARSE>
 __global__ void __launch_bounds__(kCellThreads) k_core(const gdl::Bufs B, int64_t n) {
   __shared__ DevParams sP;
   __shared__ WarpStage<D> stage[kWarpsPerBlock];
+  __shared__ RowList rows[kWarpsPerBlock];
   if (threadIdx.x == 0) sP = *B.P;
   __syncthreads();
   const DevParams& P = sP;
   const GridView<SPARSE> gv = view_of<SPARSE>(B);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   WarpStage<D>& S = stage[w];
+  RowList& RL = rows[w];
+  const int nrows = kRows[D - 2].n;
   const double* __restrict__ X = B.X;
   const float* __restrict__ Xf = B.Xf;
   const int64_t M = *B.M;
@@ -514,10 +654,7 @@ __global__ void __launch_bounds__(kCellThreads) k_core(const gdl::Bufs B, int64_
       continue;
     }
     const CellXYZ<D> cc = decompose<D>(key_at<SPARSE>(B, b), P);
-    const int64_t Gl = P.G[D - 1];
-    const int64_t cl = cc.c[D - 1];
-    const int64_t l0 = cl - 2 < 0 ? 0 : cl - 2;
-    const int64_t l1 = cl + 2 >= Gl ? Gl - 1 : cl + 2;
+    const int total = build_rows<D, SPARSE>(RL, gv, cc, P, lane);
     int ncore = 0, mn = INT_MAX;
     for (int c0 = 0; c0 < sz; c0 += 32) {
       const int na = min(32, sz - c0);
@@ -531,26 +668,21 @@ __global__ void __launch_bounds__(kCellThreads) k_core(const gdl::Bufs B, int64_
       __syncwarp();
       int mycnt = 0;
       bool done = false;
-      const int nrows = D == 3 ? 25 : 5;
-      for (int r = 0; r < nrows && !done; ++r) {
-        const int ox = kRowOrder[D == 3 ? r / 5 : r];
-        const int oy = D == 3 ? kRowOrder[r % 5] : 0;
-        int64_t rowkey = offset_key<D>(cc, ox, oy, 0, P);
-        if (rowkey < 0) continue;
-        rowkey -= cl;  // key of the row's first cell
-        const int2 rg = gv.span((uint64_t)(rowkey + l0), (uint64_t)(rowkey + l1));
-        for (int64_t qb = rg.x; qb < rg.y && !done; qb += 32) {
-          const int64_t q = qb + lane;
-          const bool valid = q < rg.y;
-          Cand<D, F32> c;
-          if (valid) load_cand<D, F32>(c, X, Xf, n, q);
-          for (int j = 0; j < na; ++j) {
-            bool hit = valid && pair_test<D, F32>(S.x[j], S.f[j], c, X, n, q, true, P, t);
-            unsigned bal = __ballot_sync(kFull, hit);
-            if (lane == j) mycnt += __popc(bal);
-          }
-          done = __all_sync(kFull, lane >= na || mycnt >= P.minpts);
+      for (int base = 0; base < total && !done; base += 32) {
+        const int c = base + lane;
+        const bool valid = c < total;
+        int q = 0;
+        Cand<D, F32> cd;
+        if (valid) {
+          q = row_pos(RL, nrows, c);
+          load_cand<D, F32>(cd, X, Xf, n, q);
         }
+        for (int j = 0; j < na; ++j) {
+          bool hit = valid && pair_test<D, F32>(S.x[j], S.f[j], cd, X, n, q, true, P, t);
+          unsigned bal = __ballot_sync(kFull, hit);
+          if (lane == j) mycnt += __popc(bal);
+        }
+        done = __all_sync(kFull, lane >= na || mycnt >= P.minpts);
       }
       const bool isc = lane < na && mycnt >= P.minpts;
       if (lane < na) B.core[b + c0 + lane] = isc ? 1 : 0;
@@ -575,25 +707,13 @@ __global__ void k_parent_init(const gdl::Bufs B) {
   }
 }
 
-// Half stencil of cell offsets (o > 0 lexicographically).  PASS 0: offsets with
-// every |o_k| <= 1; PASS 1: the others.  Running the near pass first lets most
-// far pairs be skipped because their cells are already in one component.
-template <int D>
-__device__ __forceinline__ bool half_offset(int t, int pass, int& ox, int& oy, int& oz) {
-  if (D == 2) {
-    ox = t / 5 - 2; oy = t % 5 - 2; oz = 0;
-  } else {
-    ox = t / 25 - 2; oy = (t / 5) % 5 - 2; oz = t % 5 - 2;
-  }
-  bool pos = ox > 0 || (ox == 0 && (oy > 0 || (oy == 0 && oz > 0)));
-  if (!pos) return false;
-  bool near = abs(ox) <= 1 && abs(oy) <= 1 && abs(oz) <= 1;
-  return (pass == 0) == near;
-}
-
-// One warp per cell A with core points; for each half-stencil neighbour cell B
-// with core points in another component, look for one core-core pair that are
-// neighbours both ways (lanes over B's points, A's points broadcast) and unite.
+// One warp per cell A with core points.  Lanes look up the half-stencil
+// neighbour cells of this pass in parallel (pass 0: offsets within +-1, pass 1:
+// the rest -- running the near pass first lets most far pairs be skipped
+// because their cells are already in one component).  For each neighbour B
+// with core points in another component, the warp looks for one core-core pair
+// that are neighbours both ways (lanes over B's points, A's core points
+// broadcast) and unites the two cells.
 template <int D, bool F32, bool SPARSE>
 __global__ void __launch_bounds__(kCellThreads) k_union(const gdl::Bufs B, int64_t n, int pass) {
   __shared__ DevParams sP;
@@ -606,43 +726,55 @@ __global__ void __launch_bounds__(kCellThreads) k_union(const gdl::Bufs B, int64
   const float* __restrict__ Xf = B.Xf;
   const int64_t M = *B.M;
   const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
-  constexpr int NT = D == 3 ? 125 : 25;
+  const OffTab& T = kHalf[D - 2][pass];
   Tally t;
   for (int64_t m = (int64_t)blockIdx.x * kWarpsPerBlock + w; m < M; m += W) {
     const int b = B.reps[m];
     if (B.cellcore[b] == 0) continue;
     const int e = B.reps[m + 1];
     const CellXYZ<D> cc = decompose<D>(key_at<SPARSE>(B, b), P);
-    for (int tt = 0; tt < NT; ++tt) {
-      int ox, oy, oz;
-      if (!half_offset<D>(tt, pass, ox, oy, oz)) continue;
-      const int64_t kb = offset_key<D>(cc, ox, oy, oz, P);
-      if (kb < 0) continue;
-      const int2 cb = gv.cell((uint64_t)kb);
-      const int bB = cb.x, eB = cb.y;
-      if (bB == eB || B.cellcore[bB] == 0) continue;
-      if (uf_find(B.parent, b) == uf_find(B.parent, bB)) continue;
-      bool found = false;
-      for (int qb = bB; qb < eB && !found; qb += 32) {
-        const int q = qb + lane;
-        const bool valid = q < eB && B.core[q];
-        Cand<D, F32> c;
-        if (valid) load_cand<D, F32>(c, X, Xf, n, q);
-        for (int a = b; a < e && !found; ++a) {
-          if (!B.core[a]) continue;
-          double ax[D];
-          float af[D];
-#pragma unroll
-          for (int k = 0; k < D; ++k) {
-            ax[k] = X[k * n + a];
-            if (F32) af[k] = Xf[k * n + a];
-          }
-          bool hit = valid && link_test<D, F32>(ax, af, c, X, n, a, q, P, t, B.asym, B.ctr);
-          found = __any_sync(kFull, hit);
+    for (int t0 = 0; t0 < T.n; t0 += 32) {
+      const int tt = t0 + lane;
+      bool cand = false;
+      int bB = 0, eB = 0;
+      if (tt < T.n) {
+        const int64_t kb = offset_key<D>(cc, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
+        if (kb >= 0) {
+          const int2 cb = gv.cell((uint64_t)kb);
+          bB = cb.x;
+          eB = cb.y;
+          cand = bB < eB && B.cellcore[bB] > 0 && uf_find(B.parent, bB) != uf_find(B.parent, b);
         }
       }
-      if (found && lane == 0) uf_union(B.parent, B.cellmin, b, bB);
-      __syncwarp();
+      unsigned mask = __ballot_sync(kFull, cand);
+      while (mask) {
+        const int src = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const int cbB = __shfl_sync(kFull, bB, src);
+        const int ceB = __shfl_sync(kFull, eB, src);
+        if (uf_find(B.parent, b) == uf_find(B.parent, cbB)) continue;
+        bool found = false;
+        for (int qb = cbB; qb < ceB && !found; qb += 32) {
+          const int q = qb + lane;
+          const bool valid = q < ceB && B.core[q];
+          Cand<D, F32> c;
+          if (valid) load_cand<D, F32>(c, X, Xf, n, q);
+          for (int a = b; a < e && !found; ++a) {
+            if (!B.core[a]) continue;
+            double ax[D];
+            float af[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+              ax[k] = X[k * n + a];
+              if (F32) af[k] = Xf[k * n + a];
+            }
+            bool hit = valid && link_test<D, F32>(ax, af, c, X, n, a, q, P, t, B.asym, B.ctr);
+            found = __any_sync(kFull, hit);
+          }
+        }
+        if (found && lane == 0) uf_union(B.parent, B.cellmin, b, cbB);
+        __syncwarp();
+      }
     }
   }
   flush_tally(t, B.ctr);
@@ -762,7 +894,9 @@ __global__ void k_label(const gdl::Bufs B, int64_t n) {
 // Border points: one warp per cell with non-core points (only non-dense cells
 // have any).  Each staged non-core point takes the smallest cluster id among
 // the cells whose core points have it in their neighbourhood (centre = the core
-// point, as the reference's expansion queries from the core point).
+// point, as the reference's expansion queries from the core point).  Lanes look
+// the stencil cells up in parallel; cells whose cluster id cannot improve any
+// staged point are skipped.
 template <int D, bool F32, bool SPARSE>
 __global__ void __launch_bounds__(kCellThreads) k_border(const gdl::Bufs B, int64_t n) {
   __shared__ DevParams sP;
@@ -778,7 +912,7 @@ __global__ void __launch_bounds__(kCellThreads) k_border(const gdl::Bufs B, int6
   const float* __restrict__ Xf = B.Xf;
   const int64_t M = *B.M;
   const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
-  constexpr int NT = D == 3 ? 125 : 25;
+  const OffTab& T = kFullSt[D - 2];
   Tally t;
   for (int64_t m = (int64_t)blockIdx.x * kWarpsPerBlock + w; m < M; m += W) {
     const int b = B.reps[m], e = B.reps[m + 1];
@@ -802,33 +936,44 @@ __global__ void __launch_bounds__(kCellThreads) k_border(const gdl::Bufs B, int6
       }
       __syncwarp();
       int best = INT_MAX;  // lane j < na: best cluster of staged point j
-      for (int tt = 0; tt < NT; ++tt) {
-        int ox, oy, oz;
-        if (D == 2) { ox = tt / 5 - 2; oy = tt % 5 - 2; oz = 0; }
-        else { ox = tt / 25 - 2; oy = (tt / 5) % 5 - 2; oz = tt % 5 - 2; }
-        const int64_t kb = offset_key<D>(cc, ox, oy, oz, P);
-        if (kb < 0) continue;
-        const int2 cb = gv.cell((uint64_t)kb);
-        const int bB = cb.x, eB = cb.y;
-        if (bB == eB || B.cellcore[bB] == 0) continue;
-        const int cB = B.cellcid[bB];
-        // can any staged point still improve?
-        const bool want = lane < na && cB < best;
-        unsigned wantm = __ballot_sync(kFull, want);
-        if (!wantm) continue;
-        for (int qb = bB; qb < eB && wantm; qb += 32) {
-          const int q = qb + lane;
-          const bool valid = q < eB && B.core[q];
-          Cand<D, F32> c;
-          if (valid) load_cand<D, F32>(c, X, Xf, n, q);
-          unsigned pending = wantm;
-          while (pending) {
-            const int j = __ffs(pending) - 1;
-            pending &= pending - 1;
-            bool hit = valid && pair_test<D, F32>(S.x[j], S.f[j], c, X, n, q, false, P, t);
-            if (__any_sync(kFull, hit)) {
-              if (lane == j) best = cB;
-              wantm &= ~(1u << j);
+      for (int t0 = 0; t0 < T.n; t0 += 32) {
+        const int tt = t0 + lane;
+        bool has = false;
+        int bB = 0, eB = 0, cid = INT_MAX;
+        if (tt < T.n) {
+          const int64_t kb = offset_key<D>(cc, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
+          if (kb >= 0) {
+            const int2 cb = gv.cell((uint64_t)kb);
+            bB = cb.x;
+            eB = cb.y;
+            if (bB < eB && B.cellcore[bB] > 0) {
+              has = true;
+              cid = B.cellcid[bB];
+            }
+          }
+        }
+        unsigned mask = __ballot_sync(kFull, has);
+        while (mask) {
+          const int src = __ffs(mask) - 1;
+          mask &= mask - 1;
+          const int cB = __shfl_sync(kFull, cid, src);
+          const int cbB = __shfl_sync(kFull, bB, src);
+          const int ceB = __shfl_sync(kFull, eB, src);
+          unsigned wantm = __ballot_sync(kFull, lane < na && cB < best);
+          for (int qb = cbB; qb < ceB && wantm; qb += 32) {
+            const int q = qb + lane;
+            const bool valid = q < ceB && B.core[q];
+            Cand<D, F32> c;
+            if (valid) load_cand<D, F32>(c, X, Xf, n, q);
+            unsigned pending = wantm;
+            while (pending) {
+              const int j = __ffs(pending) - 1;
+              pending &= pending - 1;
+              bool hit = valid && pair_test<D, F32>(S.x[j], S.f[j], c, X, n, q, false, P, t);
+              if (__any_sync(kFull, hit)) {
+                if (lane == j) best = cB;
+                wantm &= ~(1u << j);
+              }
             }
           }
         }
@@ -882,16 +1027,18 @@ static int grid_for(int64_t work, int threads, int sms, int per_sm) {
 
 void bbox(const double* pts, int64_t n, int dim, double* partial, int nblocks, int* flags,
           cudaStream_t s) {
-  if (dim == 2) k_bbox_partial<2><<<nblocks, kBboxThreads, 0, s>>>(pts, n, partial, flags);
-  else k_bbox_partial<3><<<nblocks, kBboxThreads, 0, s>>>(pts, n, partial, flags);
+  long long* part = reinterpret_cast<long long*>(partial);
+  if (dim == 2) k_bbox_partial<2><<<nblocks, kBboxThreads, 0, s>>>(pts, n, part, flags);
+  else k_bbox_partial<3><<<nblocks, kBboxThreads, 0, s>>>(pts, n, part, flags);
 }
 
 void params(const double* partial, int nblocks, int dim, DevParams* P, double eps, int minpts,
             double cell_mult, uint64_t max_cells, const int* flags, cudaStream_t s) {
+  const long long* part = reinterpret_cast<const long long*>(partial);
   if (dim == 2)
-    k_params<2><<<1, 32, 0, s>>>(partial, nblocks, P, eps, minpts, cell_mult, max_cells, flags);
+    k_params<2><<<1, 256, 0, s>>>(part, nblocks, P, eps, minpts, cell_mult, max_cells, flags);
   else
-    k_params<3><<<1, 32, 0, s>>>(partial, nblocks, P, eps, minpts, cell_mult, max_cells, flags);
+    k_params<3><<<1, 256, 0, s>>>(part, nblocks, P, eps, minpts, cell_mult, max_cells, flags);
 }
 
 void keys(const double* pts, int64_t n, int dim, bool sparse, const DevParams* P, void* keys,
