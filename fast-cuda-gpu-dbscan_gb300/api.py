@@ -77,6 +77,9 @@ SIGNATURES = [
     ("gd_dbscan", ctypes.c_int, [_P, ctypes.POINTER(GdPoints), ctypes.c_double, ctypes.c_int32,
                                  _P, ctypes.POINTER(GdStats)]),
     ("gd_get_stats", ctypes.c_int, [_P, ctypes.POINTER(GdStats)]),
+    ("gd_dbscan_noalloc", ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int32, ctypes.c_double,
+                                         ctypes.c_int32, ctypes.c_int32, _P,
+                                         ctypes.POINTER(ctypes.c_int64), _P]),
     ("gd_import_dataset", ctypes.c_int, [ctypes.c_char_p, ctypes.c_int32, ctypes.c_int64,
                                          ctypes.POINTER(ctypes.POINTER(ctypes.c_double)),
                                          ctypes.POINTER(ctypes.c_int64)]),

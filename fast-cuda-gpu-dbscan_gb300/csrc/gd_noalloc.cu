@@ -1,0 +1,254 @@
+// gd_noalloc.cu -- gd_dbscan_noalloc: exact DBSCAN for small point sets that
+// allocates no memory at all.
+//
+// Who needs it: callers that may not call cudaMalloc/cudaFree -- code that runs
+// while a CUDA graph is being captured into, real-time loops whose memory was
+// fixed at start-up, or hosts whose allocator policy forbids device
+// allocations after initialisation.  They pass device pointers for the points
+// and the labels; every other buffer of the pipeline lives in one file-scope
+// __device__ array (kScratchBytes, about 5 MiB) that the module holds on every
+// GPU that loads this library until the process exits.
+//
+// Limits and rules:
+//   * n <= GD_NOALLOC_MAX_POINTS (32768); larger inputs are rejected with
+//     GD_ERANGE.  Grids of more than 8*32768 cells use the hash of occupied
+//     cells instead of the dense table, so any extent fits.
+//   * The first call on a device looks the array's device address up
+//     (cudaGetSymbolAddress, with that device current) and caches it; make that
+//     first call before any stream capture begins.
+//   * All calls share the one array and it keeps the previous call's contents:
+//     everything that must start at zero (counters, flags, cluster marks, the
+//     cell table or hash) is cleared inside each call.  Calls whose work
+//     overlaps on the GPU (two host threads, or two streams) race on the array
+//     and must be serialised by the caller.
+//   * The call synchronises the stream once (to read the grid size) and at the
+//     end; it uses the same kernels as gd_dbscan, so the labels are identical.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "gbdbscan.h"
+#include "gd_launch.h"
+
+namespace gdio {
+void set_error(const std::string& m);
+}
+
+namespace {
+
+constexpr int64_t kMaxPoints = GD_NOALLOC_MAX_POINTS;
+constexpr uint64_t kTableCells = 8ull * kMaxPoints;      // dense table limit
+constexpr uint64_t kHashSlots = 2ull * kMaxPoints;       // power of two
+constexpr int kBboxBlocks = 256;
+
+constexpr size_t up(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// byte offsets of the buffers inside the scratch array
+constexpr size_t kOffSmall = 0;                                   // params | M | K | flags | ctr
+constexpr size_t kOffPartial = kOffSmall + 4096;
+constexpr size_t kOffKeys0 = kOffPartial + up(kBboxBlocks * 6 * 8);
+constexpr size_t kOffKeys1 = kOffKeys0 + up(kMaxPoints * 8);
+constexpr size_t kOffVals0 = kOffKeys1 + up(kMaxPoints * 8);
+constexpr size_t kOffVals1 = kOffVals0 + up(kMaxPoints * 4);
+constexpr size_t kOffX = kOffVals1 + up(kMaxPoints * 4);
+constexpr size_t kOffXf = kOffX + up(kMaxPoints * 3 * 8);
+constexpr size_t kOffTable = kOffXf + up(kMaxPoints * 3 * 4);
+constexpr size_t kOffHkeys = kOffTable + up((kTableCells + 1) * 4);
+constexpr size_t kOffHvals = kOffHkeys + up(kHashSlots * 8);
+constexpr size_t kOffReps = kOffHvals + up(kHashSlots * 4);
+constexpr size_t kOffRunfl = kOffReps + up((kMaxPoints + 1) * 4);
+constexpr size_t kOffRunpos = kOffRunfl + up(kMaxPoints * 4);
+constexpr size_t kOffCore = kOffRunpos + up(kMaxPoints * 4);
+constexpr size_t kOffCellcore = kOffCore + up(kMaxPoints);
+constexpr size_t kOffCellmin = kOffCellcore + up(kMaxPoints * 4);
+constexpr size_t kOffParent = kOffCellmin + up(kMaxPoints * 4);
+constexpr size_t kOffFmark = kOffParent + up(kMaxPoints * 4);
+constexpr size_t kOffCellcid = kOffFmark + up(kMaxPoints * 4);
+constexpr size_t kOffLab = kOffCellcid + up(kMaxPoints * 4);
+constexpr size_t kOffAsym = kOffLab + up(kMaxPoints * 4);
+constexpr size_t kOffSortTemp = kOffAsym + up(gd::kAsymCap * 8);
+constexpr size_t kSortTempBytes = 64 * 1024;   // >= sort_temp_bytes(kMaxPoints), checked below
+constexpr size_t kOffScanTemp = kOffSortTemp + kSortTempBytes;
+constexpr size_t kScanTempBytes = 4096;        // >= scan_temp_bytes(kTableCells + 1), checked below
+constexpr size_t kScratchBytes = kOffScanTemp + kScanTempBytes;
+
+// The scratch.  In host code this name is only a stand-in for the symbol, not
+// a device address: kernels get the address from cudaGetSymbolAddress below.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mu;
+unsigned char* g_scratch_ptr[kMaxDevices] = {};
+
+gd_status fail(gd_status s, const std::string& m) {
+  gdio::set_error(m);
+  return s;
+}
+
+gd_status cuda_fail(cudaError_t e, const char* what) {
+  return fail(GD_ECUDA, std::string("gd_dbscan_noalloc: ") + what + ": " + cudaGetErrorString(e));
+}
+
+#define NA_CUDA(call, what)                            \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+// Device address of the scratch array on the current device (set up once per
+// device, with that device current).
+gd_status scratch_of(int dev, unsigned char** out) {
+  std::lock_guard<std::mutex> lock(g_setup_mu);
+  if (!g_scratch_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress");
+    g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
+  }
+  *out = g_scratch_ptr[dev];
+  return GD_OK;
+}
+
+}  // namespace
+
+extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int32_t dim,
+                                       double eps, int32_t minpts, int32_t precision,
+                                       int32_t* labels_dev, int64_t* n_clusters, void* stream) {
+  if (n < 0 || (dim != 2 && dim != 3))
+    return fail(GD_EINVAL, "gd_dbscan_noalloc: n must be >= 0 and dim 2 or 3");
+  if (n > kMaxPoints)
+    return fail(GD_ERANGE, "gd_dbscan_noalloc: n = " + std::to_string(n) +
+                               " exceeds the fixed scratch capacity of " +
+                               std::to_string(kMaxPoints) + " points; use gd_dbscan");
+  if (!(eps > 0) || eps != eps || eps > 1.7e308)
+    return fail(GD_EINVAL, "gd_dbscan_noalloc: eps must be positive and finite");
+  if (minpts < 1) return fail(GD_EINVAL, "gd_dbscan_noalloc: minpts must be >= 1");
+  if (precision != GD_PREC_FP64 && precision != GD_PREC_FP32_BAND)
+    return fail(GD_EINVAL, "gd_dbscan_noalloc: unknown precision mode");
+  if (n > 0 && (!coords_dev || !labels_dev))
+    return fail(GD_EINVAL, "gd_dbscan_noalloc: NULL pointer");
+  if (n_clusters) *n_clusters = 0;
+  if (n == 0) return GD_OK;
+  static_assert(kSortTempBytes >= 16 * 256 * 4 + 256 + 256, "sort temp too small");
+  if (gdprim::sort_temp_bytes(kMaxPoints) > kSortTempBytes ||
+      gdprim::scan_temp_bytes((int64_t)kTableCells + 1) > kScanTempBytes ||
+      gdprim::scan_temp_bytes(kMaxPoints) > kScanTempBytes)
+    return fail(GD_EINVAL, "gd_dbscan_noalloc: scratch layout inconsistent (build error)");
+
+  int dev = 0;
+  NA_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return fail(GD_ENODEV, "gd_dbscan_noalloc: device index");
+  int sms = 0;
+  NA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  unsigned char* base = nullptr;
+  gd_status st = scratch_of(dev, &base);
+  if (st != GD_OK) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int D = dim;
+
+  gd::DevParams* dP = reinterpret_cast<gd::DevParams*>(base + kOffSmall);
+  uint32_t* dM = reinterpret_cast<uint32_t*>(base + kOffSmall + 512);
+  uint32_t* dK = reinterpret_cast<uint32_t*>(base + kOffSmall + 516);
+  int* dFlags = reinterpret_cast<int*>(base + kOffSmall + 520);
+  unsigned long long* dCtr = reinterpret_cast<unsigned long long*>(base + kOffSmall + 640);
+
+  // index build (the same stages as gd_index_build)
+  NA_CUDA(cudaMemsetAsync(base + kOffSmall, 0, 4096, s), "clear counters");
+  int nb = (int)std::min<int64_t>(kBboxBlocks, (n + 255) / 256);
+  double* partial = reinterpret_cast<double*>(base + kOffPartial);
+  gdl::bbox(coords_dev, n, D, partial, nb, dFlags, s);
+  gdl::params(partial, nb, D, dP, eps, minpts, 0.5 * (1.0 + 1.0 / 65536.0), kTableCells, dFlags, s);
+  gd::DevParams hp;
+  NA_CUDA(cudaMemcpyAsync(&hp, dP, sizeof hp, cudaMemcpyDeviceToHost, s), "read grid parameters");
+  NA_CUDA(cudaStreamSynchronize(s), "grid parameters");
+  if (hp.flags & gd::kFlagNonFinite)
+    return fail(GD_EINVAL, "gd_dbscan_noalloc: input has NaN or Inf coordinates");
+  if (hp.flags & gd::kFlagGridTooLarge)
+    return fail(GD_ERANGE, "gd_dbscan_noalloc: eps-cell grid too large");
+  const bool f32 = precision == GD_PREC_FP32_BAND && hp.eps2_lo32 > 0.0f;
+  const bool sparse = hp.sparse != 0;
+  const uint64_t C = hp.C;
+  gdl::keys(coords_dev, n, D, sparse, dP, base + kOffKeys0, sms, s);
+  uint32_t* vb[2] = {reinterpret_cast<uint32_t*>(base + kOffVals0),
+                     reinterpret_cast<uint32_t*>(base + kOffVals1)};
+  const void* skeys;
+  int r;
+  if (sparse) {
+    using U64 = unsigned long long;
+    U64* kb[2] = {reinterpret_cast<U64*>(base + kOffKeys0), reinterpret_cast<U64*>(base + kOffKeys1)};
+    r = gdprim::radix_sort_pairs<U64>(kb, vb, n, hp.key_bits, true, base + kOffSortTemp, s);
+    skeys = kb[r];
+  } else {
+    uint32_t* kb[2] = {reinterpret_cast<uint32_t*>(base + kOffKeys0),
+                       reinterpret_cast<uint32_t*>(base + kOffKeys1)};
+    r = gdprim::radix_sort_pairs<uint32_t>(kb, vb, n, hp.key_bits, true, base + kOffSortTemp, s);
+    skeys = kb[r];
+  }
+  uint32_t* ids = vb[r];
+  double* X = reinterpret_cast<double*>(base + kOffX);
+  float* Xf = reinterpret_cast<float*>(base + kOffXf);
+  gdl::gather(coords_dev, ids, n, D, f32, dP, X, Xf, sms, s);
+  uint32_t* fl = reinterpret_cast<uint32_t*>(base + kOffRunfl);
+  uint32_t* pos = reinterpret_cast<uint32_t*>(base + kOffRunpos);
+  int* reps = reinterpret_cast<int*>(base + kOffReps);
+  gdl::run_flags(skeys, sparse, n, fl, sms, s);
+  gdprim::exclusive_scan_u32(fl, pos, n, base + kOffScanTemp, dM, s);
+  gdl::run_scatter(fl, pos, n, reps, dM, dCtr, sms, s);
+  unsigned long long* hkeys = reinterpret_cast<unsigned long long*>(base + kOffHkeys);
+  uint32_t* hvals = reinterpret_cast<uint32_t*>(base + kOffHvals);
+  uint32_t* table = reinterpret_cast<uint32_t*>(base + kOffTable);
+  if (sparse) {
+    NA_CUDA(cudaMemsetAsync(hkeys, 0xff, kHashSlots * 8, s), "clear cell hash");
+    gdl::hash_insert(static_cast<const unsigned long long*>(skeys), reps, dM, n, hkeys, hvals,
+                     (uint32_t)(kHashSlots - 1), sms, s);
+  } else {
+    NA_CUDA(cudaMemsetAsync(table, 0, (C + 1) * 4, s), "clear cell table");
+    gdl::cell_counts(static_cast<const uint32_t*>(skeys), reps, dM, n, table, sms, s);
+    gdprim::exclusive_scan_u32(table, table, (int64_t)C + 1, base + kOffScanTemp, nullptr, s);
+  }
+
+  // expansion (the same stages as gd_expand)
+  gdl::Bufs B;
+  B.P = dP;
+  B.keys = skeys;
+  B.ids = ids;
+  B.reps = reps;
+  B.M = dM;
+  B.runfl = fl;
+  B.runpos = pos;
+  B.start = table;
+  B.hkeys = hkeys;
+  B.hvals = hvals;
+  B.hmask = (uint32_t)(kHashSlots - 1);
+  B.X = X;
+  B.Xf = Xf;
+  B.core = base + kOffCore;
+  B.cellcore = reinterpret_cast<int*>(base + kOffCellcore);
+  B.cellmin = reinterpret_cast<int*>(base + kOffCellmin);
+  B.parent = reinterpret_cast<int*>(base + kOffParent);
+  B.Fmark = reinterpret_cast<uint32_t*>(base + kOffFmark);
+  B.cellcid = reinterpret_cast<int*>(base + kOffCellcid);
+  B.lab = reinterpret_cast<int*>(base + kOffLab);
+  B.asym = reinterpret_cast<int*>(base + kOffAsym);
+  B.ctr = dCtr;
+  gdl::core(B, n, D, f32, sparse, sms, s);
+  gdl::unite(B, n, D, f32, sparse, sms, s);
+  NA_CUDA(cudaMemsetAsync(B.Fmark, 0, n * 4, s), "clear cluster marks");
+  gdl::roots(B, n, sms, s);
+  gdprim::exclusive_scan_u32(B.Fmark, B.Fmark, n, base + kOffScanTemp, dK, s);
+  gdl::label(B, n, sms, s);
+  gdl::border(B, n, D, f32, sparse, sms, s);
+  gdl::scatter_labels(B, n, labels_dev, nullptr, sms, s);
+  NA_CUDA(cudaGetLastError(), "launch");
+  unsigned long long asym_edges = 0;
+  uint32_t K = 0;
+  NA_CUDA(cudaMemcpyAsync(&asym_edges, dCtr + gd::kCtrAsymEdges, 8, cudaMemcpyDeviceToHost, s),
+          "read counters");
+  NA_CUDA(cudaMemcpyAsync(&K, dK, 4, cudaMemcpyDeviceToHost, s), "read cluster count");
+  NA_CUDA(cudaStreamSynchronize(s), "DBSCAN pipeline");
+  if (asym_edges > (unsigned long long)gd::kAsymCap)
+    return fail(GD_ERANGE, "gd_dbscan_noalloc: too many one-directional core neighbour pairs");
+  if (n_clusters) *n_clusters = K;
+  return GD_OK;
+}

@@ -138,6 +138,24 @@ gd_status gd_dbscan(gd_ctx* ctx, const gd_points* pts, double eps, int32_t minpt
 /* Statistics of the last gd_expand / gd_dbscan on this context. */
 gd_status gd_get_stats(gd_ctx* ctx, gd_stats* stats);
 
+/* ---- exact DBSCAN without any memory allocation ------------------------ */
+/* No counterpart in the reference.  For callers that may not allocate device
+   memory -- code running while a CUDA graph is captured, real-time loops whose
+   memory was fixed at start-up, hosts whose allocator policy forbids device
+   allocations after initialisation.  Same labels as gd_dbscan, for up to
+   GD_NOALLOC_MAX_POINTS points; larger n is rejected with GD_ERANGE.
+   coords_dev (n x dim float64) and labels_dev (n int32) are device pointers
+   on the current device; stream may be NULL (default stream).  All scratch is
+   one fixed static device array of about 5 MiB that every GPU which loads the
+   library keeps until the process exits; nothing is allocated or freed.
+   The first call on a device looks up that array's address; make it before
+   any stream capture.  Calls share the array: calls that overlap on the GPU
+   race and must be serialised by the caller.  n_clusters may be NULL. */
+#define GD_NOALLOC_MAX_POINTS 32768
+gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int32_t dim, double eps,
+                            int32_t minpts, int32_t precision, int32_t* labels_dev,
+                            int64_t* n_clusters, void* stream);
+
 /* ---- dataset files ------------------------------------------------------- */
 /* Replaces ImportDataset (main.cu:469-498): reads a headerless CSV with dim
    comma-separated values per line (max_points <= 0: no limit; the reference
