@@ -65,7 +65,7 @@ struct gd_ctx {
 
   DevBuf pts, keys0, keys1, vals0, vals1, X, Xf, table, reps, runfl, runpos, core, cellcore,
       cellmin, parent, Fmark, cellcid, lab, out, coreout, sorttemp, scantemp, partial, small,
-      asym, hkeys, hvals;
+      asym, hkeys, hvals, hvcell, hvmask;
 
   // state of the current instance
   int stage = 0;  // 0: nothing, 1: indexed, 2: expanded
@@ -104,7 +104,7 @@ struct gd_ctx {
     DevBuf* all[] = {&pts, &keys0, &keys1, &vals0, &vals1, &X, &Xf, &table, &reps, &runfl,
                      &runpos, &core, &cellcore, &cellmin, &parent, &Fmark, &cellcid, &lab,
                      &out, &coreout, &sorttemp, &scantemp, &partial, &small, &asym, &hkeys,
-                     &hvals};
+                     &hvals, &hvcell, &hvmask};
     for (DevBuf* b : all) {
       if (b->p) cudaFree(b->p);
       b->p = nullptr;
@@ -144,6 +144,8 @@ struct gd_ctx {
     B.cellcid = static_cast<int*>(cellcid.p);
     B.lab = static_cast<int*>(lab.p);
     B.asym = static_cast<int*>(asym.p);
+    B.hv_cell = static_cast<int*>(hvcell.p);
+    B.hv_mask = static_cast<unsigned long long*>(hvmask.p);
     B.ctr = dCtr();
     return B;
   }
@@ -407,6 +409,8 @@ gd_status gd_expand(gd_ctx* ctx, int32_t minpts) {
   if ((st = ctx->ensure(ctx->cellcid, n * 4, "cell cluster ids")) != GD_OK) return st;
   if ((st = ctx->ensure(ctx->lab, n * 4, "labels")) != GD_OK) return st;
   if ((st = ctx->ensure(ctx->asym, gd::kAsymCap * 8, "one-directional links")) != GD_OK) return st;
+  if ((st = ctx->ensure(ctx->hvcell, n * 4, "heavy-work list")) != GD_OK) return st;
+  if ((st = ctx->ensure(ctx->hvmask, n * 8, "heavy-work masks")) != GD_OK) return st;
   size_t sc = gdprim::scan_temp_bytes(n);
   if ((st = ctx->ensure(ctx->scantemp, std::max(sc, ctx->scantemp.bytes), "scan temp")) != GD_OK)
     return st;
@@ -428,8 +432,9 @@ gd_status gd_expand(gd_ctx* ctx, int32_t minpts) {
   gdl::label(B, n, ctx->sms, s);
   gdl::border(B, n, D, ctx->f32, ctx->sparse, ctx->sms, s);
   GD_CUDA(cudaGetLastError(), "expand launch");
-  // core, parent init, 2 union passes, compress, merge replay, roots, scan, label, border
-  ctx->launches += 1 + 1 + 2 + 1 + 1 + 1 + 3 + 1 + 1;
+  // core (scan+heavy), parent init, 2 union passes (scan+heavy), compress, merge replay,
+  // roots, scan, label, border (scan+heavy)
+  ctx->launches += 2 + 1 + 4 + 1 + 1 + 1 + 3 + 1 + 2;
   ctx->stage = 2;
   return GD_OK;
 }

@@ -65,6 +65,9 @@ enum Counter {
   kCtrNoise,            // noise points
   kCtrDenseCells,       // cells with >= minpts points
   kCtrAsymEdges,        // one-directional core pairs recorded for the merge replay
+  kCtrHeavyCore,        // cells queued for warp-cooperative core counting
+  kCtrHeavyUnion,       // cells queued for warp-cooperative link searches
+  kCtrHeavyBorder,      // cells queued for warp-cooperative border search
   kCtrCount = 16
 };
 

@@ -67,7 +67,9 @@ constexpr size_t kOffFmark = kOffParent + up(kMaxPoints * 4);
 constexpr size_t kOffCellcid = kOffFmark + up(kMaxPoints * 4);
 constexpr size_t kOffLab = kOffCellcid + up(kMaxPoints * 4);
 constexpr size_t kOffAsym = kOffLab + up(kMaxPoints * 4);
-constexpr size_t kOffSortTemp = kOffAsym + up(gd::kAsymCap * 8);
+constexpr size_t kOffHvCell = kOffAsym + up(gd::kAsymCap * 8);
+constexpr size_t kOffHvMask = kOffHvCell + up(kMaxPoints * 4);
+constexpr size_t kOffSortTemp = kOffHvMask + up(kMaxPoints * 8);
 constexpr size_t kSortTempBytes = 64 * 1024;   // >= sort_temp_bytes(kMaxPoints), checked below
 constexpr size_t kOffScanTemp = kOffSortTemp + kSortTempBytes;
 constexpr size_t kScanTempBytes = 4096;        // >= scan_temp_bytes(kTableCells + 1), checked below
@@ -231,6 +233,8 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   B.cellcid = reinterpret_cast<int*>(base + kOffCellcid);
   B.lab = reinterpret_cast<int*>(base + kOffLab);
   B.asym = reinterpret_cast<int*>(base + kOffAsym);
+  B.hv_cell = reinterpret_cast<int*>(base + kOffHvCell);
+  B.hv_mask = reinterpret_cast<unsigned long long*>(base + kOffHvMask);
   B.ctr = dCtr;
   gdl::core(B, n, D, f32, sparse, sms, s);
   gdl::unite(B, n, D, f32, sparse, sms, s);

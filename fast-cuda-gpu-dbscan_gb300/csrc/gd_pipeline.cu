@@ -614,6 +614,244 @@ __device__ __forceinline__ int row_pos(const RowList& RL, int nrows, int c) {
 constexpr int kWarpsPerBlock = 8;
 constexpr int kCellThreads = kWarpsPerBlock * 32;
 
+// ------------------------------------------------- thread-per-cell front ends
+// Most cells need little work: isolated noise points whose stencil holds fewer
+// than minpts points, cells whose neighbour links are found by the first test,
+// border points with a handful of candidate cores.  The *_scan kernels give one
+// thread to each cell and finish those cases inline (bounded work per thread);
+// a cell that needs more is appended to the heavy list and handled by the
+// warp-cooperative *_heavy kernel that follows.
+constexpr int kScanThreadsPerBlock = 256;
+constexpr int kInlineCoreTests = 160;    // points x candidates done by one thread
+constexpr int kInlineLinkTests = 48;     // tests before a link search goes to a warp
+constexpr int kInlineBorderTests = 160;  // non-core points x candidate cores
+
+// warp-aggregated append to the heavy list (all 32 lanes must call it)
+__device__ __forceinline__ void heavy_push(const gdl::Bufs& B, int slot, bool push, int64_t m,
+                                           unsigned long long mask) {
+  const unsigned bal = __ballot_sync(kFull, push);
+  if (!bal) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(bal) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(B.ctr + slot, (unsigned long long)__popc(bal));
+  base = __shfl_sync(kFull, base, leader);
+  if (push) {
+    const unsigned long long at = base + (unsigned long long)__popc(bal & ((1u << lane) - 1u));
+    B.hv_cell[at] = (int)m;
+    B.hv_mask[at] = mask;
+  }
+}
+
+template <int D, bool F32>
+__device__ __forceinline__ void load_point(double* x, float* f, const gdl::Bufs& B, int64_t n,
+                                           int64_t i) {
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    x[k] = B.X[k * n + i];
+    if (F32) f[k] = B.Xf[k * n + i];
+  }
+}
+
+template <int D, bool F32, bool SPARSE>
+__global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::Bufs B, int64_t n) {
+  __shared__ DevParams sP;
+  if (threadIdx.x == 0) sP = *B.P;
+  __syncthreads();
+  const DevParams& P = sP;
+  const GridView<SPARSE> gv = view_of<SPARSE>(B);
+  const OffTab& T = kRows[D - 2];
+  const int lane = threadIdx.x & 31;
+  const int64_t M = *B.M;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  Tally t;
+  for (int64_t m0 = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); m0 < M; m0 += stride) {
+    const int64_t m = m0 + lane;
+    bool push = false;
+    if (m < M) {
+      const int b = B.reps[m], e = B.reps[m + 1], sz = e - b;
+      if (sz >= P.minpts) {
+        push = true;  // dense: the warp kernel marks it
+      } else {
+        const CellXYZ<D> cc = decompose<D>(key_at<SPARSE>(B, b), P);
+        const int64_t Gl = P.G[D - 1], cl = cc.c[D - 1];
+        const int64_t l0 = cl - 2 < 0 ? 0 : cl - 2;
+        const int64_t l1 = cl + 2 >= Gl ? Gl - 1 : cl + 2;
+        int total = 0;
+        for (int r = 0; r < T.n; ++r) {
+          int64_t rowkey = offset_key<D>(cc, T.o[r][0], T.o[r][1], 0, P);
+          if (rowkey < 0) continue;
+          rowkey -= cl;
+          const int2 rg = gv.span((uint64_t)(rowkey + l0), (uint64_t)(rowkey + l1));
+          total += rg.y - rg.x;
+        }
+        if (total < P.minpts) {
+          // fewer candidates than minpts, self included: nothing here is core
+          for (int i = b; i < e; ++i) B.core[i] = 0;
+          B.cellcore[b] = 0;
+          B.cellmin[b] = INT_MAX;
+        } else if (total * sz <= kInlineCoreTests) {
+          int ncore = 0, mn = INT_MAX;
+          for (int i = b; i < e; ++i) {
+            double px[D];
+            float pf[D];
+            load_point<D, F32>(px, pf, B, n, i);
+            int cnt = 0;
+            for (int r = 0; r < T.n && cnt < P.minpts; ++r) {
+              int64_t rowkey = offset_key<D>(cc, T.o[r][0], T.o[r][1], 0, P);
+              if (rowkey < 0) continue;
+              rowkey -= cl;
+              const int2 rg = gv.span((uint64_t)(rowkey + l0), (uint64_t)(rowkey + l1));
+              for (int q = rg.x; q < rg.y && cnt < P.minpts; ++q) {
+                Cand<D, F32> cd;
+                load_cand<D, F32>(cd, B.X, B.Xf, n, q);
+                cnt += pair_test<D, F32>(px, pf, cd, B.X, n, q, true, P, t) ? 1 : 0;
+              }
+            }
+            const bool isc = cnt >= P.minpts;
+            B.core[i] = isc ? 1 : 0;
+            if (isc) {
+              ++ncore;
+              mn = min(mn, (int)B.ids[i]);
+            }
+          }
+          B.cellcore[b] = ncore;
+          B.cellmin[b] = mn;
+        } else {
+          push = true;
+        }
+      }
+    }
+    heavy_push(B, kCtrHeavyCore, push, m, 0);
+  }
+  flush_tally(t, B.ctr);
+}
+
+// Bounded link search between the core points of cells A and B by one thread:
+// 1 found (neighbours both ways), 0 none exists, -1 budget spent.
+template <int D, bool F32>
+__device__ __forceinline__ int inline_link(const gdl::Bufs& B, int64_t n, int bA, int eA, int bB,
+                                           int eB, const DevParams& P, Tally& t) {
+  int budget = kInlineLinkTests;
+  for (int a = bA; a < eA; ++a) {
+    if (!B.core[a]) continue;
+    double ax[D];
+    float af[D];
+    load_point<D, F32>(ax, af, B, n, a);
+    for (int q = bB; q < eB; ++q) {
+      if (!B.core[q]) continue;
+      if (budget-- == 0) return -1;
+      Cand<D, F32> cd;
+      load_cand<D, F32>(cd, B.X, B.Xf, n, q);
+      if (link_test<D, F32>(ax, af, cd, B.X, n, a, q, P, t, B.asym, B.ctr)) return 1;
+    }
+  }
+  return 0;
+}
+
+template <int D, bool F32, bool SPARSE>
+__global__ void __launch_bounds__(kScanThreadsPerBlock)
+k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
+  __shared__ DevParams sP;
+  if (threadIdx.x == 0) sP = *B.P;
+  __syncthreads();
+  const DevParams& P = sP;
+  const GridView<SPARSE> gv = view_of<SPARSE>(B);
+  const OffTab& T = kHalf[D - 2][pass];
+  const int lane = threadIdx.x & 31;
+  const int64_t M = *B.M;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  Tally t;
+  for (int64_t m0 = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); m0 < M; m0 += stride) {
+    const int64_t m = m0 + lane;
+    unsigned long long open = 0;
+    if (m < M) {
+      const int b = B.reps[m];
+      if (B.cellcore[b] > 0) {
+        const int e = B.reps[m + 1];
+        const CellXYZ<D> cc = decompose<D>(key_at<SPARSE>(B, b), P);
+        for (int tt = 0; tt < T.n; ++tt) {
+          const int64_t kb = offset_key<D>(cc, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
+          if (kb < 0) continue;
+          const int2 cb = gv.cell((uint64_t)kb);
+          if (cb.x == cb.y || B.cellcore[cb.x] == 0) continue;
+          if (uf_find(B.parent, b) == uf_find(B.parent, cb.x)) continue;
+          const int r = inline_link<D, F32>(B, n, b, e, cb.x, cb.y, P, t);
+          if (r > 0) uf_union(B.parent, B.cellmin, b, cb.x);
+          else if (r < 0) open |= 1ull << tt;
+        }
+      }
+    }
+    heavy_push(B, kCtrHeavyUnion, open != 0, m, open);
+  }
+  flush_tally(t, B.ctr);
+}
+
+template <int D, bool F32, bool SPARSE>
+__global__ void __launch_bounds__(kScanThreadsPerBlock) k_border_scan(const gdl::Bufs B, int64_t n) {
+  __shared__ DevParams sP;
+  if (threadIdx.x == 0) sP = *B.P;
+  __syncthreads();
+  const DevParams& P = sP;
+  const GridView<SPARSE> gv = view_of<SPARSE>(B);
+  const OffTab& T = kFullSt[D - 2];
+  const int lane = threadIdx.x & 31;
+  const int64_t M = *B.M;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  Tally t;
+  for (int64_t m0 = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); m0 < M; m0 += stride) {
+    const int64_t m = m0 + lane;
+    bool push = false;
+    if (m < M) {
+      const int b = B.reps[m], e = B.reps[m + 1];
+      const int nnc = (e - b) - B.cellcore[b];
+      if (nnc > 0) {
+        const CellXYZ<D> cc = decompose<D>(key_at<SPARSE>(B, b), P);
+        int cores = 0;
+        for (int tt = 0; tt < T.n; ++tt) {
+          const int64_t kb = offset_key<D>(cc, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
+          if (kb < 0) continue;
+          const int2 cb = gv.cell((uint64_t)kb);
+          if (cb.x < cb.y) cores += B.cellcore[cb.x];
+        }
+        if (cores == 0) {
+          // no core point in reach: the non-core points stay NOISE
+        } else if (cores * nnc <= kInlineBorderTests) {
+          for (int i = b; i < e; ++i) {
+            if (B.core[i]) continue;
+            double px[D];
+            float pf[D];
+            load_point<D, F32>(px, pf, B, n, i);
+            int best = INT_MAX;
+            for (int tt = 0; tt < T.n; ++tt) {
+              const int64_t kb = offset_key<D>(cc, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
+              if (kb < 0) continue;
+              const int2 cb = gv.cell((uint64_t)kb);
+              if (cb.x == cb.y || B.cellcore[cb.x] == 0) continue;
+              const int cB = B.cellcid[cb.x];
+              if (cB >= best) continue;
+              for (int q = cb.x; q < cb.y; ++q) {
+                if (!B.core[q]) continue;
+                Cand<D, F32> cd;
+                load_cand<D, F32>(cd, B.X, B.Xf, n, q);
+                if (pair_test<D, F32>(px, pf, cd, B.X, n, q, false, P, t)) {
+                  best = cB;
+                  break;
+                }
+              }
+            }
+            if (best != INT_MAX) B.lab[i] = best;
+          }
+        } else {
+          push = true;
+        }
+      }
+    }
+    heavy_push(B, kCtrHeavyBorder, push, m, 0);
+  }
+  flush_tally(t, B.ctr);
+}
+
 // ------------------------------------------------------------- core flags
 // One warp per non-empty cell.  Dense cells are all core.  Otherwise the warp
 // looks up its candidate rows (5 cells along the last axis each, 5 rows in 2D,
@@ -623,7 +861,7 @@ constexpr int kCellThreads = kWarpsPerBlock * 32;
 // soon as every staged p has reached minpts (own row first, so dense
 // neighbourhoods stop after one tile).
 template <int D, bool F32, bool SPARSE>
-__global__ void __launch_bounds__(kCellThreads) k_core(const gdl::Bufs B, int64_t n) {
+__global__ void __launch_bounds__(kCellThreads) k_core_heavy(const gdl::Bufs B, int64_t n) {
   __shared__ DevParams sP;
   __shared__ WarpStage<D> stage[kWarpsPerBlock];
   __shared__ RowList rows[kWarpsPerBlock];
@@ -641,7 +879,9 @@ __global__ void __launch_bounds__(kCellThreads) k_core(const gdl::Bufs B, int64_
   const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
   Tally t;
   unsigned long long dense = 0;
-  for (int64_t m = (int64_t)blockIdx.x * kWarpsPerBlock + w; m < M; m += W) {
+  const int64_t H = (int64_t)B.ctr[kCtrHeavyCore];
+  for (int64_t h = (int64_t)blockIdx.x * kWarpsPerBlock + w; h < H; h += W) {
+    const int64_t m = B.hv_cell[h];
     const int b = B.reps[m], e = B.reps[m + 1], sz = e - b;
     if (sz >= P.minpts) {
       int mn = INT_MAX;
@@ -715,7 +955,7 @@ __global__ void k_parent_init(const gdl::Bufs B) {
 // that are neighbours both ways (lanes over B's points, A's core points
 // broadcast) and unites the two cells.
 template <int D, bool F32, bool SPARSE>
-__global__ void __launch_bounds__(kCellThreads) k_union(const gdl::Bufs B, int64_t n, int pass) {
+__global__ void __launch_bounds__(kCellThreads) k_union_heavy(const gdl::Bufs B, int64_t n, int pass) {
   __shared__ DevParams sP;
   if (threadIdx.x == 0) sP = *B.P;
   __syncthreads();
@@ -728,16 +968,18 @@ __global__ void __launch_bounds__(kCellThreads) k_union(const gdl::Bufs B, int64
   const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
   const OffTab& T = kHalf[D - 2][pass];
   Tally t;
-  for (int64_t m = (int64_t)blockIdx.x * kWarpsPerBlock + w; m < M; m += W) {
+  const int64_t H = (int64_t)B.ctr[kCtrHeavyUnion];
+  for (int64_t h = (int64_t)blockIdx.x * kWarpsPerBlock + w; h < H; h += W) {
+    const int64_t m = B.hv_cell[h];
+    const unsigned long long open = B.hv_mask[h];
     const int b = B.reps[m];
-    if (B.cellcore[b] == 0) continue;
     const int e = B.reps[m + 1];
     const CellXYZ<D> cc = decompose<D>(key_at<SPARSE>(B, b), P);
     for (int t0 = 0; t0 < T.n; t0 += 32) {
       const int tt = t0 + lane;
       bool cand = false;
       int bB = 0, eB = 0;
-      if (tt < T.n) {
+      if (tt < T.n && ((open >> tt) & 1ull)) {
         const int64_t kb = offset_key<D>(cc, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
         if (kb >= 0) {
           const int2 cb = gv.cell((uint64_t)kb);
@@ -898,7 +1140,7 @@ __global__ void k_label(const gdl::Bufs B, int64_t n) {
 // the stencil cells up in parallel; cells whose cluster id cannot improve any
 // staged point are skipped.
 template <int D, bool F32, bool SPARSE>
-__global__ void __launch_bounds__(kCellThreads) k_border(const gdl::Bufs B, int64_t n) {
+__global__ void __launch_bounds__(kCellThreads) k_border_heavy(const gdl::Bufs B, int64_t n) {
   __shared__ DevParams sP;
   __shared__ WarpStage<D> stage[kWarpsPerBlock];
   __shared__ int sIdx[kWarpsPerBlock][32];
@@ -914,9 +1156,10 @@ __global__ void __launch_bounds__(kCellThreads) k_border(const gdl::Bufs B, int6
   const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
   const OffTab& T = kFullSt[D - 2];
   Tally t;
-  for (int64_t m = (int64_t)blockIdx.x * kWarpsPerBlock + w; m < M; m += W) {
+  const int64_t H = (int64_t)B.ctr[kCtrHeavyBorder];
+  for (int64_t h = (int64_t)blockIdx.x * kWarpsPerBlock + w; h < H; h += W) {
+    const int64_t m = B.hv_cell[h];
     const int b = B.reps[m], e = B.reps[m + 1];
-    if (B.cellcore[b] == e - b) continue;  // no non-core point here
     const CellXYZ<D> cc = decompose<D>(key_at<SPARSE>(B, b), P);
     for (int c0 = b; c0 < e; c0 += 32) {
       // stage this chunk's non-core points
@@ -1112,15 +1355,46 @@ void hash_insert(const unsigned long long* keys, const int* reps, const uint32_t
     }                                                                                       \
   } while (0)
 
+#define GD_DISPATCH_T(dim, f32, sparse, KERNEL, GRID, THREADS, ...)                         \
+  do {                                                                                      \
+    if (dim == 2) {                                                                         \
+      if (f32) {                                                                            \
+        if (sparse) KERNEL<2, true, true><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);            \
+        else KERNEL<2, true, false><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);                  \
+      } else {                                                                              \
+        if (sparse) KERNEL<2, false, true><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);           \
+        else KERNEL<2, false, false><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);                 \
+      }                                                                                     \
+    } else {                                                                                \
+      if (f32) {                                                                            \
+        if (sparse) KERNEL<3, true, true><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);            \
+        else KERNEL<3, true, false><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);                  \
+      } else {                                                                              \
+        if (sparse) KERNEL<3, false, true><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);           \
+        else KERNEL<3, false, false><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);                 \
+      }                                                                                     \
+    }                                                                                       \
+  } while (0)
+
+static int scan_grid(int64_t n, int sms) {
+  return grid_for(n, kScanThreadsPerBlock, sms, 8);
+}
+
 void core(const Bufs& B, int64_t n, int dim, bool f32, bool sparse, int sms, cudaStream_t s) {
-  int g = sms * 8;
-  GD_DISPATCH(dim, f32, sparse, k_core, g, B, n);
+  cudaMemsetAsync(B.ctr + kCtrHeavyCore, 0, 8, s);
+  GD_DISPATCH_T(dim, f32, sparse, k_core_scan, scan_grid(n, sms), kScanThreadsPerBlock, B, n);
+  GD_DISPATCH(dim, f32, sparse, k_core_heavy, sms * 8, B, n);
 }
 
 void unite(const Bufs& B, int64_t n, int dim, bool f32, bool sparse, int sms, cudaStream_t s) {
   k_parent_init<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
   int g = sms * 8;
-  for (int pass = 0; pass < 2; ++pass) GD_DISPATCH(dim, f32, sparse, k_union, g, B, n, pass);
+  for (int pass = 0; pass < 2; ++pass) {
+    cudaMemsetAsync(B.ctr + kCtrHeavyUnion, 0, 8, s);
+    GD_DISPATCH_T(dim, f32, sparse, k_union_scan, scan_grid(n, sms), kScanThreadsPerBlock, B, n,
+                  pass);
+    GD_DISPATCH(dim, f32, sparse, k_union_heavy, g, B, n, pass);
+  }
   k_compress<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
   k_asym_resolve<<<1, 32, 0, s>>>(B);
 }
@@ -1134,8 +1408,9 @@ void label(const Bufs& B, int64_t n, int sms, cudaStream_t s) {
 }
 
 void border(const Bufs& B, int64_t n, int dim, bool f32, bool sparse, int sms, cudaStream_t s) {
-  int g = sms * 8;
-  GD_DISPATCH(dim, f32, sparse, k_border, g, B, n);
+  cudaMemsetAsync(B.ctr + kCtrHeavyBorder, 0, 8, s);
+  GD_DISPATCH_T(dim, f32, sparse, k_border_scan, scan_grid(n, sms), kScanThreadsPerBlock, B, n);
+  GD_DISPATCH(dim, f32, sparse, k_border_heavy, sms * 8, B, n);
 }
 
 void scatter_labels(const Bufs& B, int64_t n, int* out, uint8_t* core_out, int sms,
