@@ -318,7 +318,8 @@ gd_status gd_index_build(gd_ctx* ctx, const gd_points* pts, double eps) {
   if ((st = ctx->ensure(ctx->vals0, n * 4, "ids")) != GD_OK) return st;
   if ((st = ctx->ensure(ctx->vals1, n * 4, "ids")) != GD_OK) return st;
   if ((st = ctx->ensure(ctx->X, (size_t)n * D * 8, "sorted coordinates")) != GD_OK) return st;
-  if (ctx->f32 && (st = ctx->ensure(ctx->Xf, (size_t)n * D * 4, "f32 coordinates")) != GD_OK)
+  const bool want_xf = ctx->f32 || ctx->hp.prune;  // centred float32 copy
+  if (want_xf && (st = ctx->ensure(ctx->Xf, (size_t)n * D * 4, "f32 coordinates")) != GD_OK)
     return st;
   uint64_t hcap = 1024;
   if (ctx->sparse) {
@@ -352,7 +353,7 @@ gd_status gd_index_build(gd_ctx* ctx, const gd_points* pts, double eps) {
     ctx->skeys = kb[r];
   }
   ctx->sids = vb[r];
-  gdl::gather(ctx->dpts, ctx->sids, n, D, ctx->f32, ctx->dP(), static_cast<double*>(ctx->X.p),
+  gdl::gather(ctx->dpts, ctx->sids, n, D, want_xf, ctx->dP(), static_cast<double*>(ctx->X.p),
               static_cast<float*>(ctx->Xf.p), ctx->sms, s);
   // cell runs and the cell lookup (dense table or hash of occupied cells)
   uint32_t* fl = static_cast<uint32_t*>(ctx->runfl.p);

@@ -45,7 +45,11 @@ struct DevParams {
   int32_t key_bits;
   int32_t flags;       // kFlag*
   int32_t sparse;      // 1: hash of occupied cells (64-bit keys); 0: dense table
-  int32_t pad;
+  int32_t prune;       // 1: cell-level inside/outside classification enabled
+  float inv_f32;       // fl32(1 / f)
+  float uerr;          // bound on the error of a point's in-cell position (cell units)
+  float thr_in;        // sum of squared max distances (cell units) below: all neighbours
+  float thr_out;       // sum of squared min distances (cell units) above: none
 };
 
 constexpr int kFlagNonFinite = 1;     // NaN or Inf coordinate

@@ -190,7 +190,7 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   uint32_t* ids = vb[r];
   double* X = reinterpret_cast<double*>(base + kOffX);
   float* Xf = reinterpret_cast<float*>(base + kOffXf);
-  gdl::gather(coords_dev, ids, n, D, f32, dP, X, Xf, sms, s);
+  gdl::gather(coords_dev, ids, n, D, f32 || hp.prune, dP, X, Xf, sms, s);
   uint32_t* fl = reinterpret_cast<uint32_t*>(base + kOffRunfl);
   uint32_t* pos = reinterpret_cast<uint32_t*>(base + kOffRunpos);
   int* reps = reinterpret_cast<int*>(base + kOffReps);

@@ -184,6 +184,22 @@ k_params(const long long* __restrict__ partial, int nblocks, DevParams* P, doubl
                     H < 4.0 * e2;
     p.eps2_lo32 = ok ? __double2float_rd(L) : -1.0f;
     p.eps2_hi32 = ok ? __double2float_ru(H) : -1.0f;
+    // Cell-level classification.  A point's position inside its cell,
+    // u_k = (fl32(x_k - c_k) - o_k) / f with o_k the cell origin in the same
+    // centred float32 frame, is within uerr of the truth (coordinate and origin
+    // errors 2 ea, three float32 roundings, and the 2^-20-cell slack of the
+    // float64 cell assignment of candidate points).  A stencil cell whose
+    // farthest corner is within eps (1 - 2^-7) holds only neighbours (float64
+    // d2 <= eps2_in, so the box test passes too); one whose nearest face is
+    // beyond eps (1 + 2^-7) holds none.  Thresholds are in squared cell units.
+    const double inv_m2 = (eps / p.f) * (eps / p.f);
+    const double uerr = 4.0 * ea / p.f + 1.0 / 262144.0;               // + 2^-18
+    const double mi = 1.0 - 1.0 / 128.0, mo = 1.0 + 1.0 / 128.0;
+    p.inv_f32 = __double2float_rn(1.0 / p.f);
+    p.uerr = __double2float_ru(uerr);
+    p.thr_in = __double2float_rd(inv_m2 * mi * mi * (1.0 - 1.0 / 65536.0));
+    p.thr_out = __double2float_ru(inv_m2 * mo * mo * (1.0 + 1.0 / 65536.0));
+    p.prune = (!(fl & kFlagNoShortcut) && uerr <= 1.0 / 256.0 && R < 1e30 && e2 > 1e-30) ? 1 : 0;
   }
   p.flags = fl;
   *P = p;
@@ -614,6 +630,45 @@ __device__ __forceinline__ int row_pos(const RowList& RL, int nrows, int c) {
 constexpr int kWarpsPerBlock = 8;
 constexpr int kCellThreads = kWarpsPerBlock * 32;
 
+// ----------------------------------------------- cell-level classification
+// Origin (low corner) of cell cc in the centred float32 frame.
+template <int D>
+__device__ __forceinline__ void cell_origin32(const CellXYZ<D>& cc, const DevParams& P, float* o) {
+#pragma unroll
+  for (int k = 0; k < D; ++k)
+    o[k] = __double2float_rn(
+        __dsub_rn(__dadd_rn(P.lo[k], __dmul_rn((double)cc.c[k], P.f)), P.centre[k]));
+}
+
+// A point's position inside its own cell, in cell units (error <= P.uerr).
+template <int D>
+__device__ __forceinline__ void frac_pos(const float* xf, const float* o, const DevParams& P,
+                                         float* u) {
+#pragma unroll
+  for (int k = 0; k < D; ++k) u[k] = __fmul_rn(__fsub_rn(xf[k], o[k]), P.inv_f32);
+}
+
+// Cell at offset (ox, oy, oz) from the point's cell: 1 every point in it is a
+// neighbour (both ways), -1 none is, 0 must be tested.
+template <int D>
+__device__ __forceinline__ int classify(const float* u, int ox, int oy, int oz,
+                                        const DevParams& P) {
+  const int off[3] = {ox, oy, oz};
+  float smax = 0.0f, smin = 0.0f;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const float a = u[k] - (float)off[k];  // position relative to the box [off, off + 1]
+    const float b = a - 1.0f;
+    const float mx = fmaxf(fabsf(a), fabsf(b)) + P.uerr;
+    const float mn = fmaxf(fmaxf(-a, b) - P.uerr, 0.0f);
+    smax = fmaf(mx, mx, smax);
+    smin = fmaf(mn, mn, smin);
+  }
+  if (smax <= P.thr_in) return 1;
+  if (smin >= P.thr_out) return -1;
+  return 0;
+}
+
 // ------------------------------------------------- thread-per-cell front ends
 // Most cells need little work: isolated noise points whose stencil holds fewer
 // than minpts points, cells whose neighbour links are found by the first test,
@@ -645,11 +700,11 @@ __device__ __forceinline__ void heavy_push(const gdl::Bufs& B, int slot, bool pu
 
 template <int D, bool F32>
 __device__ __forceinline__ void load_point(double* x, float* f, const gdl::Bufs& B, int64_t n,
-                                           int64_t i) {
+                                           int64_t i, bool prune) {
 #pragma unroll
   for (int k = 0; k < D; ++k) {
     x[k] = B.X[k * n + i];
-    if (F32) f[k] = B.Xf[k * n + i];
+    if (F32 || prune) f[k] = B.Xf[k * n + i];
   }
 }
 
@@ -662,6 +717,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::B
   const GridView<SPARSE> gv = view_of<SPARSE>(B);
   const OffTab& T = kRows[D - 2];
   const int lane = threadIdx.x & 31;
+  const bool prune = P.prune != 0;
   const int64_t M = *B.M;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   Tally t;
@@ -685,27 +741,59 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::B
           const int2 rg = gv.span((uint64_t)(rowkey + l0), (uint64_t)(rowkey + l1));
           total += rg.y - rg.x;
         }
-        if (total < P.minpts) {
-          // fewer candidates than minpts, self included: nothing here is core
-          for (int i = b; i < e; ++i) B.core[i] = 0;
-          B.cellcore[b] = 0;
-          B.cellmin[b] = INT_MAX;
-        } else if (total * sz <= kInlineCoreTests) {
-          int ncore = 0, mn = INT_MAX;
-          for (int i = b; i < e; ++i) {
+        int ncore = 0, mn = INT_MAX;
+        if (total >= P.minpts) {
+          float o[D];
+          if (prune) cell_origin32<D>(cc, P, o);
+          for (int i = b; i < e && !push; ++i) {
             double px[D];
-            float pf[D];
-            load_point<D, F32>(px, pf, B, n, i);
-            int cnt = 0;
-            for (int r = 0; r < T.n && cnt < P.minpts; ++r) {
-              int64_t rowkey = offset_key<D>(cc, T.o[r][0], T.o[r][1], 0, P);
-              if (rowkey < 0) continue;
-              rowkey -= cl;
-              const int2 rg = gv.span((uint64_t)(rowkey + l0), (uint64_t)(rowkey + l1));
-              for (int q = rg.x; q < rg.y && cnt < P.minpts; ++q) {
-                Cand<D, F32> cd;
-                load_cand<D, F32>(cd, B.X, B.Xf, n, q);
-                cnt += pair_test<D, F32>(px, pf, cd, B.X, n, q, true, P, t) ? 1 : 0;
+            float pf[D], u[D];
+            load_point<D, F32>(px, pf, B, n, i, prune);
+            if (prune) frac_pos<D>(pf, o, P, u);
+            // pass 1: cells wholly inside count without a test; sum the rest
+            int cnt = 0, ptot = total;
+            if (prune) {
+              ptot = 0;
+              for (int r = 0; r < T.n; ++r) {
+                int64_t rowkey = offset_key<D>(cc, T.o[r][0], T.o[r][1], 0, P);
+                if (rowkey < 0) continue;
+                rowkey -= cl;
+                for (int64_t z = l0; z <= l1; ++z) {
+                  const int2 c = gv.cell((uint64_t)(rowkey + z));
+                  if (c.x == c.y) continue;
+                  const int d = (int)(z - cl);
+                  const int cls = D == 3 ? classify<D>(u, T.o[r][0], T.o[r][1], d, P)
+                                         : classify<D>(u, T.o[r][0], d, 0, P);
+                  if (cls > 0) cnt += c.y - c.x;
+                  else if (cls == 0) ptot += c.y - c.x;
+                }
+              }
+            }
+            if (cnt < P.minpts && cnt + ptot >= P.minpts) {
+              if (ptot > kInlineCoreTests) {
+                push = true;  // too many candidates for one thread
+                break;
+              }
+              // pass 2: test the undecided cells
+              for (int r = 0; r < T.n && cnt < P.minpts; ++r) {
+                int64_t rowkey = offset_key<D>(cc, T.o[r][0], T.o[r][1], 0, P);
+                if (rowkey < 0) continue;
+                rowkey -= cl;
+                for (int64_t z = l0; z <= l1 && cnt < P.minpts; ++z) {
+                  const int2 c = gv.cell((uint64_t)(rowkey + z));
+                  if (c.x == c.y) continue;
+                  if (prune) {
+                    const int d = (int)(z - cl);
+                    const int cls = D == 3 ? classify<D>(u, T.o[r][0], T.o[r][1], d, P)
+                                           : classify<D>(u, T.o[r][0], d, 0, P);
+                    if (cls != 0) continue;
+                  }
+                  for (int q = c.x; q < c.y && cnt < P.minpts; ++q) {
+                    Cand<D, F32> cd;
+                    load_cand<D, F32>(cd, B.X, B.Xf, n, q);
+                    cnt += pair_test<D, F32>(px, pf, cd, B.X, n, q, true, P, t) ? 1 : 0;
+                  }
+                }
               }
             }
             const bool isc = cnt >= P.minpts;
@@ -715,10 +803,12 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::B
               mn = min(mn, (int)B.ids[i]);
             }
           }
+        } else {
+          for (int i = b; i < e; ++i) B.core[i] = 0;  // fewer candidates than minpts
+        }
+        if (!push) {
           B.cellcore[b] = ncore;
           B.cellmin[b] = mn;
-        } else {
-          push = true;
         }
       }
     }
@@ -728,16 +818,28 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::B
 }
 
 // Bounded link search between the core points of cells A and B by one thread:
-// 1 found (neighbours both ways), 0 none exists, -1 budget spent.
+// 1 found (neighbours both ways), 0 none exists, -1 budget spent.  With cell
+// classification, a core point of A that has all of B within reach links at
+// once (B holds a core point), and one that has none of B in reach is skipped.
 template <int D, bool F32>
 __device__ __forceinline__ int inline_link(const gdl::Bufs& B, int64_t n, int bA, int eA, int bB,
-                                           int eB, const DevParams& P, Tally& t) {
+                                           int eB, const float* oA, int ox, int oy, int oz,
+                                           const DevParams& P, Tally& t) {
+  const bool prune = P.prune != 0;
   int budget = kInlineLinkTests;
+  bool skipped = false;
   for (int a = bA; a < eA; ++a) {
     if (!B.core[a]) continue;
     double ax[D];
     float af[D];
-    load_point<D, F32>(ax, af, B, n, a);
+    load_point<D, F32>(ax, af, B, n, a, prune);
+    if (prune) {
+      float u[D];
+      frac_pos<D>(af, oA, P, u);
+      const int cls = classify<D>(u, ox, oy, oz, P);
+      if (cls > 0) return 1;
+      if (cls < 0) continue;
+    }
     for (int q = bB; q < eB; ++q) {
       if (!B.core[q]) continue;
       if (budget-- == 0) return -1;
@@ -746,6 +848,7 @@ __device__ __forceinline__ int inline_link(const gdl::Bufs& B, int64_t n, int bA
       if (link_test<D, F32>(ax, af, cd, B.X, n, a, q, P, t, B.asym, B.ctr)) return 1;
     }
   }
+  (void)skipped;
   return 0;
 }
 
@@ -770,13 +873,16 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
       if (B.cellcore[b] > 0) {
         const int e = B.reps[m + 1];
         const CellXYZ<D> cc = decompose<D>(key_at<SPARSE>(B, b), P);
+        float oA[D];
+        if (P.prune) cell_origin32<D>(cc, P, oA);
         for (int tt = 0; tt < T.n; ++tt) {
           const int64_t kb = offset_key<D>(cc, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
           if (kb < 0) continue;
           const int2 cb = gv.cell((uint64_t)kb);
           if (cb.x == cb.y || B.cellcore[cb.x] == 0) continue;
           if (uf_find(B.parent, b) == uf_find(B.parent, cb.x)) continue;
-          const int r = inline_link<D, F32>(B, n, b, e, cb.x, cb.y, P, t);
+          const int r = inline_link<D, F32>(B, n, b, e, cb.x, cb.y, oA, T.o[tt][0], T.o[tt][1],
+                                            T.o[tt][2], P, t);
           if (r > 0) uf_union(B.parent, B.cellmin, b, cb.x);
           else if (r < 0) open |= 1ull << tt;
         }
@@ -796,6 +902,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_border_scan(const gdl:
   const GridView<SPARSE> gv = view_of<SPARSE>(B);
   const OffTab& T = kFullSt[D - 2];
   const int lane = threadIdx.x & 31;
+  const bool prune = P.prune != 0;
   const int64_t M = *B.M;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   Tally t;
@@ -814,24 +921,39 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_border_scan(const gdl:
           const int2 cb = gv.cell((uint64_t)kb);
           if (cb.x < cb.y) cores += B.cellcore[cb.x];
         }
-        if (cores == 0) {
-          // no core point in reach: the non-core points stay NOISE
-        } else if (cores * nnc <= kInlineBorderTests) {
-          for (int i = b; i < e; ++i) {
+        if (cores > 0) {
+          // no core point in reach: the non-core points stay NOISE (else below)
+          float o[D];
+          if (prune) cell_origin32<D>(cc, P, o);
+          int budget = kInlineBorderTests;
+          for (int i = b; i < e && !push; ++i) {
             if (B.core[i]) continue;
             double px[D];
-            float pf[D];
-            load_point<D, F32>(px, pf, B, n, i);
+            float pf[D], u[D];
+            load_point<D, F32>(px, pf, B, n, i, prune);
+            if (prune) frac_pos<D>(pf, o, P, u);
             int best = INT_MAX;
-            for (int tt = 0; tt < T.n; ++tt) {
+            for (int tt = 0; tt < T.n && !push; ++tt) {
               const int64_t kb = offset_key<D>(cc, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
               if (kb < 0) continue;
               const int2 cb = gv.cell((uint64_t)kb);
               if (cb.x == cb.y || B.cellcore[cb.x] == 0) continue;
               const int cB = B.cellcid[cb.x];
               if (cB >= best) continue;
+              if (prune) {
+                const int cls = classify<D>(u, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
+                if (cls > 0) {
+                  best = cB;  // every point of that cell, a core among them, is in reach
+                  continue;
+                }
+                if (cls < 0) continue;
+              }
               for (int q = cb.x; q < cb.y; ++q) {
                 if (!B.core[q]) continue;
+                if (budget-- == 0) {
+                  push = true;  // too much for one thread
+                  break;
+                }
                 Cand<D, F32> cd;
                 load_cand<D, F32>(cd, B.X, B.Xf, n, q);
                 if (pair_test<D, F32>(px, pf, cd, B.X, n, q, false, P, t)) {
@@ -840,10 +962,8 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_border_scan(const gdl:
                 }
               }
             }
-            if (best != INT_MAX) B.lab[i] = best;
+            if (!push && best != INT_MAX) B.lab[i] = best;
           }
-        } else {
-          push = true;
         }
       }
     }
@@ -875,8 +995,7 @@ __global__ void __launch_bounds__(kCellThreads) k_core_heavy(const gdl::Bufs B, 
   const int nrows = kRows[D - 2].n;
   const double* __restrict__ X = B.X;
   const float* __restrict__ Xf = B.Xf;
-  const int64_t M = *B.M;
-  const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
+    const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
   Tally t;
   unsigned long long dense = 0;
   const int64_t H = (int64_t)B.ctr[kCtrHeavyCore];
@@ -964,8 +1083,7 @@ __global__ void __launch_bounds__(kCellThreads) k_union_heavy(const gdl::Bufs B,
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const double* __restrict__ X = B.X;
   const float* __restrict__ Xf = B.Xf;
-  const int64_t M = *B.M;
-  const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
+    const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
   const OffTab& T = kHalf[D - 2][pass];
   Tally t;
   const int64_t H = (int64_t)B.ctr[kCtrHeavyUnion];
@@ -1152,8 +1270,7 @@ __global__ void __launch_bounds__(kCellThreads) k_border_heavy(const gdl::Bufs B
   WarpStage<D>& S = stage[w];
   const double* __restrict__ X = B.X;
   const float* __restrict__ Xf = B.Xf;
-  const int64_t M = *B.M;
-  const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
+    const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
   const OffTab& T = kFullSt[D - 2];
   Tally t;
   const int64_t H = (int64_t)B.ctr[kCtrHeavyBorder];

@@ -184,3 +184,16 @@ def test_sparse_grid_vs_oracle(gpu_ctx, oracle, prec, d):
     olab, ocore, _ = oracle.oracle_dbscan(pts, 0.05, 6)
     assert np.array_equal(core, ocore)
     assert np.array_equal(lab, olab)
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_far_from_origin_disables_shortcuts(gpu_ctx, oracle, prec):
+    """|x| far above eps * 2^30: no box-test shortcut, no float32 filter, no cell
+    classification -- every decision is the plain float64 predicate."""
+    rng = np.random.default_rng(77)
+    pts = 3e9 + np.concatenate([rng.normal(0, 1.0, (3000, 2)), rng.uniform(-20, 20, (500, 2))])
+    lab, core = run(gpu_ctx, pts, 0.25, 5, prec)
+    assert gpu_ctx.stats()["precision_used"] == 0
+    olab, ocore, _ = oracle.oracle_dbscan(pts, 0.25, 5)
+    assert np.array_equal(core, ocore)
+    assert np.array_equal(lab, olab)
