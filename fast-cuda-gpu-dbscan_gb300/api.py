@@ -43,6 +43,11 @@ class GdPoints(ctypes.Structure):
                 ("on_device", ctypes.c_int32)]
 
 
+class GdInstance(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("dim", ctypes.c_int32), ("minpts", ctypes.c_int32),
+                ("eps", ctypes.c_double)]
+
+
 class GdStats(ctypes.Structure):
     _fields_ = [(name, ctypes.c_int64) for name in (
         "n_points", "n_clusters", "n_noise", "n_core", "n_border", "n_cells", "n_dense_cells",
@@ -69,6 +74,7 @@ SIGNATURES = [
     ("gd_ctx_set_stream", ctypes.c_int, [_P, _P]),
     ("gd_ctx_set_precision", ctypes.c_int, [_P, ctypes.c_int32]),
     ("gd_ctx_set_cell_mult", ctypes.c_int, [_P, ctypes.c_double]),
+    ("gd_ctx_set_cell_mults", ctypes.c_int, [_P, ctypes.c_double, ctypes.c_double]),
     ("gd_ctx_trim", ctypes.c_int, [_P]),
     ("gd_index_build", ctypes.c_int, [_P, ctypes.POINTER(GdPoints), ctypes.c_double]),
     ("gd_expand", ctypes.c_int, [_P, ctypes.c_int32]),
@@ -77,6 +83,8 @@ SIGNATURES = [
     ("gd_dbscan", ctypes.c_int, [_P, ctypes.POINTER(GdPoints), ctypes.c_double, ctypes.c_int32,
                                  _P, ctypes.POINTER(GdStats)]),
     ("gd_get_stats", ctypes.c_int, [_P, ctypes.POINTER(GdStats)]),
+    ("gd_batch_dbscan", ctypes.c_int, [_P, ctypes.c_int32, _P, _P, ctypes.c_int32, _P, _P,
+                                       ctypes.POINTER(GdStats)]),
     ("gd_dbscan_noalloc", ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int32, ctypes.c_double,
                                          ctypes.c_int32, ctypes.c_int32, _P,
                                          ctypes.POINTER(ctypes.c_int64), _P]),
@@ -168,6 +176,38 @@ class Context:
 
     def set_stream(self, stream_handle: int | None) -> None:
         _check(self._lib.gd_ctx_set_stream(self._ctx, stream_handle or None))
+
+    def set_cell_mults(self, mult2d: float, mult3d: float) -> None:
+        _check(self._lib.gd_ctx_set_cell_mults(self._ctx, mult2d, mult3d))
+
+    def batch_dbscan(self, instances, with_stats: bool = False):
+        """Cluster many independent instances in one run.
+
+        ``instances``: list of (points (n, dim) float64, eps, minpts).  Returns a
+        list of per-instance label arrays (cluster ids restart at 0 in each)."""
+        desc = (GdInstance * len(instances))()
+        parts = []
+        for i, (pts, eps, mp) in enumerate(instances):
+            a = np.ascontiguousarray(pts, dtype=np.float64)
+            desc[i].n = a.shape[0]
+            desc[i].dim = a.shape[1]
+            desc[i].minpts = int(mp)
+            desc[i].eps = float(eps)
+            parts.append(a.reshape(-1))
+        coords = np.concatenate(parts) if parts else np.zeros(0)
+        total = int(sum(d.n for d in desc))
+        lab = np.empty(max(total, 1), dtype=np.int32)
+        kc = np.zeros(max(len(instances), 1), dtype=np.int64)
+        st = GdStats()
+        _check(self._lib.gd_batch_dbscan(self._ctx, len(instances), desc, coords.ctypes.data, 0,
+                                         lab.ctypes.data, kc.ctypes.data, ctypes.byref(st)))
+        out, off = [], 0
+        for d in desc:
+            out.append(lab[off: off + d.n].copy())
+            off += d.n
+        if with_stats:
+            return out, kc[: len(instances)].copy(), st.as_dict()
+        return out
 
     def trim(self) -> None:
         _check(self._lib.gd_ctx_trim(self._ctx))

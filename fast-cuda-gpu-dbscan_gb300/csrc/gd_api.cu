@@ -1,18 +1,23 @@
 // gd_api.cu -- the C ABI (include/gbdbscan.h): contexts, device memory, and the
-// order in which the kernels of gd_pipeline.cu run for one instance.
+// order in which the kernels of gd_pipeline.cu run.
 //
-// Stage order on the context's stream (no host round-trip except one 240-byte
-// read of the grid parameters, which sizes the cell table):
-//   gd_index_build: [H2D] bbox -> params -> (read params) -> keys -> radix sort
-//                   -> gather (sorted SoA f64 [+ centred f32]) -> cell runs
-//                   -> dense cell table (counts + exclusive scan)
-//   gd_expand:      core flags -> union-find (near pass, far pass, compress)
-//                   -> root marks -> scan (cluster ids) -> labels -> borders
-//   gd_get_result:  scatter labels/core flags to caller order -> [D2H]
+// A run clusters K >= 1 instances (gd_index_build/gd_dbscan: K = 1;
+// gd_batch_dbscan: K = count).  Stage order on the context's stream; the only
+// host round-trip inside a run is one read of the 64-byte run layout, which
+// sizes the key width, the cell tables and the hash:
+//   build:  [H2D] per-instance bbox -> grids -> layout -> (read layout) -> keys
+//           -> radix sort -> gather (sorted SoA f64 [+ centred f32]) -> cell runs
+//           -> dense cell tables (counts + exclusive scan) / hash of occupied cells
+//   expand: core flags -> union-find (near pass, far pass, compress, merge
+//           replay) -> root marks -> scan (cluster numbers) -> labels -> borders
+//   finish: scatter labels/core flags to caller order -> [D2H]
+#include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "gbdbscan.h"
 #include "gd_launch.h"
@@ -34,10 +39,16 @@ gd_status cuda_fail(cudaError_t e, const char* what) {
   return fail(GD_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-#define GD_CUDA(call, what)                         \
-  do {                                              \
-    cudaError_t e_ = (call);                        \
+#define GD_CUDA(call, what)                            \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
     if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+#define GD_TRY(expr)            \
+  do {                          \
+    gd_status s_ = (expr);      \
+    if (s_ != GD_OK) return s_; \
   } while (0)
 
 struct DevBuf {
@@ -46,6 +57,9 @@ struct DevBuf {
 };
 
 constexpr double kDefaultCellMult = 0.5 * (1.0 + 1.0 / 65536.0);
+// largest multipliers allowed: cell diagonal below eps (1 - 2^-20)
+constexpr double kMaxCellMult2 = 0.70710678118654752 * (1.0 - 1.0 / 1048576.0);
+constexpr double kMaxCellMult3 = 0.57735026918962576 * (1.0 - 1.0 / 1048576.0);
 
 size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -61,28 +75,27 @@ struct gd_ctx {
   cudaStream_t own = nullptr;
   cudaStream_t stream = nullptr;
   int precision = GD_PREC_FP64;
-  double cell_mult = 0.0;
+  double mult2 = kDefaultCellMult, mult3 = kDefaultCellMult;
 
-  DevBuf pts, keys0, keys1, vals0, vals1, X, Xf, table, reps, runfl, runpos, core, cellcore,
-      cellmin, parent, Fmark, cellcid, lab, out, coreout, sorttemp, scantemp, partial, small,
-      asym, hkeys, hvals, hvcell, hvmask;
+  DevBuf coords, inst, chunks, Pv, Bi, bbox, keys0, keys1, vals0, vals1, X, Xf, table, hkeys,
+      hvals, reps, runfl, runpos, core, cellcore, cellmin, parent, Fmark, cellcid, lab, asym,
+      hvcell, hvmask, out, coreout, sorttemp, scantemp, small, kcount;
 
-  // state of the current instance
+  // the current run
   int stage = 0;  // 0: nothing, 1: indexed, 2: expanded
+  int K = 0;
   int64_t n = 0;
-  int dim = 2;
-  double eps = 0;
-  int minpts = 0;
-  bool f32 = false;
-  gd::DevParams hp{};
-  const double* dpts = nullptr;
+  int dims = 0;   // bit 0: 2D instances present, bit 1: 3D
+  bool f32 = false, key64 = false, xf = false;
+  gd::BatchInfo bi{};
+  std::vector<gd::InstDesc> hdesc;
+  std::vector<gd::Chunk> hchunk;
+  const double* coords_ptr = nullptr;  // the run's points on the device
   void* skeys = nullptr;
   uint32_t* sids = nullptr;
-  bool sparse = false;
   uint32_t hmask = 0;
   cudaEvent_t ev[8] = {};
   gd_stats st{};
-  int bbox_blocks = 0;
   int launches = 0;
 
   gd_status ensure(DevBuf& b, size_t bytes, const char* what) {
@@ -100,30 +113,35 @@ struct gd_ctx {
     return GD_OK;
   }
 
-  void free_all() {
-    DevBuf* all[] = {&pts, &keys0, &keys1, &vals0, &vals1, &X, &Xf, &table, &reps, &runfl,
-                     &runpos, &core, &cellcore, &cellmin, &parent, &Fmark, &cellcid, &lab,
-                     &out, &coreout, &sorttemp, &scantemp, &partial, &small, &asym, &hkeys,
-                     &hvals, &hvcell, &hvmask};
-    for (DevBuf* b : all) {
+  void free_all(bool keep_small) {
+    DevBuf* a[] = {&coords, &inst,   &chunks,   &Pv,      &Bi,     &bbox,     &keys0,
+                   &keys1,  &vals0,  &vals1,    &X,       &Xf,     &table,    &hkeys,
+                   &hvals,  &reps,   &runfl,    &runpos,  &core,   &cellcore, &cellmin,
+                   &parent, &Fmark,  &cellcid,  &lab,     &asym,   &hvcell,   &hvmask,
+                   &out,    &coreout, &sorttemp, &scantemp, &small, &kcount};
+    for (DevBuf* b : a) {
+      if (keep_small && b == &small) continue;
       if (b->p) cudaFree(b->p);
       b->p = nullptr;
       b->bytes = 0;
     }
   }
 
-  // small block: params | M | K | flags | counters
-  gd::DevParams* dP() { return static_cast<gd::DevParams*>(small.p); }
-  uint32_t* dM() { return reinterpret_cast<uint32_t*>(static_cast<char*>(small.p) + 512); }
-  uint32_t* dK() { return reinterpret_cast<uint32_t*>(static_cast<char*>(small.p) + 516); }
-  int* dFlags() { return reinterpret_cast<int*>(static_cast<char*>(small.p) + 520); }
+  // small block: M | total clusters | counters
+  uint32_t* dM() { return static_cast<uint32_t*>(small.p); }
+  uint32_t* dK() { return reinterpret_cast<uint32_t*>(static_cast<char*>(small.p) + 4); }
   unsigned long long* dCtr() {
-    return reinterpret_cast<unsigned long long*>(static_cast<char*>(small.p) + 640);
+    return reinterpret_cast<unsigned long long*>(static_cast<char*>(small.p) + 128);
   }
 
   gdl::Bufs bufs() {
     gdl::Bufs B;
-    B.P = dP();
+    B.coords = coords_ptr;
+    B.inst = static_cast<const gd::InstDesc*>(inst.p);
+    B.chunks = static_cast<const gd::Chunk*>(chunks.p);
+    B.Pv = static_cast<gd::DevParams*>(Pv.p);
+    B.Bi = static_cast<gd::BatchInfo*>(Bi.p);
+    B.bbox = static_cast<long long*>(bbox.p);
     B.keys = skeys;
     B.ids = sids;
     B.reps = static_cast<int*>(reps.p);
@@ -150,6 +168,249 @@ struct gd_ctx {
     return B;
   }
 };
+
+namespace {
+
+// Point runs of at most kChunkPoints points, one instance each.
+void make_chunks(const std::vector<gd::InstDesc>& desc, std::vector<gd::Chunk>& out) {
+  out.clear();
+  for (size_t i = 0; i < desc.size(); ++i)
+    for (int64_t b = 0; b < desc[i].n; b += gd::kChunkPoints) {
+      gd::Chunk c;
+      c.inst = (int32_t)i;
+      c.pad = 0;
+      c.begin = desc[i].pt_off + b;
+      c.end = desc[i].pt_off + std::min<int64_t>(desc[i].n, b + gd::kChunkPoints);
+      out.push_back(c);
+    }
+}
+
+// Build stage of a run: ctx->hdesc (internal order, 2D instances first) and
+// ctx->coords_ptr (device) are set by the caller.
+gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point) {
+  cudaStream_t s = ctx->stream;
+  const int K = (int)ctx->hdesc.size();
+  ctx->K = K;
+  int64_t n = 0;
+  for (const auto& d : ctx->hdesc) n += d.n;
+  ctx->n = n;
+  make_chunks(ctx->hdesc, ctx->hchunk);
+  const int nch = (int)ctx->hchunk.size();
+  GD_TRY(ctx->ensure(ctx->inst, K * sizeof(gd::InstDesc), "instance table"));
+  GD_TRY(ctx->ensure(ctx->chunks, std::max(1, nch) * sizeof(gd::Chunk), "chunk table"));
+  GD_TRY(ctx->ensure(ctx->Pv, K * sizeof(gd::DevParams), "instance parameters"));
+  GD_TRY(ctx->ensure(ctx->Bi, sizeof(gd::BatchInfo), "run layout"));
+  GD_TRY(ctx->ensure(ctx->bbox, K * 6 * 8, "bounding boxes"));
+  GD_CUDA(cudaMemcpyAsync(ctx->inst.p, ctx->hdesc.data(), K * sizeof(gd::InstDesc),
+                          cudaMemcpyHostToDevice, s), "upload instances");
+  if (nch)
+    GD_CUDA(cudaMemcpyAsync(ctx->chunks.p, ctx->hchunk.data(), nch * sizeof(gd::Chunk),
+                            cudaMemcpyHostToDevice, s), "upload chunks");
+  GD_CUDA(cudaMemsetAsync(ctx->small.p, 0, ctx->small.bytes, s), "clear counters");
+  GD_CUDA(cudaMemsetAsync(ctx->Bi.p, 0, sizeof(gd::BatchInfo), s), "clear layout");
+  gdl::Bufs B = ctx->bufs();
+  gdl::grids(B, K, nch, ctx->mult2, ctx->mult3, dense_floor, dense_per_point, s);
+  GD_CUDA(cudaMemcpyAsync(&ctx->bi, ctx->Bi.p, sizeof(gd::BatchInfo), cudaMemcpyDeviceToHost, s),
+          "read run layout");
+  GD_CUDA(cudaStreamSynchronize(s), "grid parameters");
+  const gd::BatchInfo& bi = ctx->bi;
+  if (bi.flags & gd::kFlagNonFinite) return fail(GD_EINVAL, "input has NaN or Inf coordinates");
+  if (bi.flags & gd::kFlagGridTooLarge)
+    return fail(GD_ERANGE, "eps-cell grid too large (extent/eps beyond 2^31 cells per axis, or "
+                           "cell keys and instance ids beyond 62 bits)");
+  ctx->key64 = bi.key64 != 0;
+  ctx->f32 = ctx->precision == GD_PREC_FP32_BAND;
+  ctx->xf = ctx->f32 || bi.any_xf;
+  ctx->dims = (bi.K2 > 0 ? 1 : 0) | (bi.K2 < K ? 2 : 0);
+  const size_t kw = ctx->key64 ? 8 : 4;
+  const int maxd = bi.max_dim;
+  GD_TRY(ctx->ensure(ctx->keys0, n * kw, "keys"));
+  GD_TRY(ctx->ensure(ctx->keys1, n * kw, "keys"));
+  GD_TRY(ctx->ensure(ctx->vals0, n * 4, "ids"));
+  GD_TRY(ctx->ensure(ctx->vals1, n * 4, "ids"));
+  GD_TRY(ctx->ensure(ctx->X, (size_t)n * maxd * 8, "sorted coordinates"));
+  if (ctx->xf) GD_TRY(ctx->ensure(ctx->Xf, (size_t)n * maxd * 4, "f32 coordinates"));
+  if (bi.table_total) GD_TRY(ctx->ensure(ctx->table, bi.table_total * 4, "cell tables"));
+  uint64_t hcap = 1024;
+  if (bi.any_sparse) {
+    while (hcap < 2 * (uint64_t)n) hcap <<= 1;
+    GD_TRY(ctx->ensure(ctx->hkeys, hcap * 8, "cell hash keys"));
+    GD_TRY(ctx->ensure(ctx->hvals, hcap * 4, "cell hash values"));
+  }
+  ctx->hmask = (uint32_t)(hcap - 1);
+  GD_TRY(ctx->ensure(ctx->reps, (n + 1) * 4, "cell reps"));
+  GD_TRY(ctx->ensure(ctx->runfl, n * 4, "run flags"));
+  GD_TRY(ctx->ensure(ctx->runpos, n * 4, "run positions"));
+  GD_TRY(ctx->ensure(ctx->sorttemp, gdprim::sort_temp_bytes(n), "sort temp"));
+  size_t sc = std::max(gdprim::scan_temp_bytes(n + 1),
+                       gdprim::scan_temp_bytes((int64_t)bi.table_total));
+  GD_TRY(ctx->ensure(ctx->scantemp, sc, "scan temp"));
+  const int key_bits = bi.LB + bi.IB;
+  int r;
+  uint32_t* vb[2] = {static_cast<uint32_t*>(ctx->vals0.p), static_cast<uint32_t*>(ctx->vals1.p)};
+  B = ctx->bufs();
+  gdl::keys(B, ctx->key64, nch, ctx->keys0.p, s);
+  if (ctx->key64) {
+    using U64 = unsigned long long;
+    U64* kb[2] = {static_cast<U64*>(ctx->keys0.p), static_cast<U64*>(ctx->keys1.p)};
+    r = gdprim::radix_sort_pairs<U64>(kb, vb, n, key_bits, true, ctx->sorttemp.p, s);
+    ctx->skeys = kb[r];
+  } else {
+    uint32_t* kb[2] = {static_cast<uint32_t*>(ctx->keys0.p), static_cast<uint32_t*>(ctx->keys1.p)};
+    r = gdprim::radix_sort_pairs<uint32_t>(kb, vb, n, key_bits, true, ctx->sorttemp.p, s);
+    ctx->skeys = kb[r];
+  }
+  ctx->sids = vb[r];
+  B = ctx->bufs();
+  gdl::gather(B, ctx->key64, n, ctx->xf, ctx->sms, s);
+  gdl::run_flags(ctx->skeys, ctx->key64, n, B.runfl, ctx->sms, s);
+  gdprim::exclusive_scan_u32(B.runfl, B.runpos, n, ctx->scantemp.p, ctx->dM(), s);
+  gdl::run_scatter(B, ctx->key64, n, ctx->sms, s);
+  int table_launches = 0;
+  if (bi.table_total) {
+    GD_CUDA(cudaMemsetAsync(ctx->table.p, 0, bi.table_total * 4, s), "clear cell tables");
+    gdl::cell_counts(B, ctx->key64, n, ctx->sms, s);
+    gdprim::exclusive_scan_u32(B.start, B.start, (int64_t)bi.table_total, ctx->scantemp.p,
+                               nullptr, s);
+    table_launches += 4;
+  }
+  if (bi.any_sparse) {
+    GD_CUDA(cudaMemsetAsync(ctx->hkeys.p, 0xff, hcap * 8, s), "clear cell hash");
+    gdl::hash_insert(B, ctx->key64, n, ctx->sms, s);
+    table_launches += 1;
+  }
+  GD_CUDA(cudaGetLastError(), "index build launch");
+  const int passes = (key_bits + 7) / 8;
+  // bbox init+chunks, params, layout, keys, sort, gather, run flags, scan,
+  // run scatter + split, tables
+  ctx->launches = 4 + 1 + (passes ? passes * 5 : 1) + 1 + 1 + 3 + 2 + table_launches;
+  ctx->st.grid_cells = (int64_t)bi.table_total;
+  ctx->st.key_bits = key_bits;
+  ctx->stage = 1;
+  return GD_OK;
+}
+
+gd_status expand_run(gd_ctx* ctx) {
+  cudaStream_t s = ctx->stream;
+  const int64_t n = ctx->n;
+  GD_TRY(ctx->ensure(ctx->core, n, "core flags"));
+  GD_TRY(ctx->ensure(ctx->cellcore, n * 4, "cell core counts"));
+  GD_TRY(ctx->ensure(ctx->cellmin, n * 4, "cell min index"));
+  GD_TRY(ctx->ensure(ctx->parent, n * 4, "union-find parents"));
+  GD_TRY(ctx->ensure(ctx->Fmark, (n + 1) * 4, "cluster marks"));
+  GD_TRY(ctx->ensure(ctx->cellcid, n * 4, "cell cluster ids"));
+  GD_TRY(ctx->ensure(ctx->lab, n * 4, "labels"));
+  GD_TRY(ctx->ensure(ctx->asym, gd::kAsymCap * 8, "one-directional links"));
+  GD_TRY(ctx->ensure(ctx->hvcell, n * 4, "heavy-work list"));
+  GD_TRY(ctx->ensure(ctx->hvmask, n * 8, "heavy-work masks"));
+  GD_TRY(ctx->ensure(ctx->scantemp, std::max(gdprim::scan_temp_bytes(n + 1), ctx->scantemp.bytes),
+                     "scan temp"));
+  // counters of this stage (the build's cell counts and 2D/3D split stay)
+  GD_CUDA(cudaMemsetAsync(ctx->dCtr() + gd::kCtrTests64, 0,
+                          (gd::kCtrHeavyBorder - gd::kCtrTests64 + 1) * 8, s), "clear counters");
+  gdl::Bufs B = ctx->bufs();
+  cudaEventRecord(ctx->ev[3], s);
+  gdl::core(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, s);
+  cudaEventRecord(ctx->ev[4], s);
+  gdl::unite(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, s);
+  cudaEventRecord(ctx->ev[5], s);
+  GD_CUDA(cudaMemsetAsync(B.Fmark, 0, (n + 1) * 4, s), "clear marks");
+  gdl::roots(B, n, ctx->sms, s);
+  gdprim::exclusive_scan_u32(B.Fmark, B.Fmark, n + 1, ctx->scantemp.p, ctx->dK(), s);
+  gdl::label(B, ctx->key64, n, ctx->sms, s);
+  gdl::border(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, s);
+  GD_CUDA(cudaGetLastError(), "expand launch");
+  const int cp = gdl::launches_per_cell_phase(ctx->dims);
+  // core, parent init, 2 union passes, compress, merge replay, roots, scan,
+  // label, border
+  ctx->launches += 2 * cp + 1 + 4 * cp + 1 + 1 + 1 + 3 + 1 + 2 * cp;
+  ctx->stage = 2;
+  return GD_OK;
+}
+
+// Scatter labels (and core flags) to the caller's point order, copy them out,
+// read the counters into ctx->st.
+gd_status finish_run(gd_ctx* ctx, int32_t* labels, uint8_t* is_core, int32_t on_device) {
+  cudaStream_t s = ctx->stream;
+  const int64_t n = ctx->n;
+  gd_stats& S = ctx->st;
+  int* out = reinterpret_cast<int*>(labels);
+  uint8_t* cout = is_core;
+  if (!on_device) {
+    GD_TRY(ctx->ensure(ctx->out, n * 4, "label output"));
+    out = static_cast<int*>(ctx->out.p);
+    if (is_core) {
+      GD_TRY(ctx->ensure(ctx->coreout, n, "core output"));
+      cout = static_cast<uint8_t*>(ctx->coreout.p);
+    }
+  }
+  GD_CUDA(cudaMemsetAsync(ctx->dCtr() + gd::kCtrCore, 0, 2 * 8, s), "clear counters");
+  gdl::Bufs B = ctx->bufs();
+  gdl::scatter_labels(B, n, out, cout, ctx->sms, s);
+  ++ctx->launches;
+  cudaEventRecord(ctx->ev[6], s);
+  if (!on_device) {
+    GD_CUDA(cudaMemcpyAsync(labels, out, n * 4, cudaMemcpyDeviceToHost, s), "copy labels");
+    if (is_core)
+      GD_CUDA(cudaMemcpyAsync(is_core, cout, n, cudaMemcpyDeviceToHost, s), "copy core flags");
+  }
+  cudaEventRecord(ctx->ev[7], s);
+  unsigned long long ctr[gd::kCtrCount];
+  uint32_t K = 0;
+  GD_CUDA(cudaMemcpyAsync(ctr, ctx->dCtr(), sizeof ctr, cudaMemcpyDeviceToHost, s), "counters");
+  GD_CUDA(cudaMemcpyAsync(&K, ctx->dK(), 4, cudaMemcpyDeviceToHost, s), "cluster count");
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "DBSCAN pipeline");
+  S.n_points = n;
+  S.n_clusters = K;
+  S.n_noise = (int64_t)ctr[gd::kCtrNoise];
+  S.n_core = (int64_t)ctr[gd::kCtrCore];
+  S.n_border = n - S.n_noise - S.n_core;
+  S.n_cells = (int64_t)ctr[gd::kCtrCells];
+  S.n_dense_cells = (int64_t)ctr[gd::kCtrDenseCells];
+  S.tests_fp64 = (int64_t)ctr[gd::kCtrTests64];
+  S.tests_fp32 = (int64_t)ctr[gd::kCtrTests32];
+  S.band_retests = (int64_t)ctr[gd::kCtrBand];
+  S.asym_pairs = (int64_t)ctr[gd::kCtrAsym];
+  S.precision_used = ctx->f32 ? GD_PREC_FP32_BAND : GD_PREC_FP64;
+  S.launches = ctx->launches;
+  if (ctr[gd::kCtrAsymEdges] > (unsigned long long)gd::kAsymCap) {
+    ctx->stage = 1;
+    return fail(GD_ERANGE, "more one-directional core neighbour pairs than the merge replay "
+                           "holds (2048)");
+  }
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+  S.ms_h2d = ms;
+  cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
+  S.ms_index = ms;
+  cudaEventElapsedTime(&ms, ctx->ev[3], ctx->ev[4]);
+  S.ms_core = ms;
+  cudaEventElapsedTime(&ms, ctx->ev[4], ctx->ev[5]);
+  S.ms_union = ms;
+  cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[6]);
+  S.ms_label = ms;
+  cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]);
+  S.ms_d2h = ms;
+  S.ms_total = S.ms_index + S.ms_core + S.ms_union + S.ms_label;
+  return GD_OK;
+}
+
+// Points of a run on the device: the caller's device pointer, or a copy of
+// the caller's host buffer.
+gd_status stage_points(gd_ctx* ctx, const double* coords, int64_t doubles, int32_t on_device) {
+  if (on_device || doubles == 0) {
+    ctx->coords_ptr = coords;
+    return GD_OK;
+  }
+  GD_TRY(ctx->ensure(ctx->coords, doubles * 8, "points"));
+  GD_CUDA(cudaMemcpyAsync(ctx->coords.p, coords, doubles * 8, cudaMemcpyHostToDevice,
+                          ctx->stream), "copy points to device");
+  ctx->coords_ptr = static_cast<const double*>(ctx->coords.p);
+  return GD_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -211,7 +472,7 @@ void gd_ctx_destroy(gd_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  ctx->free_all();
+  ctx->free_all(false);
   for (auto& ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   if (ctx->own) cudaStreamDestroy(ctx->own);
@@ -233,10 +494,17 @@ gd_status gd_ctx_set_precision(gd_ctx* ctx, int32_t precision) {
 }
 
 gd_status gd_ctx_set_cell_mult(gd_ctx* ctx, double mult) {
+  return gd_ctx_set_cell_mults(ctx, mult, mult);
+}
+
+gd_status gd_ctx_set_cell_mults(gd_ctx* ctx, double mult2d, double mult3d) {
   if (!ctx) return fail(GD_EINVAL, "NULL context");
-  if (mult != 0.0 && !(mult > 0.5 && mult < 0.5773))
-    return fail(GD_EINVAL, "cell multiplier must lie in (0.5, 1/sqrt(3)) or be 0");
-  ctx->cell_mult = mult;
+  if (mult2d != 0.0 && !(mult2d > 0.5 && mult2d <= kMaxCellMult2))
+    return fail(GD_EINVAL, "2D cell multiplier must lie in (0.5, 1/sqrt(2)) or be 0");
+  if (mult3d != 0.0 && !(mult3d > 0.5 && mult3d <= kMaxCellMult3))
+    return fail(GD_EINVAL, "3D cell multiplier must lie in (0.5, 1/sqrt(3)) or be 0");
+  ctx->mult2 = mult2d != 0.0 ? mult2d : kDefaultCellMult;
+  ctx->mult3 = mult3d != 0.0 ? mult3d : kDefaultCellMult;
   return GD_OK;
 }
 
@@ -244,10 +512,7 @@ gd_status gd_ctx_trim(gd_ctx* ctx) {
   if (!ctx) return fail(GD_EINVAL, "NULL context");
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  DevBuf keep = ctx->small;
-  ctx->small = DevBuf{};
-  ctx->free_all();
-  ctx->small = keep;
+  ctx->free_all(true);
   ctx->stage = 0;
   return GD_OK;
 }
@@ -261,131 +526,22 @@ gd_status gd_index_build(gd_ctx* ctx, const gd_points* pts, double eps) {
   if (pts->n > 0 && !pts->coords) return fail(GD_EINVAL, "gd_index_build: coords is NULL");
   if (pts->n >= (int64_t)INT32_MAX) return fail(GD_EINVAL, "gd_index_build: n must be < 2^31");
   GD_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
-  cudaStream_t s = ctx->stream;
-  const int64_t n = pts->n;
-  const int D = pts->dim;
   ctx->stage = 0;
-  ctx->n = n;
-  ctx->dim = D;
-  ctx->eps = eps;
   ctx->st = gd_stats{};
-  ctx->st.n_points = n;
-  gd_status st;
-  GD_CUDA(cudaMemsetAsync(ctx->small.p, 0, ctx->small.bytes, s), "memset");
+  ctx->st.n_points = pts->n;
   ctx->launches = 0;
-  if (n == 0) {
+  cudaEventRecord(ctx->ev[0], ctx->stream);
+  GD_TRY(stage_points(ctx, pts->coords, pts->n * pts->dim, pts->on_device));
+  cudaEventRecord(ctx->ev[1], ctx->stream);
+  ctx->hdesc.assign(1, gd::InstDesc{0, pts->n, 0, eps, pts->dim, 1});
+  if (pts->n == 0) {
+    ctx->K = 1;
+    ctx->n = 0;
     ctx->stage = 1;
     return GD_OK;
   }
-  cudaEventRecord(ctx->ev[0], s);
-  if (pts->on_device) {
-    ctx->dpts = pts->coords;
-  } else {
-    if ((st = ctx->ensure(ctx->pts, (size_t)n * D * 8, "points")) != GD_OK) return st;
-    GD_CUDA(cudaMemcpyAsync(ctx->pts.p, pts->coords, (size_t)n * D * 8, cudaMemcpyHostToDevice, s),
-            "copy points to device");
-    ctx->dpts = static_cast<const double*>(ctx->pts.p);
-  }
-  cudaEventRecord(ctx->ev[1], s);
-  // bounding box and grid parameters
-  int nb = (int)std::min<int64_t>((int64_t)ctx->sms * 4, (n + 255) / 256);
-  if (nb < 1) nb = 1;
-  ctx->bbox_blocks = nb;
-  if ((st = ctx->ensure(ctx->partial, (size_t)nb * 6 * 8, "bbox partials")) != GD_OK) return st;
-  gdl::bbox(ctx->dpts, n, D, static_cast<double*>(ctx->partial.p), nb, ctx->dFlags(), s);
-  const double mult = ctx->cell_mult > 0 ? ctx->cell_mult : kDefaultCellMult;
-  uint64_t max_cells = std::max<uint64_t>((uint64_t)1 << 26, (uint64_t)n * 8);
-  if (max_cells > 0xfffffff0ull) max_cells = 0xfffffff0ull;
-  gdl::params(static_cast<double*>(ctx->partial.p), nb, D, ctx->dP(), eps, 1, mult, max_cells,
-              ctx->dFlags(), s);
-  GD_CUDA(cudaMemcpyAsync(&ctx->hp, ctx->dP(), sizeof(gd::DevParams), cudaMemcpyDeviceToHost, s),
-          "read grid parameters");
-  GD_CUDA(cudaStreamSynchronize(s), "grid parameters");
-  if (ctx->hp.flags & gd::kFlagNonFinite)
-    return fail(GD_EINVAL, "gd_index_build: input has NaN or Inf coordinates");
-  if (ctx->hp.flags & gd::kFlagGridTooLarge) {
-    return fail(GD_ERANGE,
-                "gd_index_build: eps-cell grid too large (extent/eps beyond 2^31 cells per "
-                "axis or 2^62 cells in all)");
-  }
-  ctx->f32 = ctx->precision == GD_PREC_FP32_BAND && ctx->hp.eps2_lo32 > 0.0f;
-  ctx->sparse = ctx->hp.sparse != 0;
-  const uint64_t C = ctx->hp.C;
-  const size_t kw = ctx->sparse ? 8 : 4;  // key width
-  // buffers
-  if ((st = ctx->ensure(ctx->keys0, n * kw, "keys")) != GD_OK) return st;
-  if ((st = ctx->ensure(ctx->keys1, n * kw, "keys")) != GD_OK) return st;
-  if ((st = ctx->ensure(ctx->vals0, n * 4, "ids")) != GD_OK) return st;
-  if ((st = ctx->ensure(ctx->vals1, n * 4, "ids")) != GD_OK) return st;
-  if ((st = ctx->ensure(ctx->X, (size_t)n * D * 8, "sorted coordinates")) != GD_OK) return st;
-  const bool want_xf = ctx->f32 || ctx->hp.prune;  // centred float32 copy
-  if (want_xf && (st = ctx->ensure(ctx->Xf, (size_t)n * D * 4, "f32 coordinates")) != GD_OK)
-    return st;
-  uint64_t hcap = 1024;
-  if (ctx->sparse) {
-    while (hcap < 2 * (uint64_t)n) hcap <<= 1;
-    ctx->hmask = (uint32_t)(hcap - 1);
-    if ((st = ctx->ensure(ctx->hkeys, hcap * 8, "cell hash keys")) != GD_OK) return st;
-    if ((st = ctx->ensure(ctx->hvals, hcap * 4, "cell hash values")) != GD_OK) return st;
-  } else {
-    if ((st = ctx->ensure(ctx->table, (C + 1) * 4, "cell table")) != GD_OK) return st;
-  }
-  if ((st = ctx->ensure(ctx->reps, (n + 1) * 4, "cell reps")) != GD_OK) return st;
-  if ((st = ctx->ensure(ctx->runfl, n * 4, "run flags")) != GD_OK) return st;
-  if ((st = ctx->ensure(ctx->runpos, n * 4, "run positions")) != GD_OK) return st;
-  if ((st = ctx->ensure(ctx->sorttemp, gdprim::sort_temp_bytes(n), "sort temp")) != GD_OK)
-    return st;
-  size_t sc = gdprim::scan_temp_bytes(n);
-  if (!ctx->sparse) sc = std::max(sc, gdprim::scan_temp_bytes((int64_t)C + 1));
-  if ((st = ctx->ensure(ctx->scantemp, sc, "scan temp")) != GD_OK) return st;
-  // keys and sort
-  int r;
-  gdl::keys(ctx->dpts, n, D, ctx->sparse, ctx->dP(), ctx->keys0.p, ctx->sms, s);
-  uint32_t* vb[2] = {static_cast<uint32_t*>(ctx->vals0.p), static_cast<uint32_t*>(ctx->vals1.p)};
-  if (ctx->sparse) {
-    using U64 = unsigned long long;
-    U64* kb[2] = {static_cast<U64*>(ctx->keys0.p), static_cast<U64*>(ctx->keys1.p)};
-    r = gdprim::radix_sort_pairs<U64>(kb, vb, n, ctx->hp.key_bits, true, ctx->sorttemp.p, s);
-    ctx->skeys = kb[r];
-  } else {
-    uint32_t* kb[2] = {static_cast<uint32_t*>(ctx->keys0.p), static_cast<uint32_t*>(ctx->keys1.p)};
-    r = gdprim::radix_sort_pairs<uint32_t>(kb, vb, n, ctx->hp.key_bits, true, ctx->sorttemp.p, s);
-    ctx->skeys = kb[r];
-  }
-  ctx->sids = vb[r];
-  gdl::gather(ctx->dpts, ctx->sids, n, D, want_xf, ctx->dP(), static_cast<double*>(ctx->X.p),
-              static_cast<float*>(ctx->Xf.p), ctx->sms, s);
-  // cell runs and the cell lookup (dense table or hash of occupied cells)
-  uint32_t* fl = static_cast<uint32_t*>(ctx->runfl.p);
-  uint32_t* pos = static_cast<uint32_t*>(ctx->runpos.p);
-  gdl::run_flags(ctx->skeys, ctx->sparse, n, fl, ctx->sms, s);
-  gdprim::exclusive_scan_u32(fl, pos, n, ctx->scantemp.p, ctx->dM(), s);
-  gdl::run_scatter(fl, pos, n, static_cast<int*>(ctx->reps.p), ctx->dM(), ctx->dCtr(), ctx->sms, s);
-  if (ctx->sparse) {
-    GD_CUDA(cudaMemsetAsync(ctx->hkeys.p, 0xff, hcap * 8, s), "clear cell hash");
-    gdl::hash_insert(static_cast<const unsigned long long*>(ctx->skeys),
-                     static_cast<int*>(ctx->reps.p), ctx->dM(), n,
-                     static_cast<unsigned long long*>(ctx->hkeys.p),
-                     static_cast<uint32_t*>(ctx->hvals.p), ctx->hmask, ctx->sms, s);
-  } else {
-    GD_CUDA(cudaMemsetAsync(ctx->table.p, 0, (C + 1) * 4, s), "clear cell table");
-    gdl::cell_counts(static_cast<const uint32_t*>(ctx->skeys), static_cast<int*>(ctx->reps.p),
-                     ctx->dM(), n, static_cast<uint32_t*>(ctx->table.p), ctx->sms, s);
-    gdprim::exclusive_scan_u32(static_cast<uint32_t*>(ctx->table.p),
-                               static_cast<uint32_t*>(ctx->table.p), (int64_t)C + 1,
-                               ctx->scantemp.p, nullptr, s);
-  }
-  cudaEventRecord(ctx->ev[2], s);
-  GD_CUDA(cudaGetLastError(), "index build launch");
-  {
-    const int passes = (ctx->hp.key_bits + 7) / 8;
-    // bbox, params, keys, sort, gather, run flags, scan, run scatter, counts, scan
-    // bbox, params, keys, sort, gather, run flags, scan, run scatter, table or hash
-    ctx->launches = 3 + (passes ? passes * 5 : 1) + 1 + 1 + 3 + 1 + (ctx->sparse ? 1 : 4);
-  }
-  ctx->st.grid_cells = (int64_t)C;
-  ctx->st.key_bits = ctx->hp.key_bits;
-  ctx->stage = 1;
+  GD_TRY(build_run(ctx, (uint64_t)1 << 26, 8));
+  cudaEventRecord(ctx->ev[2], ctx->stream);
   return GD_OK;
 }
 
@@ -394,50 +550,19 @@ gd_status gd_expand(gd_ctx* ctx, int32_t minpts) {
   if (ctx->stage < 1) return fail(GD_ESTATE, "gd_expand: call gd_index_build first");
   if (minpts < 1) return fail(GD_EINVAL, "gd_expand: minpts must be >= 1");
   GD_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
-  cudaStream_t s = ctx->stream;
-  const int64_t n = ctx->n;
-  ctx->minpts = minpts;
-  if (n == 0) {
+  if (ctx->n == 0) {
     ctx->stage = 2;
     return GD_OK;
   }
-  gd_status st;
-  if ((st = ctx->ensure(ctx->core, n, "core flags")) != GD_OK) return st;
-  if ((st = ctx->ensure(ctx->cellcore, n * 4, "cell core counts")) != GD_OK) return st;
-  if ((st = ctx->ensure(ctx->cellmin, n * 4, "cell min index")) != GD_OK) return st;
-  if ((st = ctx->ensure(ctx->parent, n * 4, "union-find parents")) != GD_OK) return st;
-  if ((st = ctx->ensure(ctx->Fmark, n * 4, "cluster marks")) != GD_OK) return st;
-  if ((st = ctx->ensure(ctx->cellcid, n * 4, "cell cluster ids")) != GD_OK) return st;
-  if ((st = ctx->ensure(ctx->lab, n * 4, "labels")) != GD_OK) return st;
-  if ((st = ctx->ensure(ctx->asym, gd::kAsymCap * 8, "one-directional links")) != GD_OK) return st;
-  if ((st = ctx->ensure(ctx->hvcell, n * 4, "heavy-work list")) != GD_OK) return st;
-  if ((st = ctx->ensure(ctx->hvmask, n * 8, "heavy-work masks")) != GD_OK) return st;
-  size_t sc = gdprim::scan_temp_bytes(n);
-  if ((st = ctx->ensure(ctx->scantemp, std::max(sc, ctx->scantemp.bytes), "scan temp")) != GD_OK)
-    return st;
-  // minpts into the device parameters; counters except the cell count
-  ctx->hp.minpts = minpts;
-  GD_CUDA(cudaMemcpyAsync(ctx->dP(), &ctx->hp, sizeof(gd::DevParams), cudaMemcpyHostToDevice, s),
-          "write parameters");
-  GD_CUDA(cudaMemsetAsync(ctx->dCtr() + 1, 0, (gd::kCtrCount - 1) * 8, s), "clear counters");
-  gdl::Bufs B = ctx->bufs();
-  const int D = ctx->dim;
-  cudaEventRecord(ctx->ev[3], s);
-  gdl::core(B, n, D, ctx->f32, ctx->sparse, ctx->sms, s);
-  cudaEventRecord(ctx->ev[4], s);
-  gdl::unite(B, n, D, ctx->f32, ctx->sparse, ctx->sms, s);
-  cudaEventRecord(ctx->ev[5], s);
-  GD_CUDA(cudaMemsetAsync(B.Fmark, 0, n * 4, s), "clear marks");
-  gdl::roots(B, n, ctx->sms, s);
-  gdprim::exclusive_scan_u32(B.Fmark, B.Fmark, n, ctx->scantemp.p, ctx->dK(), s);
-  gdl::label(B, n, ctx->sms, s);
-  gdl::border(B, n, D, ctx->f32, ctx->sparse, ctx->sms, s);
-  GD_CUDA(cudaGetLastError(), "expand launch");
-  // core (scan+heavy), parent init, 2 union passes (scan+heavy), compress, merge replay,
-  // roots, scan, label, border (scan+heavy)
-  ctx->launches += 2 + 1 + 4 + 1 + 1 + 1 + 3 + 1 + 2;
-  ctx->stage = 2;
-  return GD_OK;
+  if (ctx->K == 1) {
+    // minpts does not shape the grid: set it in the instance's parameters
+    gd::DevParams* P0 = static_cast<gd::DevParams*>(ctx->Pv.p);
+    ctx->hdesc[0].minpts = minpts;
+    GD_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(P0) + offsetof(gd::DevParams, minpts),
+                            &ctx->hdesc[0].minpts, sizeof(int32_t), cudaMemcpyHostToDevice,
+                            ctx->stream), "write minpts");
+  }
+  return expand_run(ctx);
 }
 
 gd_status gd_get_result(gd_ctx* ctx, int32_t* labels, uint8_t* is_core, int32_t on_device,
@@ -445,76 +570,15 @@ gd_status gd_get_result(gd_ctx* ctx, int32_t* labels, uint8_t* is_core, int32_t 
   if (!ctx) return fail(GD_EINVAL, "gd_get_result: NULL context");
   if (ctx->stage < 2) return fail(GD_ESTATE, "gd_get_result: call gd_expand first");
   GD_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
-  cudaStream_t s = ctx->stream;
-  const int64_t n = ctx->n;
-  gd_stats& S = ctx->st;
-  if (n == 0) {
+  if (ctx->n == 0) {
     if (cluster_count) *cluster_count = 0;
     if (noise_count) *noise_count = 0;
     return GD_OK;
   }
   if (!labels) return fail(GD_EINVAL, "gd_get_result: labels is NULL");
-  gd_status st;
-  int* out = reinterpret_cast<int*>(labels);
-  uint8_t* cout = is_core;
-  if (!on_device) {
-    if ((st = ctx->ensure(ctx->out, n * 4, "label output")) != GD_OK) return st;
-    out = static_cast<int*>(ctx->out.p);
-    if (is_core) {
-      if ((st = ctx->ensure(ctx->coreout, n, "core output")) != GD_OK) return st;
-      cout = static_cast<uint8_t*>(ctx->coreout.p);
-    }
-  }
-  GD_CUDA(cudaMemsetAsync(ctx->dCtr() + gd::kCtrCore, 0, 2 * 8, s), "clear counters");
-  gdl::Bufs B = ctx->bufs();
-  gdl::scatter_labels(B, n, out, cout, ctx->sms, s);
-  ++ctx->launches;
-  cudaEventRecord(ctx->ev[6], s);
-  if (!on_device) {
-    GD_CUDA(cudaMemcpyAsync(labels, out, n * 4, cudaMemcpyDeviceToHost, s), "copy labels");
-    if (is_core)
-      GD_CUDA(cudaMemcpyAsync(is_core, cout, n, cudaMemcpyDeviceToHost, s), "copy core flags");
-  }
-  cudaEventRecord(ctx->ev[7], s);
-  unsigned long long ctr[gd::kCtrCount];
-  uint32_t K = 0;
-  GD_CUDA(cudaMemcpyAsync(ctr, ctx->dCtr(), sizeof ctr, cudaMemcpyDeviceToHost, s), "counters");
-  GD_CUDA(cudaMemcpyAsync(&K, ctx->dK(), 4, cudaMemcpyDeviceToHost, s), "cluster count");
-  cudaError_t e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return cuda_fail(e, "DBSCAN pipeline");
-  S.n_clusters = K;
-  S.n_noise = (int64_t)ctr[gd::kCtrNoise];
-  S.n_core = (int64_t)ctr[gd::kCtrCore];
-  S.n_border = n - S.n_noise - S.n_core;
-  S.n_cells = (int64_t)ctr[gd::kCtrCells];
-  S.n_dense_cells = (int64_t)ctr[gd::kCtrDenseCells];
-  S.tests_fp64 = (int64_t)ctr[gd::kCtrTests64];
-  S.tests_fp32 = (int64_t)ctr[gd::kCtrTests32];
-  S.band_retests = (int64_t)ctr[gd::kCtrBand];
-  S.asym_pairs = (int64_t)ctr[gd::kCtrAsym];
-  if (ctr[gd::kCtrAsymEdges] > (unsigned long long)gd::kAsymCap) {
-    ctx->stage = 1;
-    return fail(GD_ERANGE, "more one-directional core neighbour pairs than the merge replay "
-                           "holds (2048)");
-  }
-  S.precision_used = ctx->f32 ? GD_PREC_FP32_BAND : GD_PREC_FP64;
-  S.launches = ctx->launches;
-  float ms = 0;
-  cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
-  S.ms_h2d = ms;
-  cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
-  S.ms_index = ms;
-  cudaEventElapsedTime(&ms, ctx->ev[3], ctx->ev[4]);
-  S.ms_core = ms;
-  cudaEventElapsedTime(&ms, ctx->ev[4], ctx->ev[5]);
-  S.ms_union = ms;
-  cudaEventElapsedTime(&ms, ctx->ev[5], ctx->ev[6]);
-  S.ms_label = ms;
-  cudaEventElapsedTime(&ms, ctx->ev[6], ctx->ev[7]);
-  S.ms_d2h = ms;
-  S.ms_total = S.ms_index + S.ms_core + S.ms_union + S.ms_label;
-  if (cluster_count) *cluster_count = S.n_clusters;
-  if (noise_count) *noise_count = S.n_noise;
+  GD_TRY(finish_run(ctx, labels, is_core, on_device));
+  if (cluster_count) *cluster_count = ctx->st.n_clusters;
+  if (noise_count) *noise_count = ctx->st.n_noise;
   return GD_OK;
 }
 
@@ -522,11 +586,71 @@ gd_status gd_dbscan(gd_ctx* ctx, const gd_points* pts, double eps, int32_t minpt
                     int32_t* labels, gd_stats* stats) {
   if (!ctx || !pts) return fail(GD_EINVAL, "gd_dbscan: NULL argument");
   if (minpts < 1) return fail(GD_EINVAL, "gd_dbscan: minpts must be >= 1");
-  gd_status s = gd_index_build(ctx, pts, eps);
-  if (s != GD_OK) return s;
-  if ((s = gd_expand(ctx, minpts)) != GD_OK) return s;
-  if ((s = gd_get_result(ctx, labels, nullptr, pts->on_device, nullptr, nullptr)) != GD_OK)
-    return s;
+  GD_TRY(gd_index_build(ctx, pts, eps));
+  GD_TRY(gd_expand(ctx, minpts));
+  GD_TRY(gd_get_result(ctx, labels, nullptr, pts->on_device, nullptr, nullptr));
+  if (stats) *stats = ctx->st;
+  return GD_OK;
+}
+
+gd_status gd_batch_dbscan(gd_ctx* ctx, int32_t count, const gd_instance* inst,
+                          const double* coords, int32_t on_device, int32_t* labels,
+                          int64_t* cluster_counts, gd_stats* stats) {
+  if (!ctx || (count > 0 && !inst)) return fail(GD_EINVAL, "gd_batch_dbscan: NULL argument");
+  if (count < 0) return fail(GD_EINVAL, "gd_batch_dbscan: count must be >= 0");
+  GD_CUDA(cudaSetDevice(ctx->device), "cudaSetDevice");
+  ctx->stage = 0;
+  ctx->st = gd_stats{};
+  ctx->launches = 0;
+  // validate; caller layout offsets; internal order puts 2D instances first
+  std::vector<gd::InstDesc> user(count);
+  int64_t pt = 0, co = 0;
+  for (int i = 0; i < count; ++i) {
+    const gd_instance& I = inst[i];
+    if (I.n < 0 || (I.dim != 2 && I.dim != 3) || !(I.eps > 0) || !std::isfinite(I.eps) ||
+        I.minpts < 1)
+      return fail(GD_EINVAL, "gd_batch_dbscan: instance " + std::to_string(i) +
+                                 " has n < 0, dim not 2/3, eps not positive and finite, or "
+                                 "minpts < 1");
+    user[i] = gd::InstDesc{pt, I.n, co, I.eps, I.dim, I.minpts};
+    pt += I.n;
+    co += I.n * I.dim;
+  }
+  if (pt >= (int64_t)INT32_MAX) return fail(GD_EINVAL, "gd_batch_dbscan: total points >= 2^31");
+  if (pt > 0 && (!coords || !labels)) return fail(GD_EINVAL, "gd_batch_dbscan: NULL buffer");
+  ctx->st.n_points = pt;
+  std::vector<int> order;
+  order.reserve(count);
+  for (int pass = 2; pass <= 3; ++pass)
+    for (int i = 0; i < count; ++i)
+      if (user[i].dim == pass) order.push_back(i);
+  ctx->hdesc.resize(count);
+  for (int j = 0; j < count; ++j) ctx->hdesc[j] = user[order[j]];
+  cudaEventRecord(ctx->ev[0], ctx->stream);
+  GD_TRY(stage_points(ctx, coords, co, on_device));
+  cudaEventRecord(ctx->ev[1], ctx->stream);
+  if (pt == 0 || count == 0) {
+    ctx->K = count;
+    ctx->n = 0;
+    if (cluster_counts)
+      for (int i = 0; i < count; ++i) cluster_counts[i] = 0;
+    if (stats) *stats = ctx->st;
+    return GD_OK;
+  }
+  GD_TRY(build_run(ctx, 4096, 8));
+  cudaEventRecord(ctx->ev[2], ctx->stream);
+  GD_TRY(expand_run(ctx));
+  GD_TRY(finish_run(ctx, labels, nullptr, on_device));
+  if (cluster_counts) {
+    GD_TRY(ctx->ensure(ctx->kcount, count * 8, "cluster counts"));
+    gdl::Bufs B = ctx->bufs();
+    gdl::cluster_counts(B, count, static_cast<int64_t*>(ctx->kcount.p), ctx->stream);
+    std::vector<int64_t> kc(count);
+    GD_CUDA(cudaMemcpyAsync(kc.data(), ctx->kcount.p, count * 8, cudaMemcpyDeviceToHost,
+                            ctx->stream), "copy cluster counts");
+    GD_CUDA(cudaStreamSynchronize(ctx->stream), "cluster counts");
+    for (int j = 0; j < count; ++j) cluster_counts[order[j]] = kc[j];
+  }
   if (stats) *stats = ctx->st;
   return GD_OK;
 }

@@ -26,7 +26,42 @@ constexpr int kNoise = -2;            // common.h:8 NOISE
 constexpr int kWarp = 32;
 constexpr unsigned kFull = 0xffffffffu;
 
-// Grid and predicate parameters, computed on the device from the bounding box.
+// One clustering instance as the caller describes it (uploaded per run).
+struct InstDesc {
+  int64_t pt_off;      // first point of the instance in the concatenated point list
+  int64_t n;           // its points
+  int64_t co_off;      // its first coordinate (in doubles) in the concatenated buffer
+  double eps;
+  int32_t dim;         // 2 or 3
+  int32_t minpts;
+};
+
+// A run of points of one instance (bbox and key kernels take one block each).
+struct Chunk {
+  int32_t inst;
+  int32_t pad;
+  int64_t begin;       // global point indices [begin, end)
+  int64_t end;
+};
+constexpr int64_t kChunkPoints = 8192;
+
+// Whole-run layout, computed on the device after the per-instance grids.
+struct BatchInfo {
+  int32_t K;           // instances
+  int32_t LB;          // local key bits (widest instance grid)
+  int32_t IB;          // instance-id bits
+  int32_t key64;       // 1: keys are 64-bit
+  uint64_t table_total;// entries of all dense cell tables together
+  int32_t any_sparse;  // some instance uses the hash of occupied cells
+  int32_t flags;       // OR of the instances' kFlag* bits
+  int32_t any_xf;      // some instance wants the centred float32 copy
+  int32_t max_dim;
+  int32_t K2;          // instances [0, K2) are 2D, [K2, K) 3D
+  int32_t pad;
+};
+
+// Grid and predicate parameters of one instance, computed on the device from
+// its bounding box.
 struct DevParams {
   double lo[3];        // per-dimension minimum (grid origin)
   double hi[3];        // per-dimension maximum
@@ -50,7 +85,37 @@ struct DevParams {
   float uerr;          // bound on the error of a point's in-cell position (cell units)
   float thr_in;        // sum of squared max distances (cell units) below: all neighbours
   float thr_out;       // sum of squared min distances (cell units) above: none
+  int64_t pt_off;      // first point (global index)
+  int64_t n;           // points
+  int64_t co_off;      // first coordinate in the concatenated buffer
+  uint64_t table_off;  // dense grids: first entry of this instance's cell table
+  uint64_t kmask;      // mask of the local key bits
+  int32_t LB;          // local key bits of the run (copied from BatchInfo)
+  int32_t inst;        // instance index
 };
+
+// The predicate constants a cell kernel keeps in registers.
+struct PredParams {
+  double eps, eps2, eps2_in;
+  float eps2_lo32, eps2_hi32, uerr, thr_in, thr_out, inv_f32;
+  int32_t minpts, prune;
+};
+
+__device__ __forceinline__ PredParams pred_params(const DevParams& P) {
+  PredParams q;
+  q.eps = P.eps;
+  q.eps2 = P.eps2;
+  q.eps2_in = P.eps2_in;
+  q.eps2_lo32 = P.eps2_lo32;
+  q.eps2_hi32 = P.eps2_hi32;
+  q.uerr = P.uerr;
+  q.thr_in = P.thr_in;
+  q.thr_out = P.thr_out;
+  q.inv_f32 = P.inv_f32;
+  q.minpts = P.minpts;
+  q.prune = P.prune;
+  return q;
+}
 
 constexpr int kFlagNonFinite = 1;     // NaN or Inf coordinate
 constexpr int kFlagGridTooLarge = 2;  // keys would not fit 62 bits
@@ -72,6 +137,7 @@ enum Counter {
   kCtrHeavyCore,        // cells queued for warp-cooperative core counting
   kCtrHeavyUnion,       // cells queued for warp-cooperative link searches
   kCtrHeavyBorder,      // cells queued for warp-cooperative border search
+  kCtrCells2D,          // cells of 2D instances (they sort first)
   kCtrCount = 16
 };
 
@@ -115,9 +181,9 @@ __device__ __forceinline__ bool box_f64(const double* p, const double* q, double
 }
 
 // Full predicate given d2 = dist2_f64(p, q).
-template <int D>
+template <int D, class PP>
 __device__ __forceinline__ bool pred_from_d2(double d2, const double* p, const double* q,
-                                             const DevParams& P) {
+                                             const PP& P) {
   if (d2 <= P.eps2_in) return true;
   if (!(d2 <= P.eps2)) return false;
   return box_f64<D>(p, q, P.eps);

@@ -1,4 +1,11 @@
 // gd_launch.h -- host launchers for the kernels in gd_pipeline.cu.
+//
+// One run clusters K >= 1 independent instances together.  Their points are
+// concatenated (instance i owns global point indices [pt_off_i, pt_off_i+n_i));
+// every cell key carries the instance id in its high bits, so one sort, one
+// cell list and one launch per phase serve all instances.  Instances are
+// ordered 2D first: cells [0, M2) belong to 2D instances, [M2, M) to 3D ones,
+// and each cell phase runs one launch per dimension present.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -8,59 +15,65 @@
 
 namespace gdl {
 
-// Device buffers of one instance (see the layout in gd_internal.cuh).  Passed
-// by value to the cell kernels.
+// Device buffers of one run (see the layout in gd_internal.cuh).  Passed by
+// value to the kernels.
 struct Bufs {
-  gd::DevParams* P = nullptr;
-  const void* keys = nullptr;   // sorted cell keys: u32 (dense grid) or u64 (sparse)
-  uint32_t* ids = nullptr;      // original index per sorted position
+  const double* coords = nullptr;       // concatenated input, row-major per instance
+  const gd::InstDesc* inst = nullptr;   // K instance descriptions
+  const gd::Chunk* chunks = nullptr;    // point runs, one instance each
+  gd::DevParams* Pv = nullptr;          // K per-instance grid/predicate parameters
+  gd::BatchInfo* Bi = nullptr;          // run layout
+  long long* bbox = nullptr;            // K x 6 ordered-int bounds
+  const void* keys = nullptr;   // sorted cell keys: u32 or u64 (BatchInfo::key64)
+  uint32_t* ids = nullptr;      // global point index per sorted position
   int* reps = nullptr;          // M+1 first positions of the non-empty cells
   uint32_t* M = nullptr;        // number of non-empty cells (device scalar)
   uint32_t* runfl = nullptr;    // 1 where a cell starts (per sorted position)
   uint32_t* runpos = nullptr;   // exclusive scan of runfl: cell index = runpos+runfl-1
-  uint32_t* start = nullptr;    // dense grids: cell table, C+1 entries
+  uint32_t* start = nullptr;    // dense grids: cell tables of all dense instances
   unsigned long long* hkeys = nullptr;  // sparse grids: hash slots (key)
   uint32_t* hvals = nullptr;            // sparse grids: hash slots (cell index m)
   uint32_t hmask = 0;                   // sparse grids: slots - 1
-  double* X = nullptr;          // sorted float64 coordinates, D x n
-  float* Xf = nullptr;          // sorted centred float32 coordinates, D x n
+  double* X = nullptr;          // sorted float64 coordinates, max_dim x n
+  float* Xf = nullptr;          // sorted centred float32 coordinates, max_dim x n
   uint8_t* core = nullptr;      // core flag per sorted position
   int* cellcore = nullptr;      // per rep: number of core points
-  int* cellmin = nullptr;       // per rep: smallest original index of a core point
+  int* cellmin = nullptr;       // per rep: smallest global index of a core point
   int* parent = nullptr;        // per rep: union-find parent
-  uint32_t* Fmark = nullptr;    // n: 1 at the smallest core index of each cluster,
-                                // then its exclusive scan (cluster ids)
+  uint32_t* Fmark = nullptr;    // n+1: 1 at the smallest core index of each cluster,
+                                // then its exclusive scan (global cluster numbers)
   int* cellcid = nullptr;       // per rep: cluster id of the cell's core points
   int* lab = nullptr;           // label per sorted position
   int* asym = nullptr;          // kAsymCap (from, to) sorted-position pairs
   int* hv_cell = nullptr;       // heavy-work list: cell index m (capacity n)
   unsigned long long* hv_mask = nullptr;  // heavy-work list: stencil offsets still open
-  unsigned long long* ctr = nullptr;  // gd::Counter
+  unsigned long long* ctr = nullptr;      // gd::Counter
 };
 
-void bbox(const double* pts, int64_t n, int dim, double* partial, int nblocks, int* flags,
-          cudaStream_t s);
-void params(const double* partial, int nblocks, int dim, gd::DevParams* P, double eps,
-            int minpts, double cell_mult, uint64_t max_cells, const int* flags, cudaStream_t s);
-// keys: u32 for dense grids, u64 for sparse grids
-void keys(const double* pts, int64_t n, int dim, bool sparse, const gd::DevParams* P, void* keys,
-          int sms, cudaStream_t s);
-void gather(const double* pts, const uint32_t* ids, int64_t n, int dim, bool f32,
-            const gd::DevParams* P, double* X, float* Xf, int sms, cudaStream_t s);
-void run_flags(const void* keys, bool sparse, int64_t n, uint32_t* fl, int sms, cudaStream_t s);
-void run_scatter(const uint32_t* fl, const uint32_t* pos, int64_t n, int* reps,
-                 const uint32_t* Mdev, unsigned long long* ctr, int sms, cudaStream_t s);
-void cell_counts(const uint32_t* keys, const int* reps, const uint32_t* Mdev, int64_t n,
-                 uint32_t* table, int sms, cudaStream_t s);
-void hash_insert(const unsigned long long* keys, const int* reps, const uint32_t* Mdev, int64_t n,
-                 unsigned long long* hkeys, uint32_t* hvals, uint32_t mask, int sms,
-                 cudaStream_t s);
-void core(const Bufs& B, int64_t n, int dim, bool f32, bool sparse, int sms, cudaStream_t s);
-void unite(const Bufs& B, int64_t n, int dim, bool f32, bool sparse, int sms, cudaStream_t s);
+// per-instance bounding boxes, grids and the run layout
+void grids(const Bufs& B, int K, int nchunks, double mult2, double mult3, uint64_t dense_floor,
+           uint64_t dense_per_point, cudaStream_t s);
+// cell keys in global point order (width from the run layout)
+void keys(const Bufs& B, bool key64, int nchunks, void* keys_out, cudaStream_t s);
+void gather(const Bufs& B, bool key64, int64_t n, bool xf, int sms, cudaStream_t s);
+void run_flags(const void* keys, bool key64, int64_t n, uint32_t* fl, int sms, cudaStream_t s);
+// cell starts (reps), cell count, and the split between 2D and 3D cells
+void run_scatter(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
+// dense instances: cell counts into their table slices (scan them afterwards)
+void cell_counts(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
+// sparse instances: hash of occupied cells (clear the slots first)
+void hash_insert(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
+// cell phases; dims: bit 0 = 2D instances present, bit 1 = 3D
+void core(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s);
+void unite(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s);
 void roots(const Bufs& B, int64_t n, int sms, cudaStream_t s);
-void label(const Bufs& B, int64_t n, int sms, cudaStream_t s);
-void border(const Bufs& B, int64_t n, int dim, bool f32, bool sparse, int sms, cudaStream_t s);
+void label(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
+void border(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s);
 void scatter_labels(const Bufs& B, int64_t n, int* out, uint8_t* core_out, int sms,
                     cudaStream_t s);
+// per-instance cluster counts (K entries) from the cluster-number scan
+void cluster_counts(const Bufs& B, int K, int64_t* out, cudaStream_t s);
+// kernel launches of one cell phase (per dimension present)
+int launches_per_cell_phase(int dims);
 
 }  // namespace gdl

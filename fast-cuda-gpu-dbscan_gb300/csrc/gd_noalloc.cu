@@ -40,14 +40,18 @@ namespace {
 constexpr int64_t kMaxPoints = GD_NOALLOC_MAX_POINTS;
 constexpr uint64_t kTableCells = 8ull * kMaxPoints;      // dense table limit
 constexpr uint64_t kHashSlots = 2ull * kMaxPoints;       // power of two
-constexpr int kBboxBlocks = 256;
 
 constexpr size_t up(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // byte offsets of the buffers inside the scratch array
-constexpr size_t kOffSmall = 0;                                   // params | M | K | flags | ctr
-constexpr size_t kOffPartial = kOffSmall + 4096;
-constexpr size_t kOffKeys0 = kOffPartial + up(kBboxBlocks * 6 * 8);
+constexpr int kMaxChunks = (int)((kMaxPoints + gd::kChunkPoints - 1) / gd::kChunkPoints);
+constexpr size_t kOffSmall = 0;                                   // M | K | counters
+constexpr size_t kOffInst = kOffSmall + 4096;
+constexpr size_t kOffChunks = kOffInst + up(sizeof(gd::InstDesc));
+constexpr size_t kOffPv = kOffChunks + up(kMaxChunks * sizeof(gd::Chunk));
+constexpr size_t kOffBi = kOffPv + up(sizeof(gd::DevParams));
+constexpr size_t kOffBbox = kOffBi + up(sizeof(gd::BatchInfo));
+constexpr size_t kOffKeys0 = kOffBbox + up(6 * 8);
 constexpr size_t kOffKeys1 = kOffKeys0 + up(kMaxPoints * 8);
 constexpr size_t kOffVals0 = kOffKeys1 + up(kMaxPoints * 8);
 constexpr size_t kOffVals1 = kOffVals0 + up(kMaxPoints * 4);
@@ -64,7 +68,7 @@ constexpr size_t kOffCellcore = kOffCore + up(kMaxPoints);
 constexpr size_t kOffCellmin = kOffCellcore + up(kMaxPoints * 4);
 constexpr size_t kOffParent = kOffCellmin + up(kMaxPoints * 4);
 constexpr size_t kOffFmark = kOffParent + up(kMaxPoints * 4);
-constexpr size_t kOffCellcid = kOffFmark + up(kMaxPoints * 4);
+constexpr size_t kOffCellcid = kOffFmark + up((kMaxPoints + 1) * 4);
 constexpr size_t kOffLab = kOffCellcid + up(kMaxPoints * 4);
 constexpr size_t kOffAsym = kOffLab + up(kMaxPoints * 4);
 constexpr size_t kOffHvCell = kOffAsym + up(gd::kAsymCap * 8);
@@ -135,7 +139,7 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   static_assert(kSortTempBytes >= 16 * 256 * 4 + 256 + 256, "sort temp too small");
   if (gdprim::sort_temp_bytes(kMaxPoints) > kSortTempBytes ||
       gdprim::scan_temp_bytes((int64_t)kTableCells + 1) > kScanTempBytes ||
-      gdprim::scan_temp_bytes(kMaxPoints) > kScanTempBytes)
+      gdprim::scan_temp_bytes(kMaxPoints + 1) > kScanTempBytes)
     return fail(GD_EINVAL, "gd_dbscan_noalloc: scratch layout inconsistent (build error)");
 
   int dev = 0;
@@ -147,84 +151,91 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   gd_status st = scratch_of(dev, &base);
   if (st != GD_OK) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const int D = dim;
 
-  gd::DevParams* dP = reinterpret_cast<gd::DevParams*>(base + kOffSmall);
-  uint32_t* dM = reinterpret_cast<uint32_t*>(base + kOffSmall + 512);
-  uint32_t* dK = reinterpret_cast<uint32_t*>(base + kOffSmall + 516);
-  int* dFlags = reinterpret_cast<int*>(base + kOffSmall + 520);
-  unsigned long long* dCtr = reinterpret_cast<unsigned long long*>(base + kOffSmall + 640);
+  uint32_t* dM = reinterpret_cast<uint32_t*>(base + kOffSmall);
+  uint32_t* dK = reinterpret_cast<uint32_t*>(base + kOffSmall + 4);
+  unsigned long long* dCtr = reinterpret_cast<unsigned long long*>(base + kOffSmall + 128);
 
-  // index build (the same stages as gd_index_build)
+  // the run description: one instance, chunks of kChunkPoints points
+  gd::InstDesc desc{0, n, 0, eps, dim, minpts};
+  gd::Chunk chunks[kMaxChunks];
+  int nch = 0;
+  for (int64_t b = 0; b < n; b += gd::kChunkPoints, ++nch)
+    chunks[nch] = gd::Chunk{0, 0, b, std::min<int64_t>(n, b + gd::kChunkPoints)};
   NA_CUDA(cudaMemsetAsync(base + kOffSmall, 0, 4096, s), "clear counters");
-  int nb = (int)std::min<int64_t>(kBboxBlocks, (n + 255) / 256);
-  double* partial = reinterpret_cast<double*>(base + kOffPartial);
-  gdl::bbox(coords_dev, n, D, partial, nb, dFlags, s);
-  gdl::params(partial, nb, D, dP, eps, minpts, 0.5 * (1.0 + 1.0 / 65536.0), kTableCells, dFlags, s);
-  gd::DevParams hp;
-  NA_CUDA(cudaMemcpyAsync(&hp, dP, sizeof hp, cudaMemcpyDeviceToHost, s), "read grid parameters");
+  NA_CUDA(cudaMemsetAsync(base + kOffBi, 0, sizeof(gd::BatchInfo), s), "clear layout");
+  NA_CUDA(cudaMemcpyAsync(base + kOffInst, &desc, sizeof desc, cudaMemcpyHostToDevice, s),
+          "upload instance");
+  NA_CUDA(cudaMemcpyAsync(base + kOffChunks, chunks, nch * sizeof(gd::Chunk),
+                          cudaMemcpyHostToDevice, s), "upload chunks");
+  gdl::Bufs B;
+  B.coords = coords_dev;
+  B.inst = reinterpret_cast<const gd::InstDesc*>(base + kOffInst);
+  B.chunks = reinterpret_cast<const gd::Chunk*>(base + kOffChunks);
+  B.Pv = reinterpret_cast<gd::DevParams*>(base + kOffPv);
+  B.Bi = reinterpret_cast<gd::BatchInfo*>(base + kOffBi);
+  B.bbox = reinterpret_cast<long long*>(base + kOffBbox);
+  B.M = dM;
+  B.ctr = dCtr;
+  // index build (the same stages as gd_index_build)
+  gdl::grids(B, 1, nch, 0.5 * (1.0 + 1.0 / 65536.0), 0.5 * (1.0 + 1.0 / 65536.0), kTableCells,
+             0, s);
+  gd::BatchInfo bi;
+  NA_CUDA(cudaMemcpyAsync(&bi, base + kOffBi, sizeof bi, cudaMemcpyDeviceToHost, s),
+          "read run layout");
   NA_CUDA(cudaStreamSynchronize(s), "grid parameters");
-  if (hp.flags & gd::kFlagNonFinite)
+  if (bi.flags & gd::kFlagNonFinite)
     return fail(GD_EINVAL, "gd_dbscan_noalloc: input has NaN or Inf coordinates");
-  if (hp.flags & gd::kFlagGridTooLarge)
+  if (bi.flags & gd::kFlagGridTooLarge)
     return fail(GD_ERANGE, "gd_dbscan_noalloc: eps-cell grid too large");
-  const bool f32 = precision == GD_PREC_FP32_BAND && hp.eps2_lo32 > 0.0f;
-  const bool sparse = hp.sparse != 0;
-  const uint64_t C = hp.C;
-  gdl::keys(coords_dev, n, D, sparse, dP, base + kOffKeys0, sms, s);
+  const bool f32 = precision == GD_PREC_FP32_BAND;
+  const bool key64 = bi.key64 != 0;
+  const bool xf = f32 || bi.any_xf;
+  const int dims = dim == 2 ? 1 : 2;
+  const int key_bits = bi.LB + bi.IB;
+  gdl::keys(B, key64, nch, base + kOffKeys0, s);
   uint32_t* vb[2] = {reinterpret_cast<uint32_t*>(base + kOffVals0),
                      reinterpret_cast<uint32_t*>(base + kOffVals1)};
   const void* skeys;
   int r;
-  if (sparse) {
+  if (key64) {
     using U64 = unsigned long long;
     U64* kb[2] = {reinterpret_cast<U64*>(base + kOffKeys0), reinterpret_cast<U64*>(base + kOffKeys1)};
-    r = gdprim::radix_sort_pairs<U64>(kb, vb, n, hp.key_bits, true, base + kOffSortTemp, s);
+    r = gdprim::radix_sort_pairs<U64>(kb, vb, n, key_bits, true, base + kOffSortTemp, s);
     skeys = kb[r];
   } else {
     uint32_t* kb[2] = {reinterpret_cast<uint32_t*>(base + kOffKeys0),
                        reinterpret_cast<uint32_t*>(base + kOffKeys1)};
-    r = gdprim::radix_sort_pairs<uint32_t>(kb, vb, n, hp.key_bits, true, base + kOffSortTemp, s);
+    r = gdprim::radix_sort_pairs<uint32_t>(kb, vb, n, key_bits, true, base + kOffSortTemp, s);
     skeys = kb[r];
   }
-  uint32_t* ids = vb[r];
-  double* X = reinterpret_cast<double*>(base + kOffX);
-  float* Xf = reinterpret_cast<float*>(base + kOffXf);
-  gdl::gather(coords_dev, ids, n, D, f32 || hp.prune, dP, X, Xf, sms, s);
-  uint32_t* fl = reinterpret_cast<uint32_t*>(base + kOffRunfl);
-  uint32_t* pos = reinterpret_cast<uint32_t*>(base + kOffRunpos);
-  int* reps = reinterpret_cast<int*>(base + kOffReps);
-  gdl::run_flags(skeys, sparse, n, fl, sms, s);
-  gdprim::exclusive_scan_u32(fl, pos, n, base + kOffScanTemp, dM, s);
-  gdl::run_scatter(fl, pos, n, reps, dM, dCtr, sms, s);
-  unsigned long long* hkeys = reinterpret_cast<unsigned long long*>(base + kOffHkeys);
-  uint32_t* hvals = reinterpret_cast<uint32_t*>(base + kOffHvals);
-  uint32_t* table = reinterpret_cast<uint32_t*>(base + kOffTable);
-  if (sparse) {
-    NA_CUDA(cudaMemsetAsync(hkeys, 0xff, kHashSlots * 8, s), "clear cell hash");
-    gdl::hash_insert(static_cast<const unsigned long long*>(skeys), reps, dM, n, hkeys, hvals,
-                     (uint32_t)(kHashSlots - 1), sms, s);
-  } else {
-    NA_CUDA(cudaMemsetAsync(table, 0, (C + 1) * 4, s), "clear cell table");
-    gdl::cell_counts(static_cast<const uint32_t*>(skeys), reps, dM, n, table, sms, s);
-    gdprim::exclusive_scan_u32(table, table, (int64_t)C + 1, base + kOffScanTemp, nullptr, s);
+  B.keys = skeys;
+  B.ids = vb[r];
+  B.X = reinterpret_cast<double*>(base + kOffX);
+  B.Xf = reinterpret_cast<float*>(base + kOffXf);
+  B.runfl = reinterpret_cast<uint32_t*>(base + kOffRunfl);
+  B.runpos = reinterpret_cast<uint32_t*>(base + kOffRunpos);
+  B.reps = reinterpret_cast<int*>(base + kOffReps);
+  B.start = reinterpret_cast<uint32_t*>(base + kOffTable);
+  B.hkeys = reinterpret_cast<unsigned long long*>(base + kOffHkeys);
+  B.hvals = reinterpret_cast<uint32_t*>(base + kOffHvals);
+  B.hmask = (uint32_t)(kHashSlots - 1);
+  gdl::gather(B, key64, n, xf, sms, s);
+  gdl::run_flags(skeys, key64, n, B.runfl, sms, s);
+  gdprim::exclusive_scan_u32(B.runfl, B.runpos, n, base + kOffScanTemp, dM, s);
+  gdl::run_scatter(B, key64, n, sms, s);
+  if (bi.table_total) {
+    NA_CUDA(cudaMemsetAsync(B.start, 0, bi.table_total * 4, s), "clear cell table");
+    gdl::cell_counts(B, key64, n, sms, s);
+    gdprim::exclusive_scan_u32(B.start, B.start, (int64_t)bi.table_total, base + kOffScanTemp,
+                               nullptr, s);
+  }
+  if (bi.any_sparse) {
+    NA_CUDA(cudaMemsetAsync(B.hkeys, 0xff, kHashSlots * 8, s), "clear cell hash");
+    gdl::hash_insert(B, key64, n, sms, s);
   }
 
   // expansion (the same stages as gd_expand)
-  gdl::Bufs B;
-  B.P = dP;
-  B.keys = skeys;
-  B.ids = ids;
-  B.reps = reps;
-  B.M = dM;
-  B.runfl = fl;
-  B.runpos = pos;
-  B.start = table;
-  B.hkeys = hkeys;
-  B.hvals = hvals;
-  B.hmask = (uint32_t)(kHashSlots - 1);
-  B.X = X;
-  B.Xf = Xf;
   B.core = base + kOffCore;
   B.cellcore = reinterpret_cast<int*>(base + kOffCellcore);
   B.cellmin = reinterpret_cast<int*>(base + kOffCellmin);
@@ -235,14 +246,13 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   B.asym = reinterpret_cast<int*>(base + kOffAsym);
   B.hv_cell = reinterpret_cast<int*>(base + kOffHvCell);
   B.hv_mask = reinterpret_cast<unsigned long long*>(base + kOffHvMask);
-  B.ctr = dCtr;
-  gdl::core(B, n, D, f32, sparse, sms, s);
-  gdl::unite(B, n, D, f32, sparse, sms, s);
-  NA_CUDA(cudaMemsetAsync(B.Fmark, 0, n * 4, s), "clear cluster marks");
+  gdl::core(B, n, dims, f32, key64, sms, s);
+  gdl::unite(B, n, dims, f32, key64, sms, s);
+  NA_CUDA(cudaMemsetAsync(B.Fmark, 0, (n + 1) * 4, s), "clear cluster marks");
   gdl::roots(B, n, sms, s);
-  gdprim::exclusive_scan_u32(B.Fmark, B.Fmark, n, base + kOffScanTemp, dK, s);
-  gdl::label(B, n, sms, s);
-  gdl::border(B, n, D, f32, sparse, sms, s);
+  gdprim::exclusive_scan_u32(B.Fmark, B.Fmark, n + 1, base + kOffScanTemp, dK, s);
+  gdl::label(B, key64, n, sms, s);
+  gdl::border(B, n, dims, f32, key64, sms, s);
   gdl::scatter_labels(B, n, labels_dev, nullptr, sms, s);
   NA_CUDA(cudaGetLastError(), "launch");
   unsigned long long asym_edges = 0;

@@ -1,15 +1,20 @@
-// gd_pipeline.cu -- the exact-DBSCAN kernels for one instance.
+// gd_pipeline.cu -- the exact-DBSCAN kernels.
 //
 // Replaces, in the reference (CUDA-DClust+):
-//   host bbox + bin widths        main.cu:166-207           -> k_bbox_partial, k_params
+//   host bbox + bin widths        main.cu:166-207           -> k_bbox_chunk, k_params_inst
 //   INDEXING_STRUCTURE/insertData indexing.cu:54-118        -> k_keys (cell keys)
 //   thrust::sort_by_key           main.cu:332               -> gdprim::radix_sort_pairs
 //   INDEXING_ADJUSTMENT           indexing.cu:23-51         -> k_run_flags/k_run_scatter/
-//                                                              k_cell_counts + scan (cell table)
-//   DBSCAN kernel + searchPoints  dbscan.cu:254-474         -> k_core (core flags)
-//   MarkAsCandidate + host merge  dbscan.cu:189-222, 25-187 -> k_union (device union-find)
-//   GetDbscanResult               dbscan.cu:225-251         -> k_roots, k_label, k_border,
+//                                                              k_cell_counts + scan / k_hash_insert
+//   DBSCAN kernel + searchPoints  dbscan.cu:254-474         -> k_core_scan, k_core_heavy
+//   MarkAsCandidate + host merge  dbscan.cu:189-222, 25-187 -> k_union_scan, k_union_heavy,
+//                                                              k_asym_resolve (device union-find)
+//   GetDbscanResult               dbscan.cu:225-251         -> k_roots, k_label, k_border_*,
 //                                                              k_scatter_labels
+//
+// A run clusters K >= 1 independent instances at once: every cell key carries
+// the instance id above the instance's local cell key, so one radix sort, one
+// cell list and one launch per phase (per dimension present) serve them all.
 //
 // Grid: fine cells of side f = eps * m, m = 0.5 * (1 + 2^-16) by default, keyed
 // x-major.  Two points of one cell are always neighbours (cell diagonal
@@ -33,102 +38,90 @@
 namespace gd {
 
 // ------------------------------------------------------------------ bbox
-constexpr int kBboxThreads = 256;
-
 // Doubles ordered as int64 (monotone for non-NaN values): min/max run on the
 // integer pipe instead of the much slower float64 pipe of this GPU.
-__device__ __forceinline__ long long ord_of(double v) {
-  long long b = __double_as_longlong(v);
-  return b >= 0 ? b : b ^ 0x7fffffffffffffffLL;
-}
 __device__ __forceinline__ double dbl_of(long long o) {
   return __longlong_as_double(o >= 0 ? o : o ^ 0x7fffffffffffffffLL);
 }
 
-template <int D>
-__global__ void __launch_bounds__(kBboxThreads)
-k_bbox_partial(const double* __restrict__ pts, int64_t n, long long* __restrict__ partial,
-               int* __restrict__ flags) {
-  long long lo[D], hi[D];
-#pragma unroll
-  for (int k = 0; k < D; ++k) { lo[k] = LLONG_MAX; hi[k] = LLONG_MIN; }
+__global__ void k_bbox_init(const gdl::Bufs B, int K) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x)
+    for (int k = 0; k < 6; ++k) B.bbox[i * 6 + k] = k < 3 ? LLONG_MAX : LLONG_MIN;
+}
+
+constexpr int kBboxThreads = 256;
+
+// one block per chunk of one instance; one atomic per block and bound
+__global__ void __launch_bounds__(kBboxThreads) k_bbox_chunk(const gdl::Bufs B) {
+  const Chunk c = B.chunks[blockIdx.x];
+  const InstDesc I = B.inst[c.inst];
+  const int dim = I.dim;
+  long long lo[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, hi[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
   bool bad = false;
-  const long long* __restrict__ bits = reinterpret_cast<const long long*>(pts);
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
+  const long long* __restrict__ bits = reinterpret_cast<const long long*>(B.coords + I.co_off);
+  for (int64_t g = c.begin + threadIdx.x; g < c.end; g += blockDim.x) {
+    const int64_t l = g - I.pt_off;
 #pragma unroll
-    for (int k = 0; k < D; ++k) {
-      long long bv = bits[i * D + k];
+    for (int k = 0; k < 3; ++k) {
+      if (k >= dim) break;
+      const long long bv = bits[l * dim + k];
       bad |= (bv & 0x7ff0000000000000LL) == 0x7ff0000000000000LL;
-      long long o = bv >= 0 ? bv : bv ^ 0x7fffffffffffffffLL;
+      const long long o = bv >= 0 ? bv : bv ^ 0x7fffffffffffffffLL;
       lo[k] = min(lo[k], o);
       hi[k] = max(hi[k], o);
     }
   }
-  __shared__ long long s[2 * D][kBboxThreads / 32];
+  __shared__ long long s[6][kBboxThreads / 32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-  for (int k = 0; k < D; ++k) {
+  for (int k = 0; k < 3; ++k) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       lo[k] = min(lo[k], __shfl_xor_sync(kFull, lo[k], o));
       hi[k] = max(hi[k], __shfl_xor_sync(kFull, hi[k], o));
     }
-    if (lane == 0) { s[k][w] = lo[k]; s[D + k][w] = hi[k]; }
+    if (lane == 0) { s[k][w] = lo[k]; s[3 + k][w] = hi[k]; }
   }
-  if (__any_sync(kFull, bad) && lane == 0) atomicOr(flags, kFlagNonFinite);
+  if (__any_sync(kFull, bad) && lane == 0) atomicOr(&B.Bi->flags, kFlagNonFinite);
   __syncthreads();
-  if (threadIdx.x < 2 * D) {
+  if (threadIdx.x < 6) {
     const int k = threadIdx.x;
-    long long v = s[k][0];
-    for (int j = 1; j < kBboxThreads / 32; ++j) v = k < D ? min(v, s[k][j]) : max(v, s[k][j]);
-    partial[blockIdx.x * 2 * D + k] = v;
+    if ((k % 3) < dim) {
+      long long v = s[k][0];
+      for (int j = 1; j < kBboxThreads / 32; ++j) v = k < 3 ? min(v, s[k][j]) : max(v, s[k][j]);
+      if (k < 3) atomicMin(B.bbox + c.inst * 6 + k, v);
+      else atomicMax(B.bbox + c.inst * 6 + k, v);
+    }
   }
 }
 
-// One block: reduce the partial boxes; thread 0 derives the grid and the
-// float32 band.
-template <int D>
-__global__ void __launch_bounds__(256)
-k_params(const long long* __restrict__ partial, int nblocks, DevParams* P, double eps, int minpts,
-         double cell_mult, uint64_t max_cells, const int* __restrict__ flags) {
-  __shared__ long long s[2 * D][256];
-  long long lo[D], hi[D];
-#pragma unroll
-  for (int k = 0; k < D; ++k) { lo[k] = LLONG_MAX; hi[k] = LLONG_MIN; }
-  for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
-#pragma unroll
-    for (int k = 0; k < D; ++k) {
-      lo[k] = min(lo[k], partial[b * 2 * D + k]);
-      hi[k] = max(hi[k], partial[b * 2 * D + k + D]);
-    }
-#pragma unroll
-  for (int k = 0; k < D; ++k) { s[k][threadIdx.x] = lo[k]; s[D + k][threadIdx.x] = hi[k]; }
-  __syncthreads();
-  for (int st = 128; st > 0; st >>= 1) {
-    if (threadIdx.x < st)
-#pragma unroll
-      for (int k = 0; k < D; ++k) {
-        s[k][threadIdx.x] = min(s[k][threadIdx.x], s[k][threadIdx.x + st]);
-        s[D + k][threadIdx.x] = max(s[D + k][threadIdx.x], s[D + k][threadIdx.x + st]);
-      }
-    __syncthreads();
-  }
-  if (threadIdx.x != 0) return;
+// One thread per instance: its grid and float32 band from its bounding box.
+__global__ void k_params_inst(const gdl::Bufs B, int K, double mult2, double mult3,
+                              uint64_t dense_floor, uint64_t dense_per_point) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= K) return;
+  const InstDesc I = B.inst[i];
+  const int D = I.dim;
+  const double eps = I.eps;
   DevParams p;
-  int fl = *flags;
+  int fl = 0;
   for (int k = 0; k < 3; ++k) { p.lo[k] = 0; p.hi[k] = 0; p.centre[k] = 0; p.G[k] = 1; }
-  for (int k = 0; k < D; ++k) {
-    p.lo[k] = dbl_of(s[k][0]);
-    p.hi[k] = dbl_of(s[D + k][0]);
-    p.centre[k] = 0.5 * p.lo[k] + 0.5 * p.hi[k];
-  }
+  if (I.n > 0)
+    for (int k = 0; k < D; ++k) {
+      p.lo[k] = dbl_of(B.bbox[i * 6 + k]);
+      p.hi[k] = dbl_of(B.bbox[i * 6 + 3 + k]);
+      p.centre[k] = 0.5 * p.lo[k] + 0.5 * p.hi[k];
+    }
   p.dim = D;
-  p.minpts = minpts;
+  p.minpts = I.minpts;
   p.eps = eps;
   p.eps2 = __dmul_rn(eps, eps);
-  p.f = __dmul_rn(eps, cell_mult);
+  p.f = __dmul_rn(eps, D == 2 ? mult2 : mult3);
   p.inv_f = 1.0 / p.f;
+  p.pt_off = I.pt_off;
+  p.n = I.n;
+  p.co_off = I.co_off;
+  p.inst = i;
   double cells = 1.0;
   uint64_t C = 1;
   for (int k = 0; k < D; ++k) {
@@ -138,9 +131,11 @@ k_params(const long long* __restrict__ partial, int nblocks, DevParams* P, doubl
     cells *= t;
     C *= (uint64_t)p.G[k];
   }
-  // keys must fit 62 bits; a grid beyond the dense-table limit uses the hash
+  // local keys must fit 62 bits; a grid beyond the dense-table limit uses the hash
   if (!(cells < 4.0e18)) fl |= kFlagGridTooLarge;
-  p.sparse = (cells > (double)max_cells || C > max_cells) ? 1 : 0;
+  uint64_t limit = (uint64_t)I.n * dense_per_point;
+  if (limit < dense_floor) limit = dense_floor;
+  p.sparse = (cells > (double)limit || C > limit) ? 1 : 0;
   p.C = C;
   int bits = 0;
   while (bits < 63 && (C - 1) >> bits) ++bits;
@@ -157,19 +152,19 @@ k_params(const long long* __restrict__ partial, int nblocks, DevParams* P, doubl
     p.eps2_in = -1.0;
     fl |= kFlagNoShortcut;
   }
-  // float32 band.  a_k = fl32(x_k - c_k) is off from x_k - c_k by at most
-  // ea = R 2^-24 (R bounds |x_k - c_k|).  For a pair with true squared distance
-  // S, the float32 value s = fl(fl(u0^2) + ...), u_k = fl32(a_pk - a_qk), obeys
-  //   |s - S| <= (S + 4 ea sqrt(D S) + 4 D ea^2)(D + 3) 2^-24
-  //              + 4 ea sqrt(D S) + 4 D ea^2  =: B(S)
-  // (coordinate error, one rounding per subtraction, D roundings in the FMA
-  // chain).  Evaluated at S = 2 eps^2 and padded by 1.5 this is bmax.  Then
-  //   s < L = eps^2 (1 - 2^-17) - bmax  =>  S < eps^2 (1 - 2^-17)
-  //        =>  float64 d2 <= eps2_in  =>  neighbour both ways (box test passes);
-  //   s > H = eps^2 (1 + 2^-17) + bmax  =>  float64 d2 > eps2  =>  not a neighbour.
-  // L is rounded down and H up to float32.  Pairs with L <= s <= H take the
-  // float64 predicate.  The filter is off (fp64 only) when the bound is not small.
   {
+    // float32 band.  a_k = fl32(x_k - c_k) is off from x_k - c_k by at most
+    // ea = R 2^-24 (R bounds |x_k - c_k|).  For a pair with true squared distance
+    // S, the float32 value s = fl(fl(u0^2) + ...), u_k = fl32(a_pk - a_qk), obeys
+    //   |s - S| <= (S + 4 ea sqrt(D S) + 4 D ea^2)(D + 3) 2^-24
+    //              + 4 ea sqrt(D S) + 4 D ea^2  =: B(S)
+    // (coordinate error, one rounding per subtraction, D roundings in the FMA
+    // chain).  Evaluated at S = 2 eps^2 and padded by 1.5 this is bmax.  Then
+    //   s < L = eps^2 (1 - 2^-17) - bmax  =>  S < eps^2 (1 - 2^-17)
+    //        =>  float64 d2 <= eps2_in  =>  neighbour both ways (box test passes);
+    //   s > H = eps^2 (1 + 2^-17) + bmax  =>  float64 d2 > eps2  =>  not a neighbour.
+    // L is rounded down and H up to float32.  Pairs with L <= s <= H take the
+    // float64 predicate.  When the bound is not small every pair takes it.
     const double u32 = 1.0 / 16777216.0;               // 2^-24
     R = R * (1.0 + 1e-12) + 1e-300;
     const double ea = R * u32 * (1.0 + 1e-8);          // |fl32(x - c) - (x - c)|
@@ -183,7 +178,7 @@ k_params(const long long* __restrict__ partial, int nblocks, DevParams* P, doubl
     const bool ok = !(fl & kFlagNoShortcut) && e2 > 1e-30 && R < 1e30 && L > 0.25 * e2 &&
                     H < 4.0 * e2;
     p.eps2_lo32 = ok ? __double2float_rd(L) : -1.0f;
-    p.eps2_hi32 = ok ? __double2float_ru(H) : -1.0f;
+    p.eps2_hi32 = ok ? __double2float_ru(H) : INFINITY;
     // Cell-level classification.  A point's position inside its cell,
     // u_k = (fl32(x_k - c_k) - o_k) / f with o_k the cell origin in the same
     // centred float32 frame, is within uerr of the truth (coordinate and origin
@@ -202,44 +197,154 @@ k_params(const long long* __restrict__ partial, int nblocks, DevParams* P, doubl
     p.prune = (!(fl & kFlagNoShortcut) && uerr <= 1.0 / 256.0 && R < 1e30 && e2 > 1e-30) ? 1 : 0;
   }
   p.flags = fl;
-  *P = p;
+  p.table_off = 0;
+  p.kmask = 0;
+  p.LB = 0;
+  B.Pv[i] = p;
+}
+
+// One block: the run layout -- key widths, dense-table offsets (exclusive scan
+// over the dense instances' C+1 entries), flags.
+__global__ void __launch_bounds__(1024) k_layout(const gdl::Bufs B, int K) {
+  __shared__ unsigned long long s_part[32];
+  __shared__ int s_red[4][32];
+  __shared__ unsigned long long s_carry;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int lb = 0, fl = 0, sp = 0, xf = 0, md = 2, k2 = 0;
+  for (int i = threadIdx.x; i < K; i += blockDim.x) {
+    const DevParams& p = B.Pv[i];
+    if (p.n > 0) lb = max(lb, p.key_bits);
+    fl |= p.flags;
+    sp |= p.sparse;
+    xf |= p.prune;
+    md = max(md, p.dim);
+    k2 += p.dim == 2;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lb = max(lb, __shfl_xor_sync(kFull, lb, o));
+    fl |= __shfl_xor_sync(kFull, fl, o);
+    sp |= __shfl_xor_sync(kFull, sp, o);
+    xf |= __shfl_xor_sync(kFull, xf, o);
+    md = max(md, __shfl_xor_sync(kFull, md, o));
+    k2 += __shfl_xor_sync(kFull, k2, o);
+  }
+  if (lane == 0) { s_red[0][w] = lb; s_red[1][w] = fl | (sp << 16) | (xf << 17); s_red[2][w] = md; s_red[3][w] = k2; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int LB = 0, F = 0, MD = 2, K2 = 0;
+    for (int j = 0; j < 32; ++j) {
+      LB = max(LB, s_red[0][j]);
+      F |= s_red[1][j];
+      MD = max(MD, s_red[2][j]);
+      K2 += s_red[3][j];
+    }
+    int IB = 0;
+    while (IB < 31 && ((K - 1) >> IB)) ++IB;
+    BatchInfo bi;
+    bi.K = K;
+    bi.LB = LB;
+    bi.IB = IB;
+    bi.key64 = LB + IB > 32 ? 1 : 0;
+    bi.any_sparse = (F >> 16) & 1;
+    bi.any_xf = (F >> 17) & 1;
+    bi.flags = (F & 0xffff) | B.Bi->flags | (LB + IB > 62 ? kFlagGridTooLarge : 0);
+    bi.max_dim = MD;
+    bi.K2 = K2;
+    bi.pad = 0;
+    bi.table_total = 0;
+    *B.Bi = bi;
+    s_carry = 0;
+  }
+  __syncthreads();
+  const int LB = B.Bi->LB;
+  const uint64_t kmask = LB >= 64 ? ~0ull : ((1ull << LB) - 1ull);
+  // exclusive scan of the dense-table sizes, 1024 instances at a time
+  for (int base = 0; base < K; base += 1024) {
+    const int i = base + threadIdx.x;
+    unsigned long long v = 0;
+    if (i < K && !B.Pv[i].sparse && B.Pv[i].n > 0) v = B.Pv[i].C + 1;
+    unsigned long long inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned long long t = __shfl_up_sync(kFull, inc, o);
+      if (lane >= o) inc += t;
+    }
+    if (lane == 31) s_part[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+      unsigned long long t = s_part[lane];
+      unsigned long long ti = t;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long u = __shfl_up_sync(kFull, ti, o);
+        if (lane >= o) ti += u;
+      }
+      s_part[lane] = ti - t;
+    }
+    __syncthreads();
+    const unsigned long long ex = s_carry + s_part[w] + inc - v;
+    if (i < K) {
+      B.Pv[i].table_off = ex;
+      B.Pv[i].kmask = kmask;
+      B.Pv[i].LB = LB;
+    }
+    __syncthreads();
+    if (threadIdx.x == 1023) s_carry = ex + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) B.Bi->table_total = s_carry;
 }
 
 // ------------------------------------------------------------------ keys
-template <int D, class Key>
-__global__ void k_keys(const double* __restrict__ pts, int64_t n, const DevParams* __restrict__ Pp,
-                       Key* __restrict__ keys) {
-  const DevParams P = *Pp;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
+// One block per chunk: cell key of every point, instance id above the local key.
+template <class Key>
+__global__ void __launch_bounds__(256) k_keys(const gdl::Bufs B, Key* __restrict__ keys) {
+  const Chunk c = B.chunks[blockIdx.x];
+  const DevParams& P = B.Pv[c.inst];
+  const int D = P.dim;
+  double lo[3], inv_f = P.inv_f;
+  int64_t G[3];
+  for (int k = 0; k < 3; ++k) { lo[k] = P.lo[k]; G[k] = P.G[k]; }
+  const uint64_t hi = (uint64_t)P.inst << P.LB;
+  const double* __restrict__ pts = B.coords + P.co_off;
+  for (int64_t g = c.begin + threadIdx.x; g < c.end; g += blockDim.x) {
+    const int64_t l = g - P.pt_off;
     uint64_t key = 0;
 #pragma unroll
-    for (int k = 0; k < D; ++k) {
-      double t = __dmul_rn(__dsub_rn(pts[i * D + k], P.lo[k]), P.inv_f);
-      int64_t g = (int64_t)floor(t);
-      g = g < 0 ? 0 : (g >= P.G[k] ? P.G[k] - 1 : g);
-      key = key * (uint64_t)P.G[k] + (uint64_t)g;
+    for (int k = 0; k < 3; ++k) {
+      if (k >= D) break;
+      const double t = __dmul_rn(__dsub_rn(pts[l * D + k], lo[k]), inv_f);
+      int64_t q = (int64_t)floor(t);
+      q = q < 0 ? 0 : (q >= G[k] ? G[k] - 1 : q);
+      key = key * (uint64_t)G[k] + (uint64_t)q;
     }
-    keys[i] = (Key)key;
+    keys[g] = (Key)(hi | key);
   }
 }
 
-// sorted structure-of-arrays copy (+ float32 centred copy)
-template <int D, bool F32>
-__global__ void k_gather(const double* __restrict__ pts, const uint32_t* __restrict__ ids,
-                         int64_t n, const DevParams* __restrict__ Pp, double* __restrict__ X,
-                         float* __restrict__ Xf) {
-  double c[D];
-#pragma unroll
-  for (int k = 0; k < D; ++k) c[k] = Pp->centre[k];
+template <class Key>
+__device__ __forceinline__ int inst_of(Key key, int LB) {
+  return (int)((uint64_t)key >> LB);
+}
+
+// sorted structure-of-arrays copy (+ centred float32 copy)
+template <class Key, bool XF>
+__global__ void k_gather(const gdl::Bufs B, int64_t n) {
+  const int LB = B.Bi->LB;
+  const Key* __restrict__ keys = static_cast<const Key*>(B.keys);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t j = ids[i];
+    const int64_t g = B.ids[i];
+    const DevParams& P = B.Pv[inst_of(keys[i], LB)];
+    const int D = P.dim;
+    const double* __restrict__ src = B.coords + P.co_off + (g - P.pt_off) * D;
 #pragma unroll
-    for (int k = 0; k < D; ++k) {
-      double v = pts[j * D + k];
-      X[k * n + i] = v;
-      if (F32) Xf[k * n + i] = __double2float_rn(__dsub_rn(v, c[k]));
+    for (int k = 0; k < 3; ++k) {
+      if (k >= D) break;
+      const double v = src[k];
+      B.X[k * n + i] = v;
+      if (XF) B.Xf[k * n + i] = __double2float_rn(__dsub_rn(v, P.centre[k]));
     }
   }
 }
@@ -251,42 +356,63 @@ __global__ void k_run_flags(const Key* __restrict__ keys, int64_t n, uint32_t* _
     fl[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
 }
 
-__global__ void k_run_scatter(const uint32_t* __restrict__ fl, const uint32_t* __restrict__ pos,
-                              int64_t n, int* __restrict__ reps, const uint32_t* __restrict__ Mdev,
-                              unsigned long long* ctr) {
+__global__ void k_run_scatter(const gdl::Bufs B, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
-    if (fl[i]) reps[pos[i]] = (int)i;
+    if (B.runfl[i]) B.reps[B.runpos[i]] = (int)i;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    reps[*Mdev] = (int)n;
-    ctr[kCtrCells] = *Mdev;
+    B.reps[*B.M] = (int)n;
+    B.ctr[kCtrCells] = *B.M;
   }
 }
 
-__global__ void k_cell_counts(const uint32_t* __restrict__ keys, const int* __restrict__ reps,
-                              const uint32_t* __restrict__ Mdev, uint32_t* __restrict__ table) {
-  const int64_t M = *Mdev;
+// number of cells of 2D instances (2D instances come first): binary search
+template <class Key>
+__global__ void k_split(const gdl::Bufs B) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const Key* keys = static_cast<const Key*>(B.keys);
+  const int LB = B.Bi->LB, K2 = B.Bi->K2;
+  int64_t lo = 0, hi = *B.M;  // first cell with instance >= K2
+  while (lo < hi) {
+    const int64_t mid = (lo + hi) / 2;
+    if (inst_of(keys[B.reps[mid]], LB) < K2) lo = mid + 1;
+    else hi = mid;
+  }
+  B.ctr[kCtrCells2D] = (unsigned long long)lo;
+}
+
+// dense instances: counts into the instance's table slice (scanned afterwards)
+template <class Key>
+__global__ void k_cell_counts(const gdl::Bufs B) {
+  const Key* keys = static_cast<const Key*>(B.keys);
+  const int LB = B.Bi->LB;
+  const int64_t M = *B.M;
   for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
        m += (int64_t)gridDim.x * blockDim.x) {
-    int b = reps[m], e = reps[m + 1];
-    table[keys[b]] = (uint32_t)(e - b);
+    const int b = B.reps[m], e = B.reps[m + 1];
+    const Key key = keys[b];
+    const DevParams& P = B.Pv[inst_of(key, LB)];
+    if (P.sparse) continue;
+    B.start[P.table_off + ((uint64_t)key & P.kmask)] = (uint32_t)(e - b);
   }
 }
 
-// sparse grids: hash of the occupied cells, key -> cell index m
-__global__ void k_hash_insert(const unsigned long long* __restrict__ keys,
-                              const int* __restrict__ reps, const uint32_t* __restrict__ Mdev,
-                              unsigned long long* __restrict__ hkeys, uint32_t* __restrict__ hvals,
-                              uint32_t mask) {
-  const int64_t M = *Mdev;
+// sparse instances: hash of the occupied cells, global key -> cell index m
+template <class Key>
+__global__ void k_hash_insert(const gdl::Bufs B) {
+  const Key* keys = static_cast<const Key*>(B.keys);
+  const int LB = B.Bi->LB;
+  const int64_t M = *B.M;
+  const uint32_t mask = B.hmask;
   for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
        m += (int64_t)gridDim.x * blockDim.x) {
-    const unsigned long long k = keys[reps[m]];
+    const unsigned long long k = (unsigned long long)keys[B.reps[m]];
+    if (!B.Pv[inst_of(k, LB)].sparse) continue;
     uint32_t h = hash_key(k) & mask;
     for (uint32_t probe = 0; probe <= mask; ++probe) {
-      unsigned long long prev = atomicCAS(hkeys + h, kHashEmpty, k);
+      unsigned long long prev = atomicCAS(B.hkeys + h, kHashEmpty, k);
       if (prev == kHashEmpty || prev == k) {
-        hvals[h] = (uint32_t)m;
+        B.hvals[h] = (uint32_t)m;
         break;
       }
       h = (h + 1) & mask;
@@ -376,10 +502,10 @@ __device__ __forceinline__ float dist2_f32(const float* a, const float* b) {
 // Directed test "cand is a neighbour of centre".  One side is a staged point
 // (coords in smem), the other a candidate (coords in registers / memory).
 // stage_is_centre selects which is the centre of the query box.
-template <int D, bool F32>
+template <int D, bool F32, class PP>
 __device__ __forceinline__ bool pair_test(const double* sx, const float* sf, const Cand<D, F32>& c,
                                           const double* __restrict__ X, int64_t n, int64_t q,
-                                          bool stage_is_centre, const DevParams& P, Tally& t) {
+                                          bool stage_is_centre, const PP& P, Tally& t) {
   if (F32) {
     ++t.t32;
     float s = dist2_f32<D>(sf, c.f);
@@ -401,10 +527,10 @@ __device__ __forceinline__ bool pair_test(const double* sx, const float* sf, con
 
 // Symmetric test for core-core links: true when the pair is a neighbour in both
 // directions; counts pairs that are neighbours in exactly one direction.
-template <int D, bool F32>
+template <int D, bool F32, class PP>
 __device__ __forceinline__ bool link_test(const double* sx, const float* sf, const Cand<D, F32>& c,
                                           const double* __restrict__ X, int64_t n, int a, int q,
-                                          const DevParams& P, Tally& t,
+                                          const PP& P, Tally& t,
                                           int* __restrict__ asym_list, unsigned long long* ctr) {
   double qx[D];
   if (F32) {
@@ -461,16 +587,19 @@ __device__ __forceinline__ int warp_min_i32(int v) {
   return v;
 }
 
-// Cell lookup.  Dense grids: the cell table gives every cell's point range.
-// Sparse grids: a hash of the occupied cells' keys gives the cell index m, and
-// reps[m]..reps[m+1] its points.  The probe loop is bounded by the table size.
-template <bool SPARSE>
+// Cell lookup inside one instance.  Dense grids: the instance's slice of the
+// cell tables gives every cell's point range.  Sparse grids: a hash of the
+// occupied cells' global keys gives the cell index m, and reps[m]..reps[m+1]
+// its points.  The probe loop is bounded by the table size.
 struct GridView {
   const uint32_t* start;
   const unsigned long long* hkeys;
   const uint32_t* hvals;
   const int* reps;
   uint32_t hmask;
+  int sparse;
+  uint64_t table_off;
+  uint64_t hi;  // instance id << LB
 
   __device__ __forceinline__ int find(uint64_t k) const {
     uint32_t h = hash_key(k) & hmask;
@@ -482,36 +611,37 @@ struct GridView {
     }
     return -1;
   }
-  // points of cell k: [x, y)
+  // points of the cell with local key k: [x, y)
   __device__ __forceinline__ int2 cell(uint64_t k) const {
-    if (!SPARSE) return make_int2((int)start[k], (int)start[k + 1]);
-    int m = find(k);
+    if (!sparse) return make_int2((int)start[table_off + k], (int)start[table_off + k + 1]);
+    int m = find(hi | k);
     return m < 0 ? make_int2(0, 0) : make_int2(reps[m], reps[m + 1]);
   }
-  // points of the cells k0..k1 (consecutive keys along one row): one contiguous
-  // range, because no other key sorts between them
+  // points of the cells k0..k1 (consecutive local keys along one row): one
+  // contiguous range, because no other key sorts between them
   __device__ __forceinline__ int2 span(uint64_t k0, uint64_t k1) const {
-    if (!SPARSE) return make_int2((int)start[k0], (int)start[k1 + 1]);
-    int lo = INT_MAX, hi = 0;
+    if (!sparse)
+      return make_int2((int)start[table_off + k0], (int)start[table_off + k1 + 1]);
+    int lo = INT_MAX, hi2 = 0;
     for (uint64_t k = k0; k <= k1; ++k) {
-      int m = find(k);
+      int m = find(hi | k);
       if (m >= 0) {
         lo = min(lo, reps[m]);
-        hi = max(hi, reps[m + 1]);
+        hi2 = max(hi2, reps[m + 1]);
       }
     }
-    return lo == INT_MAX ? make_int2(0, 0) : make_int2(lo, hi);
+    return lo == INT_MAX ? make_int2(0, 0) : make_int2(lo, hi2);
   }
 };
 
-template <bool SPARSE>
-__host__ __device__ __forceinline__ GridView<SPARSE> view_of(const gdl::Bufs& B) {
-  return GridView<SPARSE>{B.start, B.hkeys, B.hvals, B.reps, B.hmask};
+__device__ __forceinline__ GridView view_of(const gdl::Bufs& B, const DevParams& P) {
+  return GridView{B.start, B.hkeys, B.hvals, B.reps, B.hmask, P.sparse, P.table_off,
+                  (uint64_t)P.inst << P.LB};
 }
 
-template <bool SPARSE>
+template <bool KEY64>
 __device__ __forceinline__ uint64_t key_at(const gdl::Bufs& B, int64_t i) {
-  if (SPARSE) return static_cast<const unsigned long long*>(B.keys)[i];
+  if (KEY64) return static_cast<const unsigned long long*>(B.keys)[i];
   return static_cast<const uint32_t*>(B.keys)[i];
 }
 
@@ -520,6 +650,28 @@ __device__ __forceinline__ int rep_of(const gdl::Bufs& B, int64_t i) {
   return B.reps[B.runpos[i] + B.runfl[i] - 1];
 }
 
+// The cell a kernel thread/warp works on: instance parameters and local key.
+struct CellCtx {
+  const DevParams* P;
+  uint64_t local;
+};
+
+template <bool KEY64>
+__device__ __forceinline__ CellCtx cell_ctx(const gdl::Bufs& B, int b, int LB) {
+  const uint64_t key = key_at<KEY64>(B, b);
+  CellCtx c;
+  c.P = B.Pv + (int)(key >> LB);
+  c.local = key & c.P->kmask;
+  return c;
+}
+
+// cell range of dimension D: 2D instances' cells come first
+template <int D>
+__device__ __forceinline__ void dim_range(const gdl::Bufs& B, int64_t& mlo, int64_t& mhi) {
+  const int64_t M = *B.M, M2 = (int64_t)B.ctr[kCtrCells2D];
+  mlo = D == 2 ? 0 : M2;
+  mhi = D == 2 ? M2 : M;
+}
 
 // ------------------------------------------------------------ stencil tables
 // Offsets within +-2 cells, built at compile time.  kRows: the (ox, oy) rows a
@@ -588,9 +740,9 @@ struct RowList {
   int pre[32];
 };
 
-template <int D, bool SPARSE>
-__device__ __forceinline__ int build_rows(RowList& RL, const GridView<SPARSE>& gv,
-                                          const CellXYZ<D>& cc, const DevParams& P, int lane) {
+template <int D>
+__device__ __forceinline__ int build_rows(RowList& RL, const GridView& gv, const CellXYZ<D>& cc,
+                                          const DevParams& P, int lane) {
   const OffTab& T = kRows[D - 2];
   const int64_t Gl = P.G[D - 1];
   const int64_t cl = cc.c[D - 1];
@@ -641,18 +793,16 @@ __device__ __forceinline__ void cell_origin32(const CellXYZ<D>& cc, const DevPar
 }
 
 // A point's position inside its own cell, in cell units (error <= P.uerr).
-template <int D>
-__device__ __forceinline__ void frac_pos(const float* xf, const float* o, const DevParams& P,
-                                         float* u) {
+template <int D, class PP>
+__device__ __forceinline__ void frac_pos(const float* xf, const float* o, const PP& P, float* u) {
 #pragma unroll
   for (int k = 0; k < D; ++k) u[k] = __fmul_rn(__fsub_rn(xf[k], o[k]), P.inv_f32);
 }
 
 // Cell at offset (ox, oy, oz) from the point's cell: 1 every point in it is a
 // neighbour (both ways), -1 none is, 0 must be tested.
-template <int D>
-__device__ __forceinline__ int classify(const float* u, int ox, int oy, int oz,
-                                        const DevParams& P) {
+template <int D, class PP>
+__device__ __forceinline__ int classify(const float* u, int ox, int oy, int oz, const PP& P) {
   const int off[3] = {ox, oy, oz};
   float smax = 0.0f, smin = 0.0f;
 #pragma unroll
@@ -677,9 +827,9 @@ __device__ __forceinline__ int classify(const float* u, int ox, int oy, int oz,
 // a cell that needs more is appended to the heavy list and handled by the
 // warp-cooperative *_heavy kernel that follows.
 constexpr int kScanThreadsPerBlock = 256;
-constexpr int kInlineCoreTests = 160;    // points x candidates done by one thread
+constexpr int kInlineCoreTests = 160;    // candidates one thread tests for one point
 constexpr int kInlineLinkTests = 48;     // tests before a link search goes to a warp
-constexpr int kInlineBorderTests = 160;  // non-core points x candidate cores
+constexpr int kInlineBorderTests = 160;  // tests one thread spends on a cell's borders
 
 // warp-aggregated append to the heavy list (all 32 lanes must call it)
 __device__ __forceinline__ void heavy_push(const gdl::Bufs& B, int slot, bool push, int64_t m,
@@ -708,28 +858,30 @@ __device__ __forceinline__ void load_point(double* x, float* f, const gdl::Bufs&
   }
 }
 
-template <int D, bool F32, bool SPARSE>
+template <int D, bool F32, bool KEY64>
 __global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::Bufs B, int64_t n) {
-  __shared__ DevParams sP;
-  if (threadIdx.x == 0) sP = *B.P;
-  __syncthreads();
-  const DevParams& P = sP;
-  const GridView<SPARSE> gv = view_of<SPARSE>(B);
   const OffTab& T = kRows[D - 2];
   const int lane = threadIdx.x & 31;
-  const bool prune = P.prune != 0;
-  const int64_t M = *B.M;
+  const int LB = B.Bi->LB;
+  int64_t mlo, mhi;
+  dim_range<D>(B, mlo, mhi);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   Tally t;
-  for (int64_t m0 = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); m0 < M; m0 += stride) {
+  for (int64_t m0 = mlo + (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); m0 < mhi;
+       m0 += stride) {
     const int64_t m = m0 + lane;
     bool push = false;
-    if (m < M) {
+    if (m < mhi) {
       const int b = B.reps[m], e = B.reps[m + 1], sz = e - b;
-      if (sz >= P.minpts) {
+      const CellCtx cx = cell_ctx<KEY64>(B, b, LB);
+      const DevParams& P = *cx.P;
+      const PredParams Q = pred_params(P);
+      if (sz >= Q.minpts) {
         push = true;  // dense: the warp kernel marks it
       } else {
-        const CellXYZ<D> cc = decompose<D>(key_at<SPARSE>(B, b), P);
+        const GridView gv = view_of(B, P);
+        const bool prune = Q.prune != 0;
+        const CellXYZ<D> cc = decompose<D>(cx.local, P);
         const int64_t Gl = P.G[D - 1], cl = cc.c[D - 1];
         const int64_t l0 = cl - 2 < 0 ? 0 : cl - 2;
         const int64_t l1 = cl + 2 >= Gl ? Gl - 1 : cl + 2;
@@ -742,14 +894,14 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::B
           total += rg.y - rg.x;
         }
         int ncore = 0, mn = INT_MAX;
-        if (total >= P.minpts) {
+        if (total >= Q.minpts) {
           float o[D];
           if (prune) cell_origin32<D>(cc, P, o);
           for (int i = b; i < e && !push; ++i) {
             double px[D];
             float pf[D], u[D];
             load_point<D, F32>(px, pf, B, n, i, prune);
-            if (prune) frac_pos<D>(pf, o, P, u);
+            if (prune) frac_pos<D>(pf, o, Q, u);
             // pass 1: cells wholly inside count without a test; sum the rest
             int cnt = 0, ptot = total;
             if (prune) {
@@ -762,41 +914,41 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::B
                   const int2 c = gv.cell((uint64_t)(rowkey + z));
                   if (c.x == c.y) continue;
                   const int d = (int)(z - cl);
-                  const int cls = D == 3 ? classify<D>(u, T.o[r][0], T.o[r][1], d, P)
-                                         : classify<D>(u, T.o[r][0], d, 0, P);
+                  const int cls = D == 3 ? classify<D>(u, T.o[r][0], T.o[r][1], d, Q)
+                                         : classify<D>(u, T.o[r][0], d, 0, Q);
                   if (cls > 0) cnt += c.y - c.x;
                   else if (cls == 0) ptot += c.y - c.x;
                 }
               }
             }
-            if (cnt < P.minpts && cnt + ptot >= P.minpts) {
+            if (cnt < Q.minpts && cnt + ptot >= Q.minpts) {
               if (ptot > kInlineCoreTests) {
                 push = true;  // too many candidates for one thread
                 break;
               }
               // pass 2: test the undecided cells
-              for (int r = 0; r < T.n && cnt < P.minpts; ++r) {
+              for (int r = 0; r < T.n && cnt < Q.minpts; ++r) {
                 int64_t rowkey = offset_key<D>(cc, T.o[r][0], T.o[r][1], 0, P);
                 if (rowkey < 0) continue;
                 rowkey -= cl;
-                for (int64_t z = l0; z <= l1 && cnt < P.minpts; ++z) {
+                for (int64_t z = l0; z <= l1 && cnt < Q.minpts; ++z) {
                   const int2 c = gv.cell((uint64_t)(rowkey + z));
                   if (c.x == c.y) continue;
                   if (prune) {
                     const int d = (int)(z - cl);
-                    const int cls = D == 3 ? classify<D>(u, T.o[r][0], T.o[r][1], d, P)
-                                           : classify<D>(u, T.o[r][0], d, 0, P);
+                    const int cls = D == 3 ? classify<D>(u, T.o[r][0], T.o[r][1], d, Q)
+                                           : classify<D>(u, T.o[r][0], d, 0, Q);
                     if (cls != 0) continue;
                   }
-                  for (int q = c.x; q < c.y && cnt < P.minpts; ++q) {
+                  for (int q = c.x; q < c.y && cnt < Q.minpts; ++q) {
                     Cand<D, F32> cd;
                     load_cand<D, F32>(cd, B.X, B.Xf, n, q);
-                    cnt += pair_test<D, F32>(px, pf, cd, B.X, n, q, true, P, t) ? 1 : 0;
+                    cnt += pair_test<D, F32>(px, pf, cd, B.X, n, q, true, Q, t) ? 1 : 0;
                   }
                 }
               }
             }
-            const bool isc = cnt >= P.minpts;
+            const bool isc = cnt >= Q.minpts;
             B.core[i] = isc ? 1 : 0;
             if (isc) {
               ++ncore;
@@ -824,10 +976,9 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::B
 template <int D, bool F32>
 __device__ __forceinline__ int inline_link(const gdl::Bufs& B, int64_t n, int bA, int eA, int bB,
                                            int eB, const float* oA, int ox, int oy, int oz,
-                                           const DevParams& P, Tally& t) {
-  const bool prune = P.prune != 0;
+                                           const PredParams& Q, Tally& t) {
+  const bool prune = Q.prune != 0;
   int budget = kInlineLinkTests;
-  bool skipped = false;
   for (int a = bA; a < eA; ++a) {
     if (!B.core[a]) continue;
     double ax[D];
@@ -835,8 +986,8 @@ __device__ __forceinline__ int inline_link(const gdl::Bufs& B, int64_t n, int bA
     load_point<D, F32>(ax, af, B, n, a, prune);
     if (prune) {
       float u[D];
-      frac_pos<D>(af, oA, P, u);
-      const int cls = classify<D>(u, ox, oy, oz, P);
+      frac_pos<D>(af, oA, Q, u);
+      const int cls = classify<D>(u, ox, oy, oz, Q);
       if (cls > 0) return 1;
       if (cls < 0) continue;
     }
@@ -845,36 +996,37 @@ __device__ __forceinline__ int inline_link(const gdl::Bufs& B, int64_t n, int bA
       if (budget-- == 0) return -1;
       Cand<D, F32> cd;
       load_cand<D, F32>(cd, B.X, B.Xf, n, q);
-      if (link_test<D, F32>(ax, af, cd, B.X, n, a, q, P, t, B.asym, B.ctr)) return 1;
+      if (link_test<D, F32>(ax, af, cd, B.X, n, a, q, Q, t, B.asym, B.ctr)) return 1;
     }
   }
-  (void)skipped;
   return 0;
 }
 
-template <int D, bool F32, bool SPARSE>
+template <int D, bool F32, bool KEY64>
 __global__ void __launch_bounds__(kScanThreadsPerBlock)
 k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
-  __shared__ DevParams sP;
-  if (threadIdx.x == 0) sP = *B.P;
-  __syncthreads();
-  const DevParams& P = sP;
-  const GridView<SPARSE> gv = view_of<SPARSE>(B);
   const OffTab& T = kHalf[D - 2][pass];
   const int lane = threadIdx.x & 31;
-  const int64_t M = *B.M;
+  const int LB = B.Bi->LB;
+  int64_t mlo, mhi;
+  dim_range<D>(B, mlo, mhi);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   Tally t;
-  for (int64_t m0 = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); m0 < M; m0 += stride) {
+  for (int64_t m0 = mlo + (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); m0 < mhi;
+       m0 += stride) {
     const int64_t m = m0 + lane;
     unsigned long long open = 0;
-    if (m < M) {
+    if (m < mhi) {
       const int b = B.reps[m];
       if (B.cellcore[b] > 0) {
         const int e = B.reps[m + 1];
-        const CellXYZ<D> cc = decompose<D>(key_at<SPARSE>(B, b), P);
+        const CellCtx cx = cell_ctx<KEY64>(B, b, LB);
+        const DevParams& P = *cx.P;
+        const PredParams Q = pred_params(P);
+        const GridView gv = view_of(B, P);
+        const CellXYZ<D> cc = decompose<D>(cx.local, P);
         float oA[D];
-        if (P.prune) cell_origin32<D>(cc, P, oA);
+        if (Q.prune) cell_origin32<D>(cc, P, oA);
         for (int tt = 0; tt < T.n; ++tt) {
           const int64_t kb = offset_key<D>(cc, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
           if (kb < 0) continue;
@@ -882,7 +1034,7 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
           if (cb.x == cb.y || B.cellcore[cb.x] == 0) continue;
           if (uf_find(B.parent, b) == uf_find(B.parent, cb.x)) continue;
           const int r = inline_link<D, F32>(B, n, b, e, cb.x, cb.y, oA, T.o[tt][0], T.o[tt][1],
-                                            T.o[tt][2], P, t);
+                                            T.o[tt][2], Q, t);
           if (r > 0) uf_union(B.parent, B.cellmin, b, cb.x);
           else if (r < 0) open |= 1ull << tt;
         }
@@ -893,27 +1045,29 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
   flush_tally(t, B.ctr);
 }
 
-template <int D, bool F32, bool SPARSE>
+template <int D, bool F32, bool KEY64>
 __global__ void __launch_bounds__(kScanThreadsPerBlock) k_border_scan(const gdl::Bufs B, int64_t n) {
-  __shared__ DevParams sP;
-  if (threadIdx.x == 0) sP = *B.P;
-  __syncthreads();
-  const DevParams& P = sP;
-  const GridView<SPARSE> gv = view_of<SPARSE>(B);
   const OffTab& T = kFullSt[D - 2];
   const int lane = threadIdx.x & 31;
-  const bool prune = P.prune != 0;
-  const int64_t M = *B.M;
+  const int LB = B.Bi->LB;
+  int64_t mlo, mhi;
+  dim_range<D>(B, mlo, mhi);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   Tally t;
-  for (int64_t m0 = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); m0 < M; m0 += stride) {
+  for (int64_t m0 = mlo + (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); m0 < mhi;
+       m0 += stride) {
     const int64_t m = m0 + lane;
     bool push = false;
-    if (m < M) {
+    if (m < mhi) {
       const int b = B.reps[m], e = B.reps[m + 1];
       const int nnc = (e - b) - B.cellcore[b];
       if (nnc > 0) {
-        const CellXYZ<D> cc = decompose<D>(key_at<SPARSE>(B, b), P);
+        const CellCtx cx = cell_ctx<KEY64>(B, b, LB);
+        const DevParams& P = *cx.P;
+        const PredParams Q = pred_params(P);
+        const GridView gv = view_of(B, P);
+        const bool prune = Q.prune != 0;
+        const CellXYZ<D> cc = decompose<D>(cx.local, P);
         int cores = 0;
         for (int tt = 0; tt < T.n; ++tt) {
           const int64_t kb = offset_key<D>(cc, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
@@ -921,8 +1075,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_border_scan(const gdl:
           const int2 cb = gv.cell((uint64_t)kb);
           if (cb.x < cb.y) cores += B.cellcore[cb.x];
         }
-        if (cores > 0) {
-          // no core point in reach: the non-core points stay NOISE (else below)
+        if (cores > 0) {  // else no core point in reach: the non-core points stay NOISE
           float o[D];
           if (prune) cell_origin32<D>(cc, P, o);
           int budget = kInlineBorderTests;
@@ -931,7 +1084,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_border_scan(const gdl:
             double px[D];
             float pf[D], u[D];
             load_point<D, F32>(px, pf, B, n, i, prune);
-            if (prune) frac_pos<D>(pf, o, P, u);
+            if (prune) frac_pos<D>(pf, o, Q, u);
             int best = INT_MAX;
             for (int tt = 0; tt < T.n && !push; ++tt) {
               const int64_t kb = offset_key<D>(cc, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
@@ -941,7 +1094,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_border_scan(const gdl:
               const int cB = B.cellcid[cb.x];
               if (cB >= best) continue;
               if (prune) {
-                const int cls = classify<D>(u, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
+                const int cls = classify<D>(u, T.o[tt][0], T.o[tt][1], T.o[tt][2], Q);
                 if (cls > 0) {
                   best = cB;  // every point of that cell, a core among them, is in reach
                   continue;
@@ -956,7 +1109,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_border_scan(const gdl:
                 }
                 Cand<D, F32> cd;
                 load_cand<D, F32>(cd, B.X, B.Xf, n, q);
-                if (pair_test<D, F32>(px, pf, cd, B.X, n, q, false, P, t)) {
+                if (pair_test<D, F32>(px, pf, cd, B.X, n, q, false, Q, t)) {
                   best = cB;
                   break;
                 }
@@ -973,36 +1126,37 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_border_scan(const gdl:
 }
 
 // ------------------------------------------------------------- core flags
-// One warp per non-empty cell.  Dense cells are all core.  Otherwise the warp
-// looks up its candidate rows (5 cells along the last axis each, 5 rows in 2D,
-// 25 in 3D; one lane per row), concatenates them, and streams the candidates
-// 32 at a time, one per lane.  Each staged point p of the cell gets
+// Heavy cells, one warp each: dense cells (>= minpts points) are all core;
+// other queued cells stream their candidate rows (5 cells along the last axis
+// each, 5 rows in 2D, 25 in 3D, looked up one per lane and concatenated) 32 at
+// a time, one candidate per lane, and every staged point of the cell gets
 // __ballot_sync + __popc of the lanes holding a neighbour.  The warp stops as
-// soon as every staged p has reached minpts (own row first, so dense
-// neighbourhoods stop after one tile).
-template <int D, bool F32, bool SPARSE>
+// soon as every staged point has reached minpts (own row first).
+template <int D, bool F32, bool KEY64>
 __global__ void __launch_bounds__(kCellThreads) k_core_heavy(const gdl::Bufs B, int64_t n) {
-  __shared__ DevParams sP;
   __shared__ WarpStage<D> stage[kWarpsPerBlock];
   __shared__ RowList rows[kWarpsPerBlock];
-  if (threadIdx.x == 0) sP = *B.P;
-  __syncthreads();
-  const DevParams& P = sP;
-  const GridView<SPARSE> gv = view_of<SPARSE>(B);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   WarpStage<D>& S = stage[w];
   RowList& RL = rows[w];
   const int nrows = kRows[D - 2].n;
   const double* __restrict__ X = B.X;
   const float* __restrict__ Xf = B.Xf;
-    const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
+  const int LB = B.Bi->LB;
+  int64_t mlo, mhi;
+  dim_range<D>(B, mlo, mhi);
+  const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
   Tally t;
   unsigned long long dense = 0;
   const int64_t H = (int64_t)B.ctr[kCtrHeavyCore];
   for (int64_t h = (int64_t)blockIdx.x * kWarpsPerBlock + w; h < H; h += W) {
     const int64_t m = B.hv_cell[h];
+    if (m < mlo || m >= mhi) continue;
     const int b = B.reps[m], e = B.reps[m + 1], sz = e - b;
-    if (sz >= P.minpts) {
+    const CellCtx cx = cell_ctx<KEY64>(B, b, LB);
+    const DevParams& P = *cx.P;
+    const PredParams Q = pred_params(P);
+    if (sz >= Q.minpts) {
       int mn = INT_MAX;
       for (int i = b + lane; i < e; i += 32) {
         B.core[i] = 1;
@@ -1012,8 +1166,9 @@ __global__ void __launch_bounds__(kCellThreads) k_core_heavy(const gdl::Bufs B, 
       if (lane == 0) { B.cellcore[b] = sz; B.cellmin[b] = mn; ++dense; }
       continue;
     }
-    const CellXYZ<D> cc = decompose<D>(key_at<SPARSE>(B, b), P);
-    const int total = build_rows<D, SPARSE>(RL, gv, cc, P, lane);
+    const GridView gv = view_of(B, P);
+    const CellXYZ<D> cc = decompose<D>(cx.local, P);
+    const int total = build_rows<D>(RL, gv, cc, P, lane);
     int ncore = 0, mn = INT_MAX;
     for (int c0 = 0; c0 < sz; c0 += 32) {
       const int na = min(32, sz - c0);
@@ -1037,13 +1192,13 @@ __global__ void __launch_bounds__(kCellThreads) k_core_heavy(const gdl::Bufs B, 
           load_cand<D, F32>(cd, X, Xf, n, q);
         }
         for (int j = 0; j < na; ++j) {
-          bool hit = valid && pair_test<D, F32>(S.x[j], S.f[j], cd, X, n, q, true, P, t);
+          bool hit = valid && pair_test<D, F32>(S.x[j], S.f[j], cd, X, n, q, true, Q, t);
           unsigned bal = __ballot_sync(kFull, hit);
           if (lane == j) mycnt += __popc(bal);
         }
-        done = __all_sync(kFull, lane >= na || mycnt >= P.minpts);
+        done = __all_sync(kFull, lane >= na || mycnt >= Q.minpts);
       }
-      const bool isc = lane < na && mycnt >= P.minpts;
+      const bool isc = lane < na && mycnt >= Q.minpts;
       if (lane < na) B.core[b + c0 + lane] = isc ? 1 : 0;
       if (isc) mn = min(mn, (int)B.ids[b + c0 + lane]);
       ncore += __popc(__ballot_sync(kFull, isc));
@@ -1066,33 +1221,34 @@ __global__ void k_parent_init(const gdl::Bufs B) {
   }
 }
 
-// One warp per cell A with core points.  Lanes look up the half-stencil
-// neighbour cells of this pass in parallel (pass 0: offsets within +-1, pass 1:
-// the rest -- running the near pass first lets most far pairs be skipped
-// because their cells are already in one component).  For each neighbour B
-// with core points in another component, the warp looks for one core-core pair
-// that are neighbours both ways (lanes over B's points, A's core points
-// broadcast) and unites the two cells.
-template <int D, bool F32, bool SPARSE>
+// Heavy link searches, one warp per queued cell A: for each still-open
+// half-stencil neighbour B (pass 0: offsets within +-1, pass 1: the rest) whose
+// core points are in another component, look for one core-core pair that are
+// neighbours both ways (lanes over B's points, A's core points broadcast) and
+// unite the two cells.
+template <int D, bool F32, bool KEY64>
 __global__ void __launch_bounds__(kCellThreads) k_union_heavy(const gdl::Bufs B, int64_t n, int pass) {
-  __shared__ DevParams sP;
-  if (threadIdx.x == 0) sP = *B.P;
-  __syncthreads();
-  const DevParams& P = sP;
-  const GridView<SPARSE> gv = view_of<SPARSE>(B);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const double* __restrict__ X = B.X;
   const float* __restrict__ Xf = B.Xf;
-    const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
+  const int LB = B.Bi->LB;
+  int64_t mlo, mhi;
+  dim_range<D>(B, mlo, mhi);
+  const int64_t W = (int64_t)gridDim.x * kWarpsPerBlock;
   const OffTab& T = kHalf[D - 2][pass];
   Tally t;
   const int64_t H = (int64_t)B.ctr[kCtrHeavyUnion];
   for (int64_t h = (int64_t)blockIdx.x * kWarpsPerBlock + w; h < H; h += W) {
     const int64_t m = B.hv_cell[h];
+    if (m < mlo || m >= mhi) continue;
     const unsigned long long open = B.hv_mask[h];
     const int b = B.reps[m];
     const int e = B.reps[m + 1];
-    const CellXYZ<D> cc = decompose<D>(key_at<SPARSE>(B, b), P);
+    const CellCtx cx = cell_ctx<KEY64>(B, b, LB);
+    const DevParams& P = *cx.P;
+    const PredParams Q = pred_params(P);
+    const GridView gv = view_of(B, P);
+    const CellXYZ<D> cc = decompose<D>(cx.local, P);
     for (int t0 = 0; t0 < T.n; t0 += 32) {
       const int tt = t0 + lane;
       bool cand = false;
@@ -1128,7 +1284,7 @@ __global__ void __launch_bounds__(kCellThreads) k_union_heavy(const gdl::Bufs B,
               ax[k] = X[k * n + a];
               if (F32) af[k] = Xf[k * n + a];
             }
-            bool hit = valid && link_test<D, F32>(ax, af, c, X, n, a, q, P, t, B.asym, B.ctr);
+            bool hit = valid && link_test<D, F32>(ax, af, c, X, n, a, q, Q, t, B.asym, B.ctr);
             found = __any_sync(kFull, hit);
           }
         }
@@ -1238,14 +1394,21 @@ __global__ void k_roots(const gdl::Bufs B) {
 }
 
 // Cluster id of every cell with core points (ordered by smallest core index:
-// Fmark now holds the exclusive scan of the root marks over original indices),
+// Fmark now holds the exclusive scan of the root marks over global indices),
 // and the provisional label of every point: its cluster if core, NOISE otherwise.
+// Cluster numbers restart at 0 in every instance: the scan value at the
+// instance's first point counts the clusters of the instances before it.
+template <bool KEY64>
 __global__ void k_label(const gdl::Bufs B, int64_t n) {
+  const int LB = B.Bi->LB;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const int b = rep_of(B, i);
     int cl = INT_MAX;
-    if (B.cellcore[b] > 0) cl = (int)B.Fmark[B.cellmin[uf_find(B.parent, b)]];
+    if (B.cellcore[b] > 0) {
+      const int64_t pt_off = B.Pv[(int)(key_at<KEY64>(B, i) >> LB)].pt_off;
+      cl = (int)(B.Fmark[B.cellmin[uf_find(B.parent, b)]] - B.Fmark[pt_off]);
+    }
     if (i == b) B.cellcid[b] = cl;
     B.lab[i] = B.core[i] ? cl : kNoise;
   }
@@ -1257,15 +1420,13 @@ __global__ void k_label(const gdl::Bufs B, int64_t n) {
 // point, as the reference's expansion queries from the core point).  Lanes look
 // the stencil cells up in parallel; cells whose cluster id cannot improve any
 // staged point are skipped.
-template <int D, bool F32, bool SPARSE>
+template <int D, bool F32, bool KEY64>
 __global__ void __launch_bounds__(kCellThreads) k_border_heavy(const gdl::Bufs B, int64_t n) {
-  __shared__ DevParams sP;
   __shared__ WarpStage<D> stage[kWarpsPerBlock];
   __shared__ int sIdx[kWarpsPerBlock][32];
-  if (threadIdx.x == 0) sP = *B.P;
-  __syncthreads();
-  const DevParams& P = sP;
-  const GridView<SPARSE> gv = view_of<SPARSE>(B);
+  const int LB = B.Bi->LB;
+  int64_t mlo, mhi;
+  dim_range<D>(B, mlo, mhi);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   WarpStage<D>& S = stage[w];
   const double* __restrict__ X = B.X;
@@ -1276,8 +1437,13 @@ __global__ void __launch_bounds__(kCellThreads) k_border_heavy(const gdl::Bufs B
   const int64_t H = (int64_t)B.ctr[kCtrHeavyBorder];
   for (int64_t h = (int64_t)blockIdx.x * kWarpsPerBlock + w; h < H; h += W) {
     const int64_t m = B.hv_cell[h];
+    if (m < mlo || m >= mhi) continue;
     const int b = B.reps[m], e = B.reps[m + 1];
-    const CellXYZ<D> cc = decompose<D>(key_at<SPARSE>(B, b), P);
+    const CellCtx cx = cell_ctx<KEY64>(B, b, LB);
+    const DevParams& P = *cx.P;
+    const PredParams Q = pred_params(P);
+    const GridView gv = view_of(B, P);
+    const CellXYZ<D> cc = decompose<D>(cx.local, P);
     for (int c0 = b; c0 < e; c0 += 32) {
       // stage this chunk's non-core points
       const int i = c0 + lane;
@@ -1329,7 +1495,7 @@ __global__ void __launch_bounds__(kCellThreads) k_border_heavy(const gdl::Bufs B
             while (pending) {
               const int j = __ffs(pending) - 1;
               pending &= pending - 1;
-              bool hit = valid && pair_test<D, F32>(S.x[j], S.f[j], c, X, n, q, false, P, t);
+              bool hit = valid && pair_test<D, F32>(S.x[j], S.f[j], c, X, n, q, false, Q, t);
               if (__any_sync(kFull, hit)) {
                 if (lane == j) best = cB;
                 wantm &= ~(1u << j);
@@ -1370,8 +1536,16 @@ __global__ void k_scatter_labels(const gdl::Bufs B, int64_t n, int* __restrict__
   }
 }
 
-}  // namespace gd
+// clusters of every instance from the global cluster-number scan (Fmark has
+// n+1 entries, the last one the total)
+__global__ void k_cluster_counts(const gdl::Bufs B, int K, int64_t* out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x) {
+    const InstDesc I = B.inst[i];
+    out[i] = (int64_t)B.Fmark[I.pt_off + I.n] - (int64_t)B.Fmark[I.pt_off];
+  }
+}
 
+}  // namespace gd
 // ------------------------------------------------------------------ launchers
 namespace gdl {
 
@@ -1385,132 +1559,91 @@ static int grid_for(int64_t work, int threads, int sms, int per_sm) {
   return (int)g;
 }
 
-void bbox(const double* pts, int64_t n, int dim, double* partial, int nblocks, int* flags,
-          cudaStream_t s) {
-  long long* part = reinterpret_cast<long long*>(partial);
-  if (dim == 2) k_bbox_partial<2><<<nblocks, kBboxThreads, 0, s>>>(pts, n, part, flags);
-  else k_bbox_partial<3><<<nblocks, kBboxThreads, 0, s>>>(pts, n, part, flags);
+void grids(const Bufs& B, int K, int nchunks, double mult2, double mult3, uint64_t dense_floor,
+           uint64_t dense_per_point, cudaStream_t s) {
+  k_bbox_init<<<(K + 255) / 256, 256, 0, s>>>(B, K);
+  if (nchunks > 0) k_bbox_chunk<<<nchunks, kBboxThreads, 0, s>>>(B);
+  k_params_inst<<<(K + 127) / 128, 128, 0, s>>>(B, K, mult2, mult3, dense_floor, dense_per_point);
+  k_layout<<<1, 1024, 0, s>>>(B, K);
 }
 
-void params(const double* partial, int nblocks, int dim, DevParams* P, double eps, int minpts,
-            double cell_mult, uint64_t max_cells, const int* flags, cudaStream_t s) {
-  const long long* part = reinterpret_cast<const long long*>(partial);
-  if (dim == 2)
-    k_params<2><<<1, 256, 0, s>>>(part, nblocks, P, eps, minpts, cell_mult, max_cells, flags);
+void keys(const Bufs& B, bool key64, int nchunks, void* keys_out, cudaStream_t s) {
+  if (nchunks <= 0) return;
+  if (key64)
+    k_keys<unsigned long long><<<nchunks, 256, 0, s>>>(B, static_cast<unsigned long long*>(keys_out));
   else
-    k_params<3><<<1, 256, 0, s>>>(part, nblocks, P, eps, minpts, cell_mult, max_cells, flags);
+    k_keys<uint32_t><<<nchunks, 256, 0, s>>>(B, static_cast<uint32_t*>(keys_out));
 }
 
-void keys(const double* pts, int64_t n, int dim, bool sparse, const DevParams* P, void* keys,
-          int sms, cudaStream_t s) {
-  int g = grid_for(n, 256, sms, 8);
+void gather(const Bufs& B, bool key64, int64_t n, bool xf, int sms, cudaStream_t s) {
+  const int g = grid_for(n, 256, sms, 8);
   using U64 = unsigned long long;
-  if (dim == 2) {
-    if (sparse) k_keys<2, U64><<<g, 256, 0, s>>>(pts, n, P, static_cast<U64*>(keys));
-    else k_keys<2, uint32_t><<<g, 256, 0, s>>>(pts, n, P, static_cast<uint32_t*>(keys));
+  if (key64) {
+    if (xf) k_gather<U64, true><<<g, 256, 0, s>>>(B, n);
+    else k_gather<U64, false><<<g, 256, 0, s>>>(B, n);
   } else {
-    if (sparse) k_keys<3, U64><<<g, 256, 0, s>>>(pts, n, P, static_cast<U64*>(keys));
-    else k_keys<3, uint32_t><<<g, 256, 0, s>>>(pts, n, P, static_cast<uint32_t*>(keys));
+    if (xf) k_gather<uint32_t, true><<<g, 256, 0, s>>>(B, n);
+    else k_gather<uint32_t, false><<<g, 256, 0, s>>>(B, n);
   }
 }
 
-void gather(const double* pts, const uint32_t* ids, int64_t n, int dim, bool f32,
-            const DevParams* P, double* X, float* Xf, int sms, cudaStream_t s) {
-  int g = grid_for(n, 256, sms, 8);
-  if (dim == 2) {
-    if (f32) k_gather<2, true><<<g, 256, 0, s>>>(pts, ids, n, P, X, Xf);
-    else k_gather<2, false><<<g, 256, 0, s>>>(pts, ids, n, P, X, Xf);
-  } else {
-    if (f32) k_gather<3, true><<<g, 256, 0, s>>>(pts, ids, n, P, X, Xf);
-    else k_gather<3, false><<<g, 256, 0, s>>>(pts, ids, n, P, X, Xf);
-  }
-}
-
-void run_flags(const void* keys, bool sparse, int64_t n, uint32_t* fl, int sms, cudaStream_t s) {
-  int g = grid_for(n, 256, sms, 8);
-  if (sparse)
-    k_run_flags<unsigned long long><<<g, 256, 0, s>>>(
-        static_cast<const unsigned long long*>(keys), n, fl);
+void run_flags(const void* keys, bool key64, int64_t n, uint32_t* fl, int sms, cudaStream_t s) {
+  const int g = grid_for(n, 256, sms, 8);
+  if (key64)
+    k_run_flags<unsigned long long><<<g, 256, 0, s>>>(static_cast<const unsigned long long*>(keys),
+                                                      n, fl);
   else
     k_run_flags<uint32_t><<<g, 256, 0, s>>>(static_cast<const uint32_t*>(keys), n, fl);
 }
 
-void run_scatter(const uint32_t* fl, const uint32_t* pos, int64_t n, int* reps,
-                 const uint32_t* Mdev, unsigned long long* ctr, int sms, cudaStream_t s) {
-  k_run_scatter<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(fl, pos, n, reps, Mdev, ctr);
+void run_scatter(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) {
+  k_run_scatter<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
+  if (key64) k_split<unsigned long long><<<1, 32, 0, s>>>(B);
+  else k_split<uint32_t><<<1, 32, 0, s>>>(B);
 }
 
-void cell_counts(const uint32_t* keys, const int* reps, const uint32_t* Mdev, int64_t n,
-                 uint32_t* table, int sms, cudaStream_t s) {
-  k_cell_counts<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(keys, reps, Mdev, table);
+void cell_counts(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) {
+  if (key64) k_cell_counts<unsigned long long><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
+  else k_cell_counts<uint32_t><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
 }
 
-void hash_insert(const unsigned long long* keys, const int* reps, const uint32_t* Mdev, int64_t n,
-                 unsigned long long* hkeys, uint32_t* hvals, uint32_t mask, int sms,
-                 cudaStream_t s) {
-  k_hash_insert<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(keys, reps, Mdev, hkeys, hvals, mask);
+void hash_insert(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) {
+  if (key64) k_hash_insert<unsigned long long><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
+  else k_hash_insert<uint32_t><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
 }
 
-#define GD_DISPATCH(dim, f32, sparse, KERNEL, GRID, ...)                                    \
-  do {                                                                                      \
-    if (dim == 2) {                                                                         \
-      if (f32) {                                                                            \
-        if (sparse) KERNEL<2, true, true><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);       \
-        else KERNEL<2, true, false><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);             \
-      } else {                                                                              \
-        if (sparse) KERNEL<2, false, true><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);      \
-        else KERNEL<2, false, false><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);            \
-      }                                                                                     \
-    } else {                                                                                \
-      if (f32) {                                                                            \
-        if (sparse) KERNEL<3, true, true><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);       \
-        else KERNEL<3, true, false><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);             \
-      } else {                                                                              \
-        if (sparse) KERNEL<3, false, true><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);      \
-        else KERNEL<3, false, false><<<GRID, kCellThreads, 0, s>>>(__VA_ARGS__);            \
-      }                                                                                     \
-    }                                                                                       \
+#define GD_L1(D, f32, key64, KERNEL, GRID, THREADS, ...)                          \
+  do {                                                                            \
+    if (f32) {                                                                    \
+      if (key64) KERNEL<D, true, true><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);     \
+      else KERNEL<D, true, false><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);          \
+    } else {                                                                      \
+      if (key64) KERNEL<D, false, true><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);    \
+      else KERNEL<D, false, false><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);         \
+    }                                                                             \
   } while (0)
 
-#define GD_DISPATCH_T(dim, f32, sparse, KERNEL, GRID, THREADS, ...)                         \
-  do {                                                                                      \
-    if (dim == 2) {                                                                         \
-      if (f32) {                                                                            \
-        if (sparse) KERNEL<2, true, true><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);            \
-        else KERNEL<2, true, false><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);                  \
-      } else {                                                                              \
-        if (sparse) KERNEL<2, false, true><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);           \
-        else KERNEL<2, false, false><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);                 \
-      }                                                                                     \
-    } else {                                                                                \
-      if (f32) {                                                                            \
-        if (sparse) KERNEL<3, true, true><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);            \
-        else KERNEL<3, true, false><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);                  \
-      } else {                                                                              \
-        if (sparse) KERNEL<3, false, true><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);           \
-        else KERNEL<3, false, false><<<GRID, THREADS, 0, s>>>(__VA_ARGS__);                 \
-      }                                                                                     \
-    }                                                                                       \
+// one launch per dimension present (bit 0: 2D instances, bit 1: 3D instances)
+#define GD_LAUNCH_DIMS(dims, f32, key64, KERNEL, GRID, THREADS, ...)              \
+  do {                                                                            \
+    if ((dims) & 1) GD_L1(2, f32, key64, KERNEL, GRID, THREADS, __VA_ARGS__);     \
+    if ((dims) & 2) GD_L1(3, f32, key64, KERNEL, GRID, THREADS, __VA_ARGS__);     \
   } while (0)
 
-static int scan_grid(int64_t n, int sms) {
-  return grid_for(n, kScanThreadsPerBlock, sms, 8);
-}
+int launches_per_cell_phase(int dims) { return ((dims & 1) ? 1 : 0) + ((dims & 2) ? 1 : 0); }
 
-void core(const Bufs& B, int64_t n, int dim, bool f32, bool sparse, int sms, cudaStream_t s) {
+void core(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s) {
   cudaMemsetAsync(B.ctr + kCtrHeavyCore, 0, 8, s);
-  GD_DISPATCH_T(dim, f32, sparse, k_core_scan, scan_grid(n, sms), kScanThreadsPerBlock, B, n);
-  GD_DISPATCH(dim, f32, sparse, k_core_heavy, sms * 8, B, n);
+  GD_LAUNCH_DIMS(dims, f32, key64, k_core_scan, sms * 8, kScanThreadsPerBlock, B, n);
+  GD_LAUNCH_DIMS(dims, f32, key64, k_core_heavy, sms * 8, kCellThreads, B, n);
 }
 
-void unite(const Bufs& B, int64_t n, int dim, bool f32, bool sparse, int sms, cudaStream_t s) {
+void unite(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s) {
   k_parent_init<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
-  int g = sms * 8;
   for (int pass = 0; pass < 2; ++pass) {
     cudaMemsetAsync(B.ctr + kCtrHeavyUnion, 0, 8, s);
-    GD_DISPATCH_T(dim, f32, sparse, k_union_scan, scan_grid(n, sms), kScanThreadsPerBlock, B, n,
-                  pass);
-    GD_DISPATCH(dim, f32, sparse, k_union_heavy, g, B, n, pass);
+    GD_LAUNCH_DIMS(dims, f32, key64, k_union_scan, sms * 8, kScanThreadsPerBlock, B, n, pass);
+    GD_LAUNCH_DIMS(dims, f32, key64, k_union_heavy, sms * 8, kCellThreads, B, n, pass);
   }
   k_compress<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
   k_asym_resolve<<<1, 32, 0, s>>>(B);
@@ -1520,19 +1653,24 @@ void roots(const Bufs& B, int64_t n, int sms, cudaStream_t s) {
   k_roots<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
 }
 
-void label(const Bufs& B, int64_t n, int sms, cudaStream_t s) {
-  k_label<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
+void label(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) {
+  if (key64) k_label<true><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
+  else k_label<false><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
 }
 
-void border(const Bufs& B, int64_t n, int dim, bool f32, bool sparse, int sms, cudaStream_t s) {
+void border(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s) {
   cudaMemsetAsync(B.ctr + kCtrHeavyBorder, 0, 8, s);
-  GD_DISPATCH_T(dim, f32, sparse, k_border_scan, scan_grid(n, sms), kScanThreadsPerBlock, B, n);
-  GD_DISPATCH(dim, f32, sparse, k_border_heavy, sms * 8, B, n);
+  GD_LAUNCH_DIMS(dims, f32, key64, k_border_scan, sms * 8, kScanThreadsPerBlock, B, n);
+  GD_LAUNCH_DIMS(dims, f32, key64, k_border_heavy, sms * 8, kCellThreads, B, n);
 }
 
 void scatter_labels(const Bufs& B, int64_t n, int* out, uint8_t* core_out, int sms,
                     cudaStream_t s) {
   k_scatter_labels<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n, out, core_out);
+}
+
+void cluster_counts(const Bufs& B, int K, int64_t* out, cudaStream_t s) {
+  k_cluster_counts<<<(K + 255) / 256, 256, 0, s>>>(B, K, out);
 }
 
 }  // namespace gdl

@@ -105,6 +105,9 @@ gd_status gd_ctx_set_precision(gd_ctx* ctx, int32_t precision);
    a cell's points are mutual neighbours, and larger than eps/2 so neighbours
    stay within +-2 cells. */
 gd_status gd_ctx_set_cell_mult(gd_ctx* ctx, double mult);
+/* Separate multipliers for 2D (range (0.5, 1/sqrt(2))) and 3D instances
+   (range (0.5, 1/sqrt(3))); 0 restores the default.  Set by the autotuner. */
+gd_status gd_ctx_set_cell_mults(gd_ctx* ctx, double mult2d, double mult3d);
 /* Frees the context's cached device buffers (they regrow on the next call). */
 gd_status gd_ctx_trim(gd_ctx* ctx);
 
@@ -137,6 +140,27 @@ gd_status gd_dbscan(gd_ctx* ctx, const gd_points* pts, double eps, int32_t minpt
 
 /* Statistics of the last gd_expand / gd_dbscan on this context. */
 gd_status gd_get_stats(gd_ctx* ctx, gd_stats* stats);
+
+/* ---- many independent instances in one run ------------------------------ */
+typedef struct gd_instance {
+  int64_t n;        /* points of this instance */
+  int32_t dim;      /* 2 or 3 */
+  int32_t minpts;
+  double eps;
+} gd_instance;
+
+/* No counterpart in the reference (which clusters one data set per program
+   run, main.cu:35-459).  Clusters `count` independent instances, each with its
+   own eps, minpts and dimension, in one pass of the pipeline: one sort, one
+   cell list and one launch per phase for all of them.  coords holds the
+   instances back to back, each row-major [n][dim], in the given order (host or
+   device memory per on_device); labels receives one label per point in the same
+   order, cluster ids restarting at 0 in every instance (NOISE = -2).
+   cluster_counts (host, count entries) and stats may be NULL.  Every
+   instance's labels equal those of gd_dbscan on that instance alone. */
+gd_status gd_batch_dbscan(gd_ctx* ctx, int32_t count, const gd_instance* inst,
+                          const double* coords, int32_t on_device, int32_t* labels,
+                          int64_t* cluster_counts, gd_stats* stats);
 
 /* ---- exact DBSCAN without any memory allocation ------------------------ */
 /* No counterpart in the reference.  For callers that may not allocate device
