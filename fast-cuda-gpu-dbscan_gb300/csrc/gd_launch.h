@@ -59,7 +59,7 @@ void gather(const Bufs& B, bool key64, int64_t n, bool xf, int sms, cudaStream_t
 void run_flags(const void* keys, bool key64, int64_t n, uint32_t* fl, int sms, cudaStream_t s);
 // cell starts (reps), cell count, and the split between 2D and 3D cells
 void run_scatter(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
-// dense instances: cell counts into their table slices (scan them afterwards)
+// cell counts into the instances' table slices (scan them afterwards)
 void cell_counts(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
 // sparse instances: hash of occupied cells (clear the slots first)
 void hash_insert(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);

@@ -203,8 +203,8 @@ __global__ void k_params_inst(const gdl::Bufs B, int K, double mult2, double mul
   B.Pv[i] = p;
 }
 
-// One block: the run layout -- key widths, dense-table offsets (exclusive scan
-// over the dense instances' C+1 entries), flags.
+// One block: the run layout -- key widths, cell-table offsets (exclusive scan
+// over every instance's table length), flags.
 __global__ void __launch_bounds__(1024) k_layout(const gdl::Bufs B, int K) {
   __shared__ unsigned long long s_part[32];
   __shared__ int s_red[4][32];
@@ -263,7 +263,9 @@ __global__ void __launch_bounds__(1024) k_layout(const gdl::Bufs B, int K) {
   for (int base = 0; base < K; base += 1024) {
     const int i = base + threadIdx.x;
     unsigned long long v = 0;
-    if (i < K && !B.Pv[i].sparse && B.Pv[i].n > 0) v = B.Pv[i].C + 1;
+    // a dense instance's table has C+1 entries; a sparse instance keeps one
+    // entry holding its point count, so the scan stays in sorted-position units
+    if (i < K) v = B.Pv[i].sparse ? 1 : B.Pv[i].C + 1;
     unsigned long long inc = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -381,11 +383,15 @@ __global__ void k_split(const gdl::Bufs B) {
   B.ctr[kCtrCells2D] = (unsigned long long)lo;
 }
 
-// dense instances: counts into the instance's table slice (scanned afterwards)
+// Cell counts into the instances' table slices (scanned afterwards into start
+// positions).  A sparse instance's one-entry slice holds its point count.
 template <class Key>
 __global__ void k_cell_counts(const gdl::Bufs B) {
   const Key* keys = static_cast<const Key*>(B.keys);
   const int LB = B.Bi->LB;
+  const int K = B.Bi->K;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x)
+    if (B.Pv[i].sparse) B.start[B.Pv[i].table_off] = (uint32_t)B.Pv[i].n;
   const int64_t M = *B.M;
   for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
        m += (int64_t)gridDim.x * blockDim.x) {
