@@ -219,7 +219,10 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
     return fail(GD_ERANGE, "eps-cell grid too large (extent/eps beyond 2^31 cells per axis, or "
                            "cell keys and instance ids beyond 62 bits)");
   ctx->key64 = bi.key64 != 0;
-  ctx->f32 = ctx->precision == GD_PREC_FP32_BAND;
+  // float32 filter when asked for; a single instance without a valid band
+  // runs the float64 kernels (a batch keeps the filter: such instances send
+  // every pair to the float64 predicate)
+  ctx->f32 = ctx->precision == GD_PREC_FP32_BAND && !(K == 1 && bi.band_off);
   ctx->xf = ctx->f32 || bi.any_xf;
   ctx->dims = (bi.K2 > 0 ? 1 : 0) | (bi.K2 < K ? 2 : 0);
   const size_t kw = ctx->key64 ? 8 : 4;

@@ -57,7 +57,8 @@ struct BatchInfo {
   int32_t any_xf;      // some instance wants the centred float32 copy
   int32_t max_dim;
   int32_t K2;          // instances [0, K2) are 2D, [K2, K) 3D
-  int32_t pad;
+  int32_t band_off;    // some instance has no valid float32 band (all its pairs
+                       // take the float64 predicate)
 };
 
 // Grid and predicate parameters of one instance, computed on the device from

@@ -188,7 +188,7 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
     return fail(GD_EINVAL, "gd_dbscan_noalloc: input has NaN or Inf coordinates");
   if (bi.flags & gd::kFlagGridTooLarge)
     return fail(GD_ERANGE, "gd_dbscan_noalloc: eps-cell grid too large");
-  const bool f32 = precision == GD_PREC_FP32_BAND;
+  const bool f32 = precision == GD_PREC_FP32_BAND && !bi.band_off;
   const bool key64 = bi.key64 != 0;
   const bool xf = f32 || bi.any_xf;
   const int dims = dim == 2 ? 1 : 2;

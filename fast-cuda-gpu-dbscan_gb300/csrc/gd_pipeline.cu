@@ -217,6 +217,7 @@ __global__ void __launch_bounds__(1024) k_layout(const gdl::Bufs B, int K) {
     fl |= p.flags;
     sp |= p.sparse;
     xf |= p.prune;
+    if (p.n > 0 && !(p.eps2_lo32 > 0.0f)) xf |= 2;
     md = max(md, p.dim);
     k2 += p.dim == 2;
   }
@@ -229,7 +230,12 @@ __global__ void __launch_bounds__(1024) k_layout(const gdl::Bufs B, int K) {
     md = max(md, __shfl_xor_sync(kFull, md, o));
     k2 += __shfl_xor_sync(kFull, k2, o);
   }
-  if (lane == 0) { s_red[0][w] = lb; s_red[1][w] = fl | (sp << 16) | (xf << 17); s_red[2][w] = md; s_red[3][w] = k2; }
+  if (lane == 0) {
+    s_red[0][w] = lb;
+    s_red[1][w] = fl | (sp << 16) | (xf << 17);
+    s_red[2][w] = md;
+    s_red[3][w] = k2;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     int LB = 0, F = 0, MD = 2, K2 = 0;
@@ -251,7 +257,7 @@ __global__ void __launch_bounds__(1024) k_layout(const gdl::Bufs B, int K) {
     bi.flags = (F & 0xffff) | B.Bi->flags | (LB + IB > 62 ? kFlagGridTooLarge : 0);
     bi.max_dim = MD;
     bi.K2 = K2;
-    bi.pad = 0;
+    bi.band_off = (F >> 18) & 1;
     bi.table_total = 0;
     *B.Bi = bi;
     s_carry = 0;
