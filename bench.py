@@ -181,6 +181,138 @@ def run_reference(args, rank):
     }
 
 
+def run_batch(args, rank, world, local, dist):
+    """Batched workload: many independent instances (own eps, minpts, dim) in one
+    gd_batch_dbscan run, against the single-instance path called once per
+    instance on the same device-resident data (labels must agree)."""
+    import ctypes
+
+    import torch
+    gdm = importlib.import_module(PKG)
+    api = importlib.import_module(PKG + ".api")
+    ds = importlib.import_module(PKG + ".datasets")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    t0 = time.perf_counter()
+    insts = ds.batch4096(seed=0, count=args.instances, workers=min(16, os.cpu_count() or 1))
+    gen_s = time.perf_counter() - t0
+    K = len(insts)
+    desc = (api.GdInstance * K)()
+    for i, inst in enumerate(insts):
+        desc[i].n, desc[i].dim, desc[i].minpts, desc[i].eps = inst.n, inst.dim, inst.minpts, inst.eps
+    flat = np.concatenate([inst.points.reshape(-1) for inst in insts])
+    ntot = int(sum(inst.n for inst in insts))
+    prec = gdm.GD_PREC_FP64 if args.precision == "fp64" else gdm.GD_PREC_FP32_BAND
+    stream = torch.cuda.current_stream(dev)
+    ctx = gdm.Context(local, precision=prec)
+    ctx.set_stream(stream.cuda_stream)
+    d_flat = torch.from_numpy(flat).to(dev)
+    d_lab = torch.empty(ntot, dtype=torch.int32, device=dev)
+    kc = np.zeros(K, dtype=np.int64)
+    st = api.GdStats()
+
+    def step_batch():
+        api._check(ctx._lib.gd_batch_dbscan(ctx._ctx, K, desc, d_flat.data_ptr(), 1,
+                                            d_lab.data_ptr(), kc.ctypes.data, ctypes.byref(st)))
+
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.int32, device=dev)
+    for _ in range(args.warmup):
+        step_batch()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms = []
+        for _ in range(args.steps):
+            flush.fill_(1)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            step_batch()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+    t_batch = sum(ms) / len(ms)
+    batch_labels = d_lab.cpu().numpy()
+    # the single-instance path once per instance, same device-resident data
+    offs = np.cumsum([0] + [inst.n * inst.dim for inst in insts])
+    poffs = np.cumsum([0] + [inst.n for inst in insts])
+    loop_lab = torch.empty(ntot, dtype=torch.int32, device=dev)
+    gp = api.GdPoints()
+
+    def step_loop():
+        for i, inst in enumerate(insts):
+            gp.coords = d_flat.data_ptr() + int(offs[i]) * 8
+            gp.n, gp.dim, gp.on_device = inst.n, inst.dim, 1
+            api._check(ctx._lib.gd_dbscan(ctx._ctx, ctypes.byref(gp), inst.eps, inst.minpts,
+                                          loop_lab.data_ptr() + int(poffs[i]) * 4, None))
+
+    step_loop()
+    torch.cuda.synchronize()
+    loops = []
+    for _ in range(max(1, min(3, args.steps))):
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        step_loop()
+        torch.cuda.synchronize()
+        loops.append(time.perf_counter() - a)
+    t_loop = sum(loops) / len(loops)
+    same = bool(np.array_equal(loop_lab.cpu().numpy(), batch_labels))
+    # end to end with pinned host buffers
+    h_flat = torch.from_numpy(flat).pin_memory().numpy()
+    h_lab = torch.empty(ntot, dtype=torch.int32).pin_memory().numpy()
+
+    def step_e2e():
+        api._check(ctx._lib.gd_batch_dbscan(ctx._ctx, K, desc, h_flat.ctypes.data, 0,
+                                            h_lab.ctypes.data, kc.ctypes.data, ctypes.byref(st)))
+
+    step_e2e()
+    e2e = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        step_e2e()
+        e2e.append(time.perf_counter() - a)
+    t_e2e = sum(e2e) / len(e2e)
+    same_e2e = bool(np.array_equal(h_lab, batch_labels))
+    peak, peak_kind = peaks()
+    algo = int(sum(inst.n * (8 * inst.dim + 4) for inst in insts))
+    achieved = algo / (t_batch / 1e3) / 1e9
+    value = world * ntot / (t_batch / 1e3)
+    line = {
+        "metric": METRIC + " (batched instances)", "value": value, "unit": "points/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_batch,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == gdm.GD_PREC_FP64 else "f32+f64band", "data": "synthetic",
+        "config": {"workload": "batch4096", "instances": K, "points": ntot,
+                   "dims": {"2": int(sum(i.dim == 2 for i in insts)),
+                            "3": int(sum(i.dim == 3 for i in insts))},
+                   "precision": args.precision, "parallelism": f"replicas{world}",
+                   "generation_s": round(gen_s, 1),
+                   "l2": "512 MiB flush write between timed steps"},
+        "e2e": {"value": world * ntot / t_e2e, "unit": "points/s",
+                "h2d_bytes_per_step": int(flat.nbytes), "d2h_bytes_per_step": ntot * 4,
+                "ms_per_step": t_e2e * 1e3, "labels_equal_device_run": same_e2e},
+        "looped_single_instance": {"value": ntot / t_loop, "ms_per_batch": t_loop * 1e3,
+                                   "speedup_batched": t_loop * 1e3 / t_batch,
+                                   "labels_identical": same},
+        "gpu_launches": int(st.launches) * args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "kernel": "whole batched pipeline (one step)", "algorithmic_bytes": algo},
+        "clocks": clk.summary(),
+        "phases_ms": {k: getattr(st, k) for k in ("ms_index", "ms_core", "ms_union", "ms_label",
+                                                  "ms_total")},
+        "counts": {k: getattr(st, k) for k in ("n_clusters", "n_noise", "n_core", "n_cells",
+                                               "tests_fp64", "tests_fp32", "band_retests")},
+    }
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -188,7 +320,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="zipf2d_10m",
-                    choices=["zipf2d_10m", "aniso3d_20m", "blobs2d_100k"])
+                    choices=["zipf2d_10m", "aniso3d_20m", "blobs2d_100k", "batch4096"])
+    ap.add_argument("--instances", type=int, default=4096,
+                    help="batch4096 workload: number of instances")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32band"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -214,6 +348,9 @@ def main():
     import torch
     gdm = importlib.import_module(PKG)
     gdm.load_library()
+    if args.workload == "batch4096":
+        run_batch(args, rank, world, local, dist)
+        return
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     inst = make_workload(args.workload)

@@ -77,7 +77,7 @@ struct gd_ctx {
   int precision = GD_PREC_FP64;
   double mult2 = kDefaultCellMult, mult3 = kDefaultCellMult;
 
-  DevBuf coords, inst, chunks, Pv, Bi, bbox, keys0, keys1, vals0, vals1, X, Xf, table, hkeys,
+  DevBuf coords, inst, chunks, Pv, Bi, bbox, keys0, keys1, vals0, vals1, X, Xf, table, occ, hkeys,
       hvals, reps, runfl, runpos, core, cellcore, cellmin, parent, Fmark, cellcid, lab, asym,
       hvcell, hvmask, out, coreout, sorttemp, scantemp, small, kcount;
 
@@ -115,7 +115,7 @@ struct gd_ctx {
 
   void free_all(bool keep_small) {
     DevBuf* a[] = {&coords, &inst,   &chunks,   &Pv,      &Bi,     &bbox,     &keys0,
-                   &keys1,  &vals0,  &vals1,    &X,       &Xf,     &table,    &hkeys,
+                   &keys1,  &vals0,  &vals1,    &X,       &Xf,     &table,    &occ, &hkeys,
                    &hvals,  &reps,   &runfl,    &runpos,  &core,   &cellcore, &cellmin,
                    &parent, &Fmark,  &cellcid,  &lab,     &asym,   &hvcell,   &hvmask,
                    &out,    &coreout, &sorttemp, &scantemp, &small, &kcount};
@@ -149,6 +149,7 @@ struct gd_ctx {
     B.runfl = static_cast<uint32_t*>(runfl.p);
     B.runpos = static_cast<uint32_t*>(runpos.p);
     B.start = static_cast<uint32_t*>(table.p);
+    B.occ = static_cast<uint32_t*>(occ.p);
     B.hkeys = static_cast<unsigned long long*>(hkeys.p);
     B.hvals = static_cast<uint32_t*>(hvals.p);
     B.hmask = hmask;
@@ -233,7 +234,10 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
   GD_TRY(ctx->ensure(ctx->vals1, n * 4, "ids"));
   GD_TRY(ctx->ensure(ctx->X, (size_t)n * maxd * 8, "sorted coordinates"));
   if (ctx->xf) GD_TRY(ctx->ensure(ctx->Xf, (size_t)n * maxd * 4, "f32 coordinates"));
-  if (bi.table_total) GD_TRY(ctx->ensure(ctx->table, bi.table_total * 4, "cell tables"));
+  if (bi.table_total) {
+    GD_TRY(ctx->ensure(ctx->table, bi.table_total * 4, "cell tables"));
+    GD_TRY(ctx->ensure(ctx->occ, (bi.table_total / 32 + 1) * 4, "cell occupancy"));
+  }
   uint64_t hcap = 1024;
   if (bi.any_sparse) {
     while (hcap < 2 * (uint64_t)n) hcap <<= 1;
@@ -272,6 +276,7 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
   int table_launches = 0;
   if (bi.table_total) {
     GD_CUDA(cudaMemsetAsync(ctx->table.p, 0, bi.table_total * 4, s), "clear cell tables");
+    GD_CUDA(cudaMemsetAsync(ctx->occ.p, 0, (bi.table_total / 32 + 1) * 4, s), "clear occupancy");
     gdl::cell_counts(B, ctx->key64, n, ctx->sms, s);
     gdprim::exclusive_scan_u32(B.start, B.start, (int64_t)bi.table_total, ctx->scantemp.p,
                                nullptr, s);

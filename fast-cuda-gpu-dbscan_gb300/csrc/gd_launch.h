@@ -31,6 +31,7 @@ struct Bufs {
   uint32_t* runfl = nullptr;    // 1 where a cell starts (per sorted position)
   uint32_t* runpos = nullptr;   // exclusive scan of runfl: cell index = runpos+runfl-1
   uint32_t* start = nullptr;    // dense grids: cell tables of all dense instances
+  uint32_t* occ = nullptr;      // dense grids: occupancy bit per cell-table entry
   unsigned long long* hkeys = nullptr;  // sparse grids: hash slots (key)
   uint32_t* hvals = nullptr;            // sparse grids: hash slots (cell index m)
   uint32_t hmask = 0;                   // sparse grids: slots - 1

@@ -58,7 +58,8 @@ constexpr size_t kOffVals1 = kOffVals0 + up(kMaxPoints * 4);
 constexpr size_t kOffX = kOffVals1 + up(kMaxPoints * 4);
 constexpr size_t kOffXf = kOffX + up(kMaxPoints * 3 * 8);
 constexpr size_t kOffTable = kOffXf + up(kMaxPoints * 3 * 4);
-constexpr size_t kOffHkeys = kOffTable + up((kTableCells + 1) * 4);
+constexpr size_t kOffOcc = kOffTable + up((kTableCells + 1) * 4);
+constexpr size_t kOffHkeys = kOffOcc + up((kTableCells / 32 + 1) * 4);
 constexpr size_t kOffHvals = kOffHkeys + up(kHashSlots * 8);
 constexpr size_t kOffReps = kOffHvals + up(kHashSlots * 4);
 constexpr size_t kOffRunfl = kOffReps + up((kMaxPoints + 1) * 4);
@@ -217,6 +218,7 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   B.runpos = reinterpret_cast<uint32_t*>(base + kOffRunpos);
   B.reps = reinterpret_cast<int*>(base + kOffReps);
   B.start = reinterpret_cast<uint32_t*>(base + kOffTable);
+  B.occ = reinterpret_cast<uint32_t*>(base + kOffOcc);
   B.hkeys = reinterpret_cast<unsigned long long*>(base + kOffHkeys);
   B.hvals = reinterpret_cast<uint32_t*>(base + kOffHvals);
   B.hmask = (uint32_t)(kHashSlots - 1);
@@ -226,6 +228,7 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   gdl::run_scatter(B, key64, n, sms, s);
   if (bi.table_total) {
     NA_CUDA(cudaMemsetAsync(B.start, 0, bi.table_total * 4, s), "clear cell table");
+    NA_CUDA(cudaMemsetAsync(B.occ, 0, (bi.table_total / 32 + 1) * 4, s), "clear occupancy");
     gdl::cell_counts(B, key64, n, sms, s);
     gdprim::exclusive_scan_u32(B.start, B.start, (int64_t)bi.table_total, base + kOffScanTemp,
                                nullptr, s);

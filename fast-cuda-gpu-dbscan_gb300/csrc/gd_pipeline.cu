@@ -405,7 +405,9 @@ __global__ void k_cell_counts(const gdl::Bufs B) {
     const Key key = keys[b];
     const DevParams& P = B.Pv[inst_of(key, LB)];
     if (P.sparse) continue;
-    B.start[P.table_off + ((uint64_t)key & P.kmask)] = (uint32_t)(e - b);
+    const uint64_t idx = P.table_off + ((uint64_t)key & P.kmask);
+    B.start[idx] = (uint32_t)(e - b);
+    atomicOr(B.occ + (idx >> 5), 1u << (idx & 31));
   }
 }
 
@@ -605,6 +607,7 @@ __device__ __forceinline__ int warp_min_i32(int v) {
 // its points.  The probe loop is bounded by the table size.
 struct GridView {
   const uint32_t* start;
+  const uint32_t* occ;  // dense grids: one bit per cell-table entry
   const unsigned long long* hkeys;
   const uint32_t* hvals;
   const int* reps;
@@ -625,7 +628,11 @@ struct GridView {
   }
   // points of the cell with local key k: [x, y)
   __device__ __forceinline__ int2 cell(uint64_t k) const {
-    if (!sparse) return make_int2((int)start[table_off + k], (int)start[table_off + k + 1]);
+    if (!sparse) {
+      const uint64_t idx = table_off + k;
+      if (!((occ[idx >> 5] >> (idx & 31)) & 1u)) return make_int2(0, 0);
+      return make_int2((int)start[idx], (int)start[idx + 1]);
+    }
     int m = find(hi | k);
     return m < 0 ? make_int2(0, 0) : make_int2(reps[m], reps[m + 1]);
   }
@@ -647,7 +654,7 @@ struct GridView {
 };
 
 __device__ __forceinline__ GridView view_of(const gdl::Bufs& B, const DevParams& P) {
-  return GridView{B.start, B.hkeys, B.hvals, B.reps, B.hmask, P.sparse, P.table_off,
+  return GridView{B.start, B.occ, B.hkeys, B.hvals, B.reps, B.hmask, P.sparse, P.table_off,
                   (uint64_t)P.inst << P.LB};
 }
 
@@ -742,7 +749,36 @@ constexpr OffTab make_full(int D) {
 __constant__ OffTab kRows[2] = {make_rows(2), make_rows(3)};
 __constant__ OffTab kHalf[2][2] = {{make_half(2, 0), make_half(2, 1)},
                                    {make_half(3, 0), make_half(3, 1)}};
+// All offsets ordered near to far (smallest box-to-box distance first, then
+// largest), so a core count that stops at minpts usually stops early.
+constexpr OffTab make_near_first(int D) {
+  OffTab t = make_full(D);
+  int key[128] = {};
+  for (int i = 0; i < t.n; ++i) {
+    int mn = 0, mx = 0;
+    for (int k = 0; k < 3; ++k) {
+      int a = t.o[i][k] < 0 ? -t.o[i][k] : t.o[i][k];
+      int lo = a > 0 ? a - 1 : 0;
+      mn += lo * lo;
+      mx += (a + 1) * (a + 1);
+    }
+    key[i] = mn * 64 + mx;
+  }
+  for (int i = 1; i < t.n; ++i) {
+    int j = i;
+    while (j > 0 && key[j - 1] > key[j]) {
+      int tk = key[j]; key[j] = key[j - 1]; key[j - 1] = tk;
+      for (int k = 0; k < 3; ++k) {
+        signed char tc = t.o[j][k]; t.o[j][k] = t.o[j - 1][k]; t.o[j - 1][k] = tc;
+      }
+      --j;
+    }
+  }
+  return t;
+}
+
 __constant__ OffTab kFullSt[2] = {make_full(2), make_full(3)};
+__constant__ OffTab kNearSt[2] = {make_near_first(2), make_near_first(3)};
 
 // Per-warp list of candidate rows: row r holds the points lo[r] .. lo[r]+len,
 // and pre[r] is the exclusive prefix of the lengths (rows concatenated in
@@ -839,7 +875,7 @@ __device__ __forceinline__ int classify(const float* u, int ox, int oy, int oz, 
 // a cell that needs more is appended to the heavy list and handled by the
 // warp-cooperative *_heavy kernel that follows.
 constexpr int kScanThreadsPerBlock = 256;
-constexpr int kInlineCoreTests = 160;    // candidates one thread tests for one point
+constexpr int kInlineCoreTests = 256;    // pair tests one thread spends on a cell's points
 constexpr int kInlineLinkTests = 48;     // tests before a link search goes to a warp
 constexpr int kInlineBorderTests = 160;  // tests one thread spends on a cell's borders
 
@@ -894,81 +930,48 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::B
         const GridView gv = view_of(B, P);
         const bool prune = Q.prune != 0;
         const CellXYZ<D> cc = decompose<D>(cx.local, P);
-        const int64_t Gl = P.G[D - 1], cl = cc.c[D - 1];
-        const int64_t l0 = cl - 2 < 0 ? 0 : cl - 2;
-        const int64_t l1 = cl + 2 >= Gl ? Gl - 1 : cl + 2;
-        int total = 0;
-        for (int r = 0; r < T.n; ++r) {
-          int64_t rowkey = offset_key<D>(cc, T.o[r][0], T.o[r][1], 0, P);
-          if (rowkey < 0) continue;
-          rowkey -= cl;
-          const int2 rg = gv.span((uint64_t)(rowkey + l0), (uint64_t)(rowkey + l1));
-          total += rg.y - rg.x;
-        }
+        const OffTab& N = kNearSt[D - 2];
+        float o[D];
+        if (prune) cell_origin32<D>(cc, P, o);
         int ncore = 0, mn = INT_MAX;
-        if (total >= Q.minpts) {
-          float o[D];
-          if (prune) cell_origin32<D>(cc, P, o);
-          for (int i = b; i < e && !push; ++i) {
-            double px[D];
-            float pf[D], u[D];
-            load_point<D, F32>(px, pf, B, n, i, prune);
-            if (prune) frac_pos<D>(pf, o, Q, u);
-            // pass 1: cells wholly inside count without a test; sum the rest
-            int cnt = 0, ptot = total;
+        int budget = kInlineCoreTests;
+        for (int i = b; i < e && !push; ++i) {
+          double px[D];
+          float pf[D], u[D];
+          load_point<D, F32>(px, pf, B, n, i, prune);
+          if (prune) frac_pos<D>(pf, o, Q, u);
+          // stencil cells near to far: wholly inside ones count without a
+          // test, undecided ones are tested; stop at minpts
+          int cnt = 0;
+          for (int tt = 0; tt < N.n && cnt < Q.minpts && !push; ++tt) {
+            const int64_t kb = offset_key<D>(cc, N.o[tt][0], N.o[tt][1], N.o[tt][2], P);
+            if (kb < 0) continue;
+            const int2 c = gv.cell((uint64_t)kb);
+            if (c.x == c.y) continue;
             if (prune) {
-              ptot = 0;
-              for (int r = 0; r < T.n; ++r) {
-                int64_t rowkey = offset_key<D>(cc, T.o[r][0], T.o[r][1], 0, P);
-                if (rowkey < 0) continue;
-                rowkey -= cl;
-                for (int64_t z = l0; z <= l1; ++z) {
-                  const int2 c = gv.cell((uint64_t)(rowkey + z));
-                  if (c.x == c.y) continue;
-                  const int d = (int)(z - cl);
-                  const int cls = D == 3 ? classify<D>(u, T.o[r][0], T.o[r][1], d, Q)
-                                         : classify<D>(u, T.o[r][0], d, 0, Q);
-                  if (cls > 0) cnt += c.y - c.x;
-                  else if (cls == 0) ptot += c.y - c.x;
-                }
+              const int cls = classify<D>(u, N.o[tt][0], N.o[tt][1], N.o[tt][2], Q);
+              if (cls > 0) {
+                cnt += c.y - c.x;
+                continue;
               }
+              if (cls < 0) continue;
             }
-            if (cnt < Q.minpts && cnt + ptot >= Q.minpts) {
-              if (ptot > kInlineCoreTests) {
-                push = true;  // too many candidates for one thread
+            for (int q = c.x; q < c.y && cnt < Q.minpts; ++q) {
+              if (budget-- == 0) {
+                push = true;  // too much for one thread
                 break;
               }
-              // pass 2: test the undecided cells
-              for (int r = 0; r < T.n && cnt < Q.minpts; ++r) {
-                int64_t rowkey = offset_key<D>(cc, T.o[r][0], T.o[r][1], 0, P);
-                if (rowkey < 0) continue;
-                rowkey -= cl;
-                for (int64_t z = l0; z <= l1 && cnt < Q.minpts; ++z) {
-                  const int2 c = gv.cell((uint64_t)(rowkey + z));
-                  if (c.x == c.y) continue;
-                  if (prune) {
-                    const int d = (int)(z - cl);
-                    const int cls = D == 3 ? classify<D>(u, T.o[r][0], T.o[r][1], d, Q)
-                                           : classify<D>(u, T.o[r][0], d, 0, Q);
-                    if (cls != 0) continue;
-                  }
-                  for (int q = c.x; q < c.y && cnt < Q.minpts; ++q) {
-                    Cand<D, F32> cd;
-                    load_cand<D, F32>(cd, B.X, B.Xf, n, q);
-                    cnt += pair_test<D, F32>(px, pf, cd, B.X, n, q, true, Q, t) ? 1 : 0;
-                  }
-                }
-              }
-            }
-            const bool isc = cnt >= Q.minpts;
-            B.core[i] = isc ? 1 : 0;
-            if (isc) {
-              ++ncore;
-              mn = min(mn, (int)B.ids[i]);
+              Cand<D, F32> cd;
+              load_cand<D, F32>(cd, B.X, B.Xf, n, q);
+              cnt += pair_test<D, F32>(px, pf, cd, B.X, n, q, true, Q, t) ? 1 : 0;
             }
           }
-        } else {
-          for (int i = b; i < e; ++i) B.core[i] = 0;  // fewer candidates than minpts
+          const bool isc = cnt >= Q.minpts;
+          B.core[i] = isc ? 1 : 0;
+          if (isc) {
+            ++ncore;
+            mn = min(mn, (int)B.ids[i]);
+          }
         }
         if (!push) {
           B.cellcore[b] = ncore;

@@ -197,20 +197,29 @@ def batch_sizes(rng: np.random.Generator, count: int, lo: int, hi: int) -> np.nd
     return np.exp(rng.uniform(math.log(lo), math.log(hi), size=count)).astype(np.int64)
 
 
+def _batch_one(args) -> Instance:
+    seed, i, n, dim = args
+    inst = mixture_instance(_rng(seed * 1_000_003 + i + 1), n, dim)
+    inst.name = f"batch{i}"
+    return inst
+
+
 def batch4096(seed: int = 0, count: int = 4096, lo: int = 256, hi: int = 200_000,
-              scale: float = 1.0) -> list[Instance]:
-    """The batched workload: ``count`` independent mixture instances."""
+              scale: float = 1.0, workers: int = 0) -> list[Instance]:
+    """The batched workload: ``count`` independent mixture instances.
+
+    ``workers`` > 1 generates the instances in a spawned process pool (each
+    instance has its own seed, so the result does not depend on the pool)."""
     rng = _rng(seed)
     sizes = batch_sizes(rng, count, lo, hi)
     dims = np.where(rng.uniform(size=count) < 0.5, 2, 3)
-    out = []
-    for i in range(count):
-        n = max(int(sizes[i] * scale), 8)
-        sub = _rng(seed * 1_000_003 + i + 1)
-        inst = mixture_instance(sub, n, int(dims[i]))
-        inst.name = f"batch{i}"
-        out.append(inst)
-    return out
+    tasks = [(seed, i, max(int(sizes[i] * scale), 8), int(dims[i])) for i in range(count)]
+    if workers > 1:
+        import multiprocessing as mp
+        from concurrent.futures import ProcessPoolExecutor
+        with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+            return list(ex.map(_batch_one, tasks, chunksize=16))
+    return [_batch_one(t) for t in tasks]
 
 
 def poisson_arrivals(seed: int, rate: float, duration: float) -> np.ndarray:
