@@ -241,8 +241,8 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
   uint64_t hcap = 1024;
   if (bi.any_sparse) {
     while (hcap < 2 * (uint64_t)n) hcap <<= 1;
-    GD_TRY(ctx->ensure(ctx->hkeys, hcap * 8, "cell hash keys"));
-    GD_TRY(ctx->ensure(ctx->hvals, hcap * 4, "cell hash values"));
+    GD_TRY(ctx->ensure(ctx->hkeys, hcap * 8, "row hash keys"));
+    GD_TRY(ctx->ensure(ctx->hvals, hcap * 8, "row hash values"));
   }
   ctx->hmask = (uint32_t)(hcap - 1);
   GD_TRY(ctx->ensure(ctx->reps, (n + 1) * 4, "cell reps"));
@@ -283,7 +283,7 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
     table_launches += 4;
   }
   if (bi.any_sparse) {
-    GD_CUDA(cudaMemsetAsync(ctx->hkeys.p, 0xff, hcap * 8, s), "clear cell hash");
+    GD_CUDA(cudaMemsetAsync(ctx->hkeys.p, 0xff, hcap * 8, s), "clear row hash");
     gdl::hash_insert(B, ctx->key64, n, ctx->sms, s);
     table_launches += 1;
   }

@@ -32,8 +32,8 @@ struct Bufs {
   uint32_t* runpos = nullptr;   // exclusive scan of runfl: cell index = runpos+runfl-1
   uint32_t* start = nullptr;    // dense grids: cell tables of all dense instances
   uint32_t* occ = nullptr;      // dense grids: occupancy bit per cell-table entry
-  unsigned long long* hkeys = nullptr;  // sparse grids: hash slots (key)
-  uint32_t* hvals = nullptr;            // sparse grids: hash slots (cell index m)
+  unsigned long long* hkeys = nullptr;  // sparse grids: row hash slots (key of the row's first cell)
+  uint32_t* hvals = nullptr;            // sparse grids: row hash slots (begin, end) pairs
   uint32_t hmask = 0;                   // sparse grids: slots - 1
   double* X = nullptr;          // sorted float64 coordinates, max_dim x n
   float* Xf = nullptr;          // sorted centred float32 coordinates, max_dim x n
@@ -62,7 +62,7 @@ void run_flags(const void* keys, bool key64, int64_t n, uint32_t* fl, int sms, c
 void run_scatter(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
 // cell counts into the instances' table slices (scan them afterwards)
 void cell_counts(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
-// sparse instances: hash of occupied cells (clear the slots first)
+// sparse instances: hash of occupied rows (clear the slots first)
 void hash_insert(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
 // cell phases; dims: bit 0 = 2D instances present, bit 1 = 3D
 void core(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s);

@@ -61,7 +61,7 @@ constexpr size_t kOffTable = kOffXf + up(kMaxPoints * 3 * 4);
 constexpr size_t kOffOcc = kOffTable + up((kTableCells + 1) * 4);
 constexpr size_t kOffHkeys = kOffOcc + up((kTableCells / 32 + 1) * 4);
 constexpr size_t kOffHvals = kOffHkeys + up(kHashSlots * 8);
-constexpr size_t kOffReps = kOffHvals + up(kHashSlots * 4);
+constexpr size_t kOffReps = kOffHvals + up(kHashSlots * 8);
 constexpr size_t kOffRunfl = kOffReps + up((kMaxPoints + 1) * 4);
 constexpr size_t kOffRunpos = kOffRunfl + up(kMaxPoints * 4);
 constexpr size_t kOffCore = kOffRunpos + up(kMaxPoints * 4);
@@ -234,7 +234,7 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
                                nullptr, s);
   }
   if (bi.any_sparse) {
-    NA_CUDA(cudaMemsetAsync(B.hkeys, 0xff, kHashSlots * 8, s), "clear cell hash");
+    NA_CUDA(cudaMemsetAsync(B.hkeys, 0xff, kHashSlots * 8, s), "clear row hash");
     gdl::hash_insert(B, key64, n, sms, s);
   }
 

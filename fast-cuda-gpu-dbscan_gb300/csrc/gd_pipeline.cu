@@ -5,7 +5,7 @@
 //   INDEXING_STRUCTURE/insertData indexing.cu:54-118        -> k_keys (cell keys)
 //   thrust::sort_by_key           main.cu:332               -> gdprim::radix_sort_pairs
 //   INDEXING_ADJUSTMENT           indexing.cu:23-51         -> k_run_flags/k_run_scatter/
-//                                                              k_cell_counts + scan / k_hash_insert
+//                                                              k_cell_counts + scan / k_row_hash
 //   DBSCAN kernel + searchPoints  dbscan.cu:254-474         -> k_core_scan, k_core_heavy
 //   MarkAsCandidate + host merge  dbscan.cu:189-222, 25-187 -> k_union_scan, k_union_heavy,
 //                                                              k_asym_resolve (device union-find)
@@ -411,22 +411,42 @@ __global__ void k_cell_counts(const gdl::Bufs B) {
   }
 }
 
-// sparse instances: hash of the occupied cells, global key -> cell index m
+// sparse instances: hash of the occupied rows, global key of the row's first
+// cell -> [begin, end) of the row's points.  The thread of a row's first cell
+// walks the row's cells to its end.
 template <class Key>
-__global__ void k_hash_insert(const gdl::Bufs B) {
+__global__ void k_row_hash(const gdl::Bufs B) {
   const Key* keys = static_cast<const Key*>(B.keys);
   const int LB = B.Bi->LB;
   const int64_t M = *B.M;
   const uint32_t mask = B.hmask;
   for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
        m += (int64_t)gridDim.x * blockDim.x) {
-    const unsigned long long k = (unsigned long long)keys[B.reps[m]];
-    if (!B.Pv[inst_of(k, LB)].sparse) continue;
+    const uint64_t key = (uint64_t)keys[B.reps[m]];
+    const int inst = (int)(key >> LB);
+    const DevParams& P = B.Pv[inst];
+    if (!P.sparse) continue;
+    const uint64_t Gl = (uint64_t)P.G[P.dim - 1];
+    const uint64_t hi = key & ~P.kmask;
+    const uint64_t local = key & P.kmask;
+    const uint64_t rowkey = local - local % Gl;
+    if (m > 0) {
+      const uint64_t pk = (uint64_t)keys[B.reps[m - 1]];
+      if ((pk & ~P.kmask) == hi && (pk & P.kmask) >= rowkey) continue;  // not the row's first cell
+    }
+    int64_t m2 = m + 1;
+    while (m2 < M) {
+      const uint64_t k2 = (uint64_t)keys[B.reps[m2]];
+      if ((k2 & ~P.kmask) != hi || (k2 & P.kmask) >= rowkey + Gl) break;
+      ++m2;
+    }
+    const unsigned long long k = hi | rowkey;
     uint32_t h = hash_key(k) & mask;
     for (uint32_t probe = 0; probe <= mask; ++probe) {
       unsigned long long prev = atomicCAS(B.hkeys + h, kHashEmpty, k);
       if (prev == kHashEmpty || prev == k) {
-        B.hvals[h] = (uint32_t)m;
+        B.hvals[2 * h] = (uint32_t)B.reps[m];
+        B.hvals[2 * h + 1] = (uint32_t)B.reps[m2];
         break;
       }
       h = (h + 1) & mask;
@@ -602,29 +622,60 @@ __device__ __forceinline__ int warp_min_i32(int v) {
 }
 
 // Cell lookup inside one instance.  Dense grids: the instance's slice of the
-// cell tables gives every cell's point range.  Sparse grids: a hash of the
-// occupied cells' global keys gives the cell index m, and reps[m]..reps[m+1]
-// its points.  The probe loop is bounded by the table size.
+// cell tables gives every cell's point range (an occupancy bit per entry skips
+// empty cells without touching the table).  Sparse grids: a hash of the
+// occupied rows (all cells sharing every coordinate but the last) gives the
+// row's point range, and a binary search on the sorted keys the cells inside
+// it.  The probe loop is bounded by the table size.
 struct GridView {
   const uint32_t* start;
-  const uint32_t* occ;  // dense grids: one bit per cell-table entry
+  const uint32_t* occ;
   const unsigned long long* hkeys;
-  const uint32_t* hvals;
+  const uint32_t* hvals;   // per slot: row begin, row end
   const int* reps;
+  const void* keys;
   uint32_t hmask;
   int sparse;
+  int key64;
   uint64_t table_off;
-  uint64_t hi;  // instance id << LB
+  uint64_t hi;             // instance id << LB
+  int64_t Gl;              // cells along the last axis
 
-  __device__ __forceinline__ int find(uint64_t k) const {
+  __device__ __forceinline__ uint64_t gkey(int64_t i) const {
+    return key64 ? static_cast<const unsigned long long*>(keys)[i]
+                 : (uint64_t) static_cast<const uint32_t*>(keys)[i];
+  }
+  // sparse grids: points [begin, end) of the row whose first cell is rowkey
+  __device__ __forceinline__ int2 row(uint64_t rowkey) const {
+    const unsigned long long k = hi | rowkey;
     uint32_t h = hash_key(k) & hmask;
     for (uint32_t probe = 0; probe <= hmask; ++probe) {
-      unsigned long long kk = hkeys[h];
-      if (kk == k) return (int)hvals[h];
-      if (kk == kHashEmpty) return -1;
+      const unsigned long long kk = hkeys[h];
+      if (kk == k) return make_int2((int)hvals[2 * h], (int)hvals[2 * h + 1]);
+      if (kk == kHashEmpty) break;
       h = (h + 1) & hmask;
     }
-    return -1;
+    return make_int2(0, 0);
+  }
+  // first sorted position in [b, e) whose key is >= g
+  __device__ __forceinline__ int lower(int b, int e, uint64_t g) const {
+    while (b < e) {
+      const int mid = (int)(((unsigned)b + (unsigned)e) >> 1);
+      if (gkey(mid) < g) b = mid + 1;
+      else e = mid;
+    }
+    return b;
+  }
+  // points of the cells z0..z1 of the row whose first cell is rowkey: one
+  // contiguous range, because no other key sorts between them
+  __device__ __forceinline__ int2 span_row(uint64_t rowkey, int64_t z0, int64_t z1) const {
+    if (!sparse)
+      return make_int2((int)start[table_off + rowkey + z0], (int)start[table_off + rowkey + z1 + 1]);
+    const int2 r = row(rowkey);
+    if (r.x == r.y) return r;
+    const int a = lower(r.x, r.y, hi | (rowkey + (uint64_t)z0));
+    const int b = lower(a, r.y, hi | (rowkey + (uint64_t)z1 + 1));
+    return make_int2(a, b);
   }
   // points of the cell with local key k: [x, y)
   __device__ __forceinline__ int2 cell(uint64_t k) const {
@@ -633,29 +684,21 @@ struct GridView {
       if (!((occ[idx >> 5] >> (idx & 31)) & 1u)) return make_int2(0, 0);
       return make_int2((int)start[idx], (int)start[idx + 1]);
     }
-    int m = find(hi | k);
-    return m < 0 ? make_int2(0, 0) : make_int2(reps[m], reps[m + 1]);
+    const int64_t z = (int64_t)(k % (uint64_t)Gl);
+    return span_row(k - (uint64_t)z, z, z);
   }
-  // points of the cells k0..k1 (consecutive local keys along one row): one
-  // contiguous range, because no other key sorts between them
+  // points of the cells k0..k1 (consecutive local keys along one row)
   __device__ __forceinline__ int2 span(uint64_t k0, uint64_t k1) const {
     if (!sparse)
       return make_int2((int)start[table_off + k0], (int)start[table_off + k1 + 1]);
-    int lo = INT_MAX, hi2 = 0;
-    for (uint64_t k = k0; k <= k1; ++k) {
-      int m = find(hi | k);
-      if (m >= 0) {
-        lo = min(lo, reps[m]);
-        hi2 = max(hi2, reps[m + 1]);
-      }
-    }
-    return lo == INT_MAX ? make_int2(0, 0) : make_int2(lo, hi2);
+    const int64_t z0 = (int64_t)(k0 % (uint64_t)Gl);
+    return span_row(k0 - (uint64_t)z0, z0, z0 + (int64_t)(k1 - k0));
   }
 };
 
 __device__ __forceinline__ GridView view_of(const gdl::Bufs& B, const DevParams& P) {
-  return GridView{B.start, B.occ, B.hkeys, B.hvals, B.reps, B.hmask, P.sparse, P.table_off,
-                  (uint64_t)P.inst << P.LB};
+  return GridView{B.start, B.occ, B.hkeys, B.hvals, B.reps, B.keys, B.hmask, P.sparse,
+                  B.Bi->key64, P.table_off, (uint64_t)P.inst << P.LB, P.G[P.dim - 1]};
 }
 
 template <bool KEY64>
@@ -867,13 +910,54 @@ __device__ __forceinline__ int classify(const float* u, int ox, int oy, int oz, 
   return 0;
 }
 
+// Per-axis terms of the classification for one point: mx[k][o+2] is the
+// squared largest distance (plus uerr) along axis k from the point to the cell
+// slab at offset o, mn[k][o+2] the squared smallest one (minus uerr).  A cell's
+// test then costs two sums of D table entries.
+template <int D>
+struct PointCls {
+  float mx[D][5];
+  float mn[D][5];
+};
+
+template <int D, class PP>
+__device__ __forceinline__ void point_cls(const float* u, const PP& P, PointCls<D>& pc) {
+#pragma unroll
+  for (int k = 0; k < D; ++k)
+#pragma unroll
+    for (int o = -2; o <= 2; ++o) {
+      const float a = u[k] - (float)o;
+      const float b = a - 1.0f;
+      const float mx = fmaxf(fabsf(a), fabsf(b)) + P.uerr;
+      const float mn = fmaxf(fmaxf(-a, b) - P.uerr, 0.0f);
+      pc.mx[k][o + 2] = mx * mx;
+      pc.mn[k][o + 2] = mn * mn;
+    }
+}
+
+template <int D, class PP>
+__device__ __forceinline__ int cls_of(const PointCls<D>& pc, int ox, int oy, int oz, const PP& P) {
+  float smax = pc.mx[0][ox + 2] + pc.mx[1][oy + 2];
+  float smin = pc.mn[0][ox + 2] + pc.mn[1][oy + 2];
+  if (D == 3) {
+    smax += pc.mx[2][oz + 2];
+    smin += pc.mn[2][oz + 2];
+  }
+  if (smax <= P.thr_in) return 1;
+  if (smin >= P.thr_out) return -1;
+  return 0;
+}
+
 // ------------------------------------------------- thread-per-cell front ends
 // Most cells need little work: isolated noise points whose stencil holds fewer
 // than minpts points, cells whose neighbour links are found by the first test,
 // border points with a handful of candidate cores.  The *_scan kernels give one
 // thread to each cell and finish those cases inline (bounded work per thread);
 // a cell that needs more is appended to the heavy list and handled by the
-// warp-cooperative *_heavy kernel that follows.
+// warp-cooperative *_heavy kernel that follows.  The stencil is walked row by
+// row (5 rows in 2D, 25 in 3D, own row first); a row is one contiguous range of
+// sorted points, and its non-empty cells are visited through the run structure,
+// so empty cells cost nothing.
 constexpr int kScanThreadsPerBlock = 256;
 constexpr int kInlineCoreTests = 256;    // pair tests one thread spends on a cell's points
 constexpr int kInlineLinkTests = 48;     // tests before a link search goes to a warp
@@ -906,6 +990,32 @@ __device__ __forceinline__ void load_point(double* x, float* f, const gdl::Bufs&
   }
 }
 
+// Stencil rows of a cell: row r of kRows, its first cell's local key, and the
+// last-axis cell range [l0, l1] around the cell.
+template <int D>
+struct RowWalk {
+  CellXYZ<D> cc;
+  int64_t cl, l0, l1;
+  __device__ __forceinline__ void init(const CellXYZ<D>& c, const DevParams& P) {
+    cc = c;
+    const int64_t Gl = P.G[D - 1];
+    cl = c.c[D - 1];
+    l0 = cl - 2 < 0 ? 0 : cl - 2;
+    l1 = cl + 2 >= Gl ? Gl - 1 : cl + 2;
+  }
+  // local key of row r's first cell, or -1 when the row is outside the grid
+  __device__ __forceinline__ int64_t rowkey(const OffTab& T, int r, const DevParams& P) const {
+    const int64_t k = offset_key<D>(cc, T.o[r][0], T.o[r][1], 0, P);
+    return k < 0 ? k : k - cl;
+  }
+};
+
+// next cell of a row walk: [q, end), its last-axis offset from the cell in work
+template <bool KEY64>
+__device__ __forceinline__ int cell_end(const gdl::Bufs& B, int q) {
+  return B.reps[B.runpos[q] + 1];
+}
+
 template <int D, bool F32, bool KEY64>
 __global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::Bufs B, int64_t n) {
   const OffTab& T = kRows[D - 2];
@@ -929,41 +1039,50 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::B
       } else {
         const GridView gv = view_of(B, P);
         const bool prune = Q.prune != 0;
-        const CellXYZ<D> cc = decompose<D>(cx.local, P);
-        const OffTab& N = kNearSt[D - 2];
+        RowWalk<D> rw;
+        rw.init(decompose<D>(cx.local, P), P);
         float o[D];
-        if (prune) cell_origin32<D>(cc, P, o);
+        if (prune) cell_origin32<D>(rw.cc, P, o);
         int ncore = 0, mn = INT_MAX;
         int budget = kInlineCoreTests;
         for (int i = b; i < e && !push; ++i) {
           double px[D];
           float pf[D], u[D];
           load_point<D, F32>(px, pf, B, n, i, prune);
-          if (prune) frac_pos<D>(pf, o, Q, u);
-          // stencil cells near to far: wholly inside ones count without a
-          // test, undecided ones are tested; stop at minpts
+          PointCls<D> pc;
+          if (prune) {
+            frac_pos<D>(pf, o, Q, u);
+            point_cls<D>(u, Q, pc);
+          }
+          // rows own first; cells wholly inside count without a test,
+          // undecided ones are tested; stop at minpts
           int cnt = 0;
-          for (int tt = 0; tt < N.n && cnt < Q.minpts && !push; ++tt) {
-            const int64_t kb = offset_key<D>(cc, N.o[tt][0], N.o[tt][1], N.o[tt][2], P);
-            if (kb < 0) continue;
-            const int2 c = gv.cell((uint64_t)kb);
-            if (c.x == c.y) continue;
-            if (prune) {
-              const int cls = classify<D>(u, N.o[tt][0], N.o[tt][1], N.o[tt][2], Q);
+          for (int r = 0; r < T.n && cnt < Q.minpts && !push; ++r) {
+            const int64_t rk = rw.rowkey(T, r, P);
+            if (rk < 0) continue;
+            const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
+            for (int q = sp.x; q < sp.y && cnt < Q.minpts && !push;) {
+              const int qe = cell_end<KEY64>(B, q);
+              int cls = 0;
+              if (prune) {
+                const int d = (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
+                cls = D == 3 ? cls_of<D>(pc, T.o[r][0], T.o[r][1], d, Q)
+                             : cls_of<D>(pc, T.o[r][0], d, 0, Q);
+              }
               if (cls > 0) {
-                cnt += c.y - c.x;
-                continue;
+                cnt += qe - q;
+              } else if (cls == 0) {
+                for (int qq = q; qq < qe && cnt < Q.minpts; ++qq) {
+                  if (budget-- == 0) {
+                    push = true;  // too much for one thread
+                    break;
+                  }
+                  Cand<D, F32> cd;
+                  load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
+                  cnt += pair_test<D, F32>(px, pf, cd, B.X, n, qq, true, Q, t) ? 1 : 0;
+                }
               }
-              if (cls < 0) continue;
-            }
-            for (int q = c.x; q < c.y && cnt < Q.minpts; ++q) {
-              if (budget-- == 0) {
-                push = true;  // too much for one thread
-                break;
-              }
-              Cand<D, F32> cd;
-              load_cand<D, F32>(cd, B.X, B.Xf, n, q);
-              cnt += pair_test<D, F32>(px, pf, cd, B.X, n, q, true, Q, t) ? 1 : 0;
+              q = qe;
             }
           }
           const bool isc = cnt >= Q.minpts;
@@ -1017,10 +1136,23 @@ __device__ __forceinline__ int inline_link(const gdl::Bufs& B, int64_t n, int bA
   return 0;
 }
 
+// bit of offset (ox, oy, oz) in the kHalf[D][pass] table, or -1 if it is not there
+template <int D>
+__device__ __forceinline__ int half_bit(int pass, int ox, int oy, int oz) {
+  const bool pos = ox > 0 || (ox == 0 && (oy > 0 || (oy == 0 && oz > 0)));
+  if (!pos) return -1;
+  const bool near = ox >= -1 && ox <= 1 && oy >= -1 && oy <= 1 && oz >= -1 && oz <= 1;
+  if ((pass == 0) != near) return -1;
+  const OffTab& T = kHalf[D - 2][pass];
+  for (int i = 0; i < T.n; ++i)
+    if (T.o[i][0] == ox && T.o[i][1] == oy && T.o[i][2] == oz) return i;
+  return -1;
+}
+
 template <int D, bool F32, bool KEY64>
 __global__ void __launch_bounds__(kScanThreadsPerBlock)
 k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
-  const OffTab& T = kHalf[D - 2][pass];
+  const OffTab& T = kRows[D - 2];
   const int lane = threadIdx.x & 31;
   const int LB = B.Bi->LB;
   int64_t mlo, mhi;
@@ -1039,19 +1171,31 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
         const DevParams& P = *cx.P;
         const PredParams Q = pred_params(P);
         const GridView gv = view_of(B, P);
-        const CellXYZ<D> cc = decompose<D>(cx.local, P);
+        RowWalk<D> rw;
+        rw.init(decompose<D>(cx.local, P), P);
         float oA[D];
-        if (Q.prune) cell_origin32<D>(cc, P, oA);
-        for (int tt = 0; tt < T.n; ++tt) {
-          const int64_t kb = offset_key<D>(cc, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
-          if (kb < 0) continue;
-          const int2 cb = gv.cell((uint64_t)kb);
-          if (cb.x == cb.y || B.cellcore[cb.x] == 0) continue;
-          if (uf_find(B.parent, b) == uf_find(B.parent, cb.x)) continue;
-          const int r = inline_link<D, F32>(B, n, b, e, cb.x, cb.y, oA, T.o[tt][0], T.o[tt][1],
-                                            T.o[tt][2], Q, t);
-          if (r > 0) uf_union(B.parent, B.cellmin, b, cb.x);
-          else if (r < 0) open |= 1ull << tt;
+        if (Q.prune) cell_origin32<D>(rw.cc, P, oA);
+        for (int r = 0; r < T.n; ++r) {
+          const int ox = T.o[r][0], oy = T.o[r][1];
+          // rows with a negative leading offset hold no half-stencil cell
+          if (ox < 0 || (D == 3 && ox == 0 && oy < 0)) continue;
+          if (pass == 0 && (ox > 1 || oy > 1 || oy < -1)) continue;
+          const int64_t rk = rw.rowkey(T, r, P);
+          if (rk < 0) continue;
+          const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
+          for (int q = sp.x; q < sp.y;) {
+            const int qe = cell_end<KEY64>(B, q);
+            const int d = (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
+            const int bit = D == 3 ? half_bit<D>(pass, ox, oy, d) : half_bit<D>(pass, ox, d, 0);
+            if (bit >= 0 && B.cellcore[q] > 0 &&
+                uf_find(B.parent, b) != uf_find(B.parent, q)) {
+              const int res = D == 3 ? inline_link<D, F32>(B, n, b, e, q, qe, oA, ox, oy, d, Q, t)
+                                     : inline_link<D, F32>(B, n, b, e, q, qe, oA, ox, d, 0, Q, t);
+              if (res > 0) uf_union(B.parent, B.cellmin, b, q);
+              else if (res < 0) open |= 1ull << bit;
+            }
+            q = qe;
+          }
         }
       }
     }
@@ -1062,7 +1206,7 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
 
 template <int D, bool F32, bool KEY64>
 __global__ void __launch_bounds__(kScanThreadsPerBlock) k_border_scan(const gdl::Bufs B, int64_t n) {
-  const OffTab& T = kFullSt[D - 2];
+  const OffTab& T = kRows[D - 2];
   const int lane = threadIdx.x & 31;
   const int LB = B.Bi->LB;
   int64_t mlo, mhi;
@@ -1082,56 +1226,58 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_border_scan(const gdl:
         const PredParams Q = pred_params(P);
         const GridView gv = view_of(B, P);
         const bool prune = Q.prune != 0;
-        const CellXYZ<D> cc = decompose<D>(cx.local, P);
-        int cores = 0;
-        for (int tt = 0; tt < T.n; ++tt) {
-          const int64_t kb = offset_key<D>(cc, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
-          if (kb < 0) continue;
-          const int2 cb = gv.cell((uint64_t)kb);
-          if (cb.x < cb.y) cores += B.cellcore[cb.x];
-        }
-        if (cores > 0) {  // else no core point in reach: the non-core points stay NOISE
-          float o[D];
-          if (prune) cell_origin32<D>(cc, P, o);
-          int budget = kInlineBorderTests;
-          for (int i = b; i < e && !push; ++i) {
-            if (B.core[i]) continue;
-            double px[D];
-            float pf[D], u[D];
-            load_point<D, F32>(px, pf, B, n, i, prune);
-            if (prune) frac_pos<D>(pf, o, Q, u);
-            int best = INT_MAX;
-            for (int tt = 0; tt < T.n && !push; ++tt) {
-              const int64_t kb = offset_key<D>(cc, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
-              if (kb < 0) continue;
-              const int2 cb = gv.cell((uint64_t)kb);
-              if (cb.x == cb.y || B.cellcore[cb.x] == 0) continue;
-              const int cB = B.cellcid[cb.x];
-              if (cB >= best) continue;
-              if (prune) {
-                const int cls = classify<D>(u, T.o[tt][0], T.o[tt][1], T.o[tt][2], Q);
+        RowWalk<D> rw;
+        rw.init(decompose<D>(cx.local, P), P);
+        float o[D];
+        if (prune) cell_origin32<D>(rw.cc, P, o);
+        int budget = kInlineBorderTests;
+        for (int i = b; i < e && !push; ++i) {
+          if (B.core[i]) continue;
+          double px[D];
+          float pf[D], u[D];
+          load_point<D, F32>(px, pf, B, n, i, prune);
+          PointCls<D> pc;
+          if (prune) {
+            frac_pos<D>(pf, o, Q, u);
+            point_cls<D>(u, Q, pc);
+          }
+          int best = INT_MAX;
+          for (int r = 0; r < T.n && !push; ++r) {
+            const int64_t rk = rw.rowkey(T, r, P);
+            if (rk < 0) continue;
+            const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
+            for (int q = sp.x; q < sp.y && !push;) {
+              const int qe = cell_end<KEY64>(B, q);
+              const int cB = B.cellcore[q] > 0 ? B.cellcid[q] : INT_MAX;
+              if (cB < best) {
+                int cls = 0;
+                if (prune) {
+                  const int d = (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
+                  cls = D == 3 ? cls_of<D>(pc, T.o[r][0], T.o[r][1], d, Q)
+                               : cls_of<D>(pc, T.o[r][0], d, 0, Q);
+                }
                 if (cls > 0) {
                   best = cB;  // every point of that cell, a core among them, is in reach
-                  continue;
+                } else if (cls == 0) {
+                  for (int qq = q; qq < qe; ++qq) {
+                    if (!B.core[qq]) continue;
+                    if (budget-- == 0) {
+                      push = true;  // too much for one thread
+                      break;
+                    }
+                    Cand<D, F32> cd;
+                    load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
+                    if (pair_test<D, F32>(px, pf, cd, B.X, n, qq, false, Q, t)) {
+                      best = cB;
+                      break;
+                    }
+                  }
                 }
-                if (cls < 0) continue;
               }
-              for (int q = cb.x; q < cb.y; ++q) {
-                if (!B.core[q]) continue;
-                if (budget-- == 0) {
-                  push = true;  // too much for one thread
-                  break;
-                }
-                Cand<D, F32> cd;
-                load_cand<D, F32>(cd, B.X, B.Xf, n, q);
-                if (pair_test<D, F32>(px, pf, cd, B.X, n, q, false, Q, t)) {
-                  best = cB;
-                  break;
-                }
-              }
+              q = qe;
             }
-            if (!push && best != INT_MAX) B.lab[i] = best;
           }
+          if (!push && best != INT_MAX) B.lab[i] = best;
         }
       }
     }
@@ -1623,8 +1769,8 @@ void cell_counts(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) 
 }
 
 void hash_insert(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) {
-  if (key64) k_hash_insert<unsigned long long><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
-  else k_hash_insert<uint32_t><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
+  if (key64) k_row_hash<unsigned long long><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
+  else k_row_hash<uint32_t><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
 }
 
 #define GD_L1(D, f32, key64, KERNEL, GRID, THREADS, ...)                          \
