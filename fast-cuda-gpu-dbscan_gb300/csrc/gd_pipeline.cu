@@ -1054,14 +1054,34 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::B
             frac_pos<D>(pf, o, Q, u);
             point_cls<D>(u, Q, pc);
           }
-          // rows own first; cells wholly inside count without a test,
-          // undecided ones are tested; stop at minpts
-          int cnt = 0;
-          for (int r = 0; r < T.n && cnt < Q.minpts && !push; ++r) {
+          // pass 1: cells wholly inside count without a test; the undecided
+          // ones are only summed
+          int cnt = 0, ptot = 0;
+          for (int r = 0; r < T.n; ++r) {
             const int64_t rk = rw.rowkey(T, r, P);
             if (rk < 0) continue;
             const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
-            for (int q = sp.x; q < sp.y && cnt < Q.minpts && !push;) {
+            if (!prune) {
+              ptot += sp.y - sp.x;
+              continue;
+            }
+            for (int q = sp.x; q < sp.y;) {
+              const int qe = cell_end<KEY64>(B, q);
+              const int d = (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
+              const int cls = D == 3 ? cls_of<D>(pc, T.o[r][0], T.o[r][1], d, Q)
+                                     : cls_of<D>(pc, T.o[r][0], d, 0, Q);
+              if (cls > 0) cnt += qe - q;
+              else if (cls == 0) ptot += qe - q;
+              q = qe;
+            }
+          }
+          // pass 2 (only if still undecided): test the undecided cells, own row
+          // first, and stop at minpts
+          for (int r = 0; r < T.n && cnt < Q.minpts && cnt + ptot >= Q.minpts && !push; ++r) {
+            const int64_t rk = rw.rowkey(T, r, P);
+            if (rk < 0) continue;
+            const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
+            for (int q = sp.x; q < sp.y && cnt < Q.minpts && cnt + ptot >= Q.minpts && !push;) {
               const int qe = cell_end<KEY64>(B, q);
               int cls = 0;
               if (prune) {
@@ -1069,9 +1089,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::B
                 cls = D == 3 ? cls_of<D>(pc, T.o[r][0], T.o[r][1], d, Q)
                              : cls_of<D>(pc, T.o[r][0], d, 0, Q);
               }
-              if (cls > 0) {
-                cnt += qe - q;
-              } else if (cls == 0) {
+              if (cls == 0) {
                 for (int qq = q; qq < qe && cnt < Q.minpts; ++qq) {
                   if (budget-- == 0) {
                     push = true;  // too much for one thread
@@ -1079,7 +1097,10 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::B
                   }
                   Cand<D, F32> cd;
                   load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
-                  cnt += pair_test<D, F32>(px, pf, cd, B.X, n, qq, true, Q, t) ? 1 : 0;
+                  const bool hit = pair_test<D, F32>(px, pf, cd, B.X, n, qq, true, Q, t);
+                  cnt += hit ? 1 : 0;
+                  ptot -= 1;  // decided now
+                  if (cnt + ptot < Q.minpts) break;
                 }
               }
               q = qe;
@@ -1137,16 +1158,29 @@ __device__ __forceinline__ int inline_link(const gdl::Bufs& B, int64_t n, int bA
 }
 
 // bit of offset (ox, oy, oz) in the kHalf[D][pass] table, or -1 if it is not there
+struct HalfBits {
+  signed char b[2][2][5][5][5];
+};
+
+constexpr HalfBits make_half_bits() {
+  HalfBits h{};
+  for (int d = 0; d < 2; ++d)
+    for (int p = 0; p < 2; ++p) {
+      for (int x = 0; x < 5; ++x)
+        for (int y = 0; y < 5; ++y)
+          for (int z = 0; z < 5; ++z) h.b[d][p][x][y][z] = -1;
+      const OffTab t = make_half(d + 2, p);
+      for (int i = 0; i < t.n; ++i)
+        h.b[d][p][t.o[i][0] + 2][t.o[i][1] + 2][t.o[i][2] + 2] = (signed char)i;
+    }
+  return h;
+}
+
+__constant__ HalfBits kHalfBits = make_half_bits();
+
 template <int D>
 __device__ __forceinline__ int half_bit(int pass, int ox, int oy, int oz) {
-  const bool pos = ox > 0 || (ox == 0 && (oy > 0 || (oy == 0 && oz > 0)));
-  if (!pos) return -1;
-  const bool near = ox >= -1 && ox <= 1 && oy >= -1 && oy <= 1 && oz >= -1 && oz <= 1;
-  if ((pass == 0) != near) return -1;
-  const OffTab& T = kHalf[D - 2][pass];
-  for (int i = 0; i < T.n; ++i)
-    if (T.o[i][0] == ox && T.o[i][1] == oy && T.o[i][2] == oz) return i;
-  return -1;
+  return kHalfBits.b[D - 2][pass][ox + 2][oy + 2][oz + 2];
 }
 
 template <int D, bool F32, bool KEY64>
