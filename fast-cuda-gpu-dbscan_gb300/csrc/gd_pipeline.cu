@@ -962,6 +962,7 @@ constexpr int kScanThreadsPerBlock = 256;
 constexpr int kInlineCoreTests = 256;    // pair tests one thread spends on a cell's points
 constexpr int kInlineLinkTests = 48;     // tests before a link search goes to a warp
 constexpr int kInlineBorderTests = 160;  // tests one thread spends on a cell's borders
+constexpr int kDeferCells = 8;           // undecided cells queued by the core count
 
 // warp-aggregated append to the heavy list (all 32 lanes must call it)
 __device__ __forceinline__ void heavy_push(const gdl::Bufs& B, int slot, bool push, int64_t m,
@@ -1054,34 +1055,29 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::B
             frac_pos<D>(pf, o, Q, u);
             point_cls<D>(u, Q, pc);
           }
-          // pass 1: cells wholly inside count without a test; the undecided
-          // ones are only summed
-          int cnt = 0, ptot = 0;
-          for (int r = 0; r < T.n; ++r) {
+          // One walk, own row first: cells wholly inside count at once, cells
+          // wholly outside are skipped, undecided cells are queued and tested
+          // only when the queue fills or the walk ends short of minpts.
+          int cnt = 0, ptot = 0, nq = 0;
+          int qb[kDeferCells], qe_[kDeferCells];
+          auto flush = [&](void) {
+            for (int j = 0; j < nq && cnt < Q.minpts && !push; ++j)
+              for (int qq = qb[j]; qq < qe_[j] && cnt < Q.minpts; ++qq) {
+                if (budget-- == 0) {
+                  push = true;  // too much for one thread
+                  break;
+                }
+                Cand<D, F32> cd;
+                load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
+                cnt += pair_test<D, F32>(px, pf, cd, B.X, n, qq, true, Q, t) ? 1 : 0;
+              }
+            nq = 0;
+          };
+          for (int r = 0; r < T.n && cnt < Q.minpts && !push; ++r) {
             const int64_t rk = rw.rowkey(T, r, P);
             if (rk < 0) continue;
             const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
-            if (!prune) {
-              ptot += sp.y - sp.x;
-              continue;
-            }
-            for (int q = sp.x; q < sp.y;) {
-              const int qe = cell_end<KEY64>(B, q);
-              const int d = (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
-              const int cls = D == 3 ? cls_of<D>(pc, T.o[r][0], T.o[r][1], d, Q)
-                                     : cls_of<D>(pc, T.o[r][0], d, 0, Q);
-              if (cls > 0) cnt += qe - q;
-              else if (cls == 0) ptot += qe - q;
-              q = qe;
-            }
-          }
-          // pass 2 (only if still undecided): test the undecided cells, own row
-          // first, and stop at minpts
-          for (int r = 0; r < T.n && cnt < Q.minpts && cnt + ptot >= Q.minpts && !push; ++r) {
-            const int64_t rk = rw.rowkey(T, r, P);
-            if (rk < 0) continue;
-            const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
-            for (int q = sp.x; q < sp.y && cnt < Q.minpts && cnt + ptot >= Q.minpts && !push;) {
+            for (int q = sp.x; q < sp.y && cnt < Q.minpts && !push;) {
               const int qe = cell_end<KEY64>(B, q);
               int cls = 0;
               if (prune) {
@@ -1089,23 +1085,19 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::B
                 cls = D == 3 ? cls_of<D>(pc, T.o[r][0], T.o[r][1], d, Q)
                              : cls_of<D>(pc, T.o[r][0], d, 0, Q);
               }
-              if (cls == 0) {
-                for (int qq = q; qq < qe && cnt < Q.minpts; ++qq) {
-                  if (budget-- == 0) {
-                    push = true;  // too much for one thread
-                    break;
-                  }
-                  Cand<D, F32> cd;
-                  load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
-                  const bool hit = pair_test<D, F32>(px, pf, cd, B.X, n, qq, true, Q, t);
-                  cnt += hit ? 1 : 0;
-                  ptot -= 1;  // decided now
-                  if (cnt + ptot < Q.minpts) break;
-                }
+              if (cls > 0) {
+                cnt += qe - q;
+              } else if (cls == 0) {
+                if (nq == kDeferCells) flush();
+                qb[nq] = q;
+                qe_[nq] = qe;
+                ++nq;
+                ptot += qe - q;
               }
               q = qe;
             }
           }
+          if (cnt < Q.minpts && cnt + ptot >= Q.minpts) flush();
           const bool isc = cnt >= Q.minpts;
           B.core[i] = isc ? 1 : 0;
           if (isc) {
@@ -1213,10 +1205,31 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
           const int ox = T.o[r][0], oy = T.o[r][1];
           // rows with a negative leading offset hold no half-stencil cell
           if (ox < 0 || (D == 3 && ox == 0 && oy < 0)) continue;
-          if (pass == 0 && (ox > 1 || oy > 1 || oy < -1)) continue;
+          const bool near_row = ox <= 1 && oy >= -1 && oy <= 1;
+          if (pass == 0 && !near_row) continue;
           const int64_t rk = rw.rowkey(T, r, P);
           if (rk < 0) continue;
-          const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
+          const bool own = ox == 0 && (D == 2 || oy == 0);
+          // the last-axis cells this pass needs: near rows hold the near pass's
+          // cells at |dz| <= 1 and the far pass's at |dz| = 2
+          for (int seg = 0; seg < 2; ++seg) {
+          int64_t z0, z1;
+          if (pass == 0) {
+            if (seg) break;
+            z0 = own ? rw.cl + 1 : rw.cl - 1;
+            z1 = rw.cl + 1;
+          } else if (near_row) {
+            z0 = z1 = seg ? rw.cl + 2 : rw.cl - 2;
+            if (own && !seg) continue;
+          } else {
+            if (seg) break;
+            z0 = rw.cl - 2;
+            z1 = rw.cl + 2;
+          }
+          z0 = z0 < rw.l0 ? rw.l0 : z0;
+          z1 = z1 > rw.l1 ? rw.l1 : z1;
+          if (z0 > z1) continue;
+          const int2 sp = gv.span_row((uint64_t)rk, z0, z1);
           for (int q = sp.x; q < sp.y;) {
             const int qe = cell_end<KEY64>(B, q);
             const int d = (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
@@ -1229,6 +1242,7 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
               else if (res < 0) open |= 1ull << bit;
             }
             q = qe;
+          }
           }
         }
       }
