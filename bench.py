@@ -1,7 +1,7 @@
 """Benchmark: exact-DBSCAN points/sec on one GB300 (replicas on N GPUs).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload zipf2d_10m|aniso3d_20m|blobs2d_100k]
+                  [--workload zipf2d_10m|aniso3d_20m|blobs2d_100k|batch4096|serve]
                   [--precision fp64|fp32band]
 
 Default workload: 10,000,000 2D float64 points (500 Zipf-sized Gaussian blobs +
@@ -19,6 +19,11 @@ The JSON line also carries a float32-band run of the same workload, per-phase
 device times, the roofline of the pipeline, the CPU baseline (the CPU
 restatement of the reference's exact DBSCAN on this host's cores, bounded
 sample) and the SM clocks sampled during the timed region.
+
+--workload batch4096: 4096 independent instances in one gd_batch_dbscan run,
+against the single-instance path called once per instance.
+--workload serve: a Poisson request stream through the request server
+(gd_server_*), p50/p99 latency and throughput against one-at-a-time solves.
 
 --impl reference times the reference's exact CPU DBSCAN path on this host: the
 reference's own R-tree program (oracle/_ref) where it was built, otherwise the
@@ -313,6 +318,145 @@ def run_batch(args, rank, world, local, dist):
         dist.destroy_process_group()
 
 
+def _pct(xs, q):
+    return float(np.percentile(np.asarray(xs), q)) if len(xs) else None
+
+
+def run_serve(args, rank, world, local, dist):
+    """Served request stream through the request server (gd_server_*): Poisson
+    arrivals, every request with its own points, eps, minpts and dimension, host
+    buffers in and labels out.  Open loop at the stream's rate gives p50/p99
+    latency; a closed loop (every request queued at once) gives the saturation
+    throughput.  Both are compared with one-at-a-time plain solves (gd_dbscan
+    per request, in arrival order) on the same requests, and every request's
+    labels must be identical in both."""
+    import torch
+    gdm = importlib.import_module(PKG)
+    ds = importlib.import_module(PKG + ".datasets")
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    pool, arrivals, which = ds.serve_stream(seed=0, rate=args.rate, duration=args.duration,
+                                            pool=args.pool,
+                                            workers=min(16, os.cpu_count() or 1))
+    gen_s = time.perf_counter() - t0
+    # pinned host copies: both arms read the same host buffers
+    pts = [torch.from_numpy(np.ascontiguousarray(i.points)).pin_memory().numpy() for i in pool]
+    prec = gdm.GD_PREC_FP64 if args.precision == "fp64" else gdm.GD_PREC_FP32_BAND
+    nreq = len(arrivals)
+    npts = np.array([pool[w].n for w in which], dtype=np.int64)
+    budget = int(args.hbm_budget_gb * (1 << 30))
+
+    def open_loop_server(srv):
+        ids = [None] * nreq
+        start = time.perf_counter()
+
+        def submitter():
+            for r in range(nreq):
+                d = start + arrivals[r] - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                inst = pool[which[r]]
+                ids[r] = srv.submit(pts[which[r]], inst.eps, inst.minpts)
+
+        th = threading.Thread(target=submitter)
+        th.start()
+        lat, labs, batch = [], [], []
+        first = last = None
+        for r in range(nreq):
+            while ids[r] is None:
+                time.sleep(0.0002)
+            lab, info = srv.wait(ids[r])
+            lat.append(info["done_ms"] - info["submit_ms"])
+            batch.append(info["batch_size"])
+            first = info["submit_ms"] if first is None else min(first, info["submit_ms"])
+            last = info["done_ms"] if last is None else max(last, info["done_ms"])
+            labs.append(lab)
+        th.join()
+        return lat, labs, batch, (last - first) / 1e3
+
+    def open_loop_single(ctx):
+        lat, labs = [], []
+        start = time.perf_counter()
+        for r in range(nreq):
+            arr = start + arrivals[r]
+            d = arr - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            inst = pool[which[r]]
+            labs.append(ctx.dbscan(pts[which[r]], inst.eps, inst.minpts))
+            lat.append((time.perf_counter() - arr) * 1e3)
+        return lat, labs, time.perf_counter() - start - arrivals[0]
+
+    sat_n = min(nreq, args.saturation_requests)
+
+    def closed_loop_server(srv):
+        a = time.perf_counter()
+        ids = [srv.submit(pts[which[r]], pool[which[r]].eps, pool[which[r]].minpts)
+               for r in range(sat_n)]
+        for i in ids:
+            srv.wait(i)
+        return time.perf_counter() - a
+
+    def closed_loop_single(ctx):
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        for r in range(sat_n):
+            ctx.dbscan(pts[which[r]], pool[which[r]].eps, pool[which[r]].minpts)
+        return time.perf_counter() - a
+
+    with gdm.Server(local, workers=args.workers, max_batch=args.max_batch, precision=prec,
+                    hbm_budget_bytes=budget) as srv:
+        # warm-up: every pool instance once, so device buffers are grown
+        for i in [srv.submit(p, inst.eps, inst.minpts) for p, inst in zip(pts, pool)]:
+            srv.wait(i)
+        with ClockSampler(local) as clk:
+            s_lat, s_labs, s_batch, s_span = open_loop_server(srv)
+        sat_server = closed_loop_server(srv)
+        sstats = srv.stats()
+    ctx = gdm.Context(local, precision=prec)
+    for p, inst in zip(pts, pool):
+        ctx.dbscan(p, inst.eps, inst.minpts)
+    o_lat, o_labs, o_span = open_loop_single(ctx)
+    sat_single = closed_loop_single(ctx)
+    ctx.close()
+    same = all(np.array_equal(a, b) for a, b in zip(s_labs, o_labs))
+    total = int(npts.sum())
+    sat_pts = int(npts[:sat_n].sum())
+    value = world * sat_pts / sat_server
+    line = {
+        "metric": METRIC + " (served request stream)", "value": value, "unit": "points/s",
+        "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": sat_server * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == gdm.GD_PREC_FP64 else "f32+f64band", "data": "synthetic",
+        "config": {"workload": "serve", "rate_per_s": args.rate, "duration_s": args.duration,
+                   "requests": nreq, "points": total, "pool_instances": len(pool),
+                   "sizes": "log-uniform [1000, 2000000]", "workers": args.workers,
+                   "max_batch": args.max_batch, "hbm_budget_gb": args.hbm_budget_gb,
+                   "precision": args.precision, "parallelism": f"replicas{world}",
+                   "generation_s": round(gen_s, 1),
+                   "l2": "inputs stream from host memory every request"},
+        "serve": {"p50_ms": _pct(s_lat, 50), "p99_ms": _pct(s_lat, 99),
+                  "max_ms": max(s_lat), "throughput_points_s": total / s_span,
+                  "mean_batch": float(np.mean(s_batch)), "max_batch": int(max(s_batch)),
+                  "batches": int(sstats["batches"]), "failed": int(sstats["failed"])},
+        "one_at_a_time": {"p50_ms": _pct(o_lat, 50), "p99_ms": _pct(o_lat, 99),
+                          "max_ms": max(o_lat), "throughput_points_s": total / o_span,
+                          "saturation_points_s": sat_pts / sat_single},
+        "saturation": {"requests": sat_n, "points": sat_pts, "server_s": sat_server,
+                       "one_at_a_time_s": sat_single, "speedup": sat_single / sat_server},
+        "labels_identical": same,
+        "e2e": {"value": value, "unit": "points/s",
+                "h2d_bytes_per_step": int(sum(pts[which[r]].nbytes for r in range(sat_n))),
+                "d2h_bytes_per_step": sat_pts * 4},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -320,11 +464,20 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="zipf2d_10m",
-                    choices=["zipf2d_10m", "aniso3d_20m", "blobs2d_100k", "batch4096"])
+                    choices=["zipf2d_10m", "aniso3d_20m", "blobs2d_100k", "batch4096", "serve"])
     ap.add_argument("--instances", type=int, default=4096,
                     help="batch4096 workload: number of instances")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32band"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--rate", type=float, default=200.0, help="serve: arrivals per second")
+    ap.add_argument("--duration", type=float, default=60.0, help="serve: stream seconds")
+    ap.add_argument("--pool", type=int, default=512, help="serve: distinct request instances")
+    ap.add_argument("--workers", type=int, default=2, help="serve: server worker streams")
+    ap.add_argument("--max-batch", type=int, default=1024, help="serve: requests per batch")
+    ap.add_argument("--hbm-budget-gb", type=float, default=150.0,
+                    help="serve: admission budget for requests in flight")
+    ap.add_argument("--saturation-requests", type=int, default=2000,
+                    help="serve: requests of the closed-loop throughput run")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -350,6 +503,9 @@ def main():
     gdm.load_library()
     if args.workload == "batch4096":
         run_batch(args, rank, world, local, dist)
+        return
+    if args.workload == "serve":
+        run_serve(args, rank, world, local, dist)
         return
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)

@@ -61,6 +61,30 @@ class GdStats(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class GdServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("workers", ctypes.c_int32),
+                ("max_batch", ctypes.c_int32), ("precision", ctypes.c_int32),
+                ("hbm_budget_bytes", ctypes.c_int64)]
+
+
+class GdRequestInfo(ctypes.Structure):
+    _fields_ = [("n_clusters", ctypes.c_int64), ("status", ctypes.c_int32),
+                ("batch_size", ctypes.c_int32), ("submit_ms", ctypes.c_double),
+                ("start_ms", ctypes.c_double), ("done_ms", ctypes.c_double)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class GdServerStats(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_int64) for name in (
+        "submitted", "completed", "failed", "batches", "points", "max_batch_seen", "queued",
+        "inflight_bytes")]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 _lib = None
 
 # (name, restype, argtypes) of every entry point declared in include/gbdbscan.h
@@ -85,6 +109,13 @@ SIGNATURES = [
     ("gd_get_stats", ctypes.c_int, [_P, ctypes.POINTER(GdStats)]),
     ("gd_batch_dbscan", ctypes.c_int, [_P, ctypes.c_int32, _P, _P, ctypes.c_int32, _P, _P,
                                        ctypes.POINTER(GdStats)]),
+    ("gd_server_create", ctypes.c_int, [ctypes.POINTER(GdServerConfig), ctypes.POINTER(_P)]),
+    ("gd_server_destroy", None, [_P]),
+    ("gd_server_submit", ctypes.c_int, [_P, ctypes.POINTER(GdInstance), _P, _P,
+                                        ctypes.POINTER(ctypes.c_int64)]),
+    ("gd_server_wait", ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_double,
+                                      ctypes.POINTER(GdRequestInfo)]),
+    ("gd_server_get_stats", ctypes.c_int, [_P, ctypes.POINTER(GdServerStats)]),
     ("gd_dbscan_noalloc", ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int32, ctypes.c_double,
                                          ctypes.c_int32, ctypes.c_int32, _P,
                                          ctypes.POINTER(ctypes.c_int64), _P]),
@@ -278,3 +309,68 @@ class Context:
         _check(self._lib.gd_dbscan(self._ctx, ctypes.byref(gp), float(eps), int(minpts),
                                    lab.ctypes.data, ctypes.byref(st)))
         return lab, st.as_dict()
+
+
+class Server:
+    """Request server with continuous batching (gd_server_* in the C ABI).
+
+    ``submit(points, eps, minpts)`` queues one clustering request and returns its
+    id; ``wait(id)`` returns (labels, info) once it has run.  Worker threads in
+    the library each own a context and CUDA stream and cluster every admissible
+    queued request together; each request's labels equal those of
+    ``Context.dbscan`` on that request alone."""
+
+    def __init__(self, device: int = 0, workers: int = 2, max_batch: int = 1024,
+                 precision: int = GD_PREC_FP64, hbm_budget_bytes: int = 64 << 30):
+        self._lib = load_library()
+        cfg = GdServerConfig(device, workers, max_batch, precision, hbm_budget_bytes)
+        h = ctypes.c_void_p()
+        _check(self._lib.gd_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._srv = h
+        self._pending = {}  # request id -> (points, labels) kept alive until waited for
+
+    def close(self) -> None:
+        if getattr(self, "_srv", None):
+            self._lib.gd_server_destroy(self._srv)
+            self._srv = None
+            self._pending.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, points, eps: float, minpts: int) -> int:
+        a = np.ascontiguousarray(points, dtype=np.float64)
+        if a.ndim != 2:
+            raise ValueError("points must be (n, dim)")
+        lab = np.empty(max(a.shape[0], 1), dtype=np.int32)
+        inst = GdInstance(a.shape[0], a.shape[1], int(minpts), float(eps))
+        rid = ctypes.c_int64()
+        _check(self._lib.gd_server_submit(self._srv, ctypes.byref(inst), a.ctypes.data,
+                                          lab.ctypes.data, ctypes.byref(rid)))
+        self._pending[rid.value] = (a, lab)
+        return rid.value
+
+    def wait(self, request_id: int, timeout_ms: float = -1.0):
+        info = GdRequestInfo()
+        st = self._lib.gd_server_wait(self._srv, int(request_id), float(timeout_ms),
+                                      ctypes.byref(info))
+        if st == GD_ETIMEOUT:
+            _check(st)  # still running: keep its buffers
+        entry = self._pending.pop(int(request_id), None)
+        _check(st)
+        a, lab = entry
+        return lab[: a.shape[0]].copy(), info.as_dict()
+
+    def stats(self) -> dict:
+        st = GdServerStats()
+        _check(self._lib.gd_server_get_stats(self._srv, ctypes.byref(st)))
+        return st.as_dict()

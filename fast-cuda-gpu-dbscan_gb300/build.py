@@ -26,7 +26,8 @@ CLI = os.path.join(PKG, "gbdbscan_main")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
            "-I", INCLUDE, "-I", CSRC]
-LIB_SOURCES = ["gd_prims.cu", "gd_pipeline.cu", "gd_api.cu", "gd_noalloc.cu", "gd_io.cpp"]
+LIB_SOURCES = ["gd_prims.cu", "gd_pipeline.cu", "gd_api.cu", "gd_noalloc.cu", "gd_io.cpp",
+               "gd_server.cpp"]
 CLI_SOURCES = ["gd_main.cpp"]
 
 

@@ -233,6 +233,22 @@ def poisson_arrivals(seed: int, rate: float, duration: float) -> np.ndarray:
     return np.asarray(out)
 
 
+def serve_stream(seed: int = 0, rate: float = 200.0, duration: float = 60.0,
+                 pool: int = 512, lo: int = 1_000, hi: int = 2_000_000,
+                 workers: int = 0) -> tuple[list[Instance], np.ndarray, np.ndarray]:
+    """The served request stream: Poisson arrivals at ``rate`` per second for
+    ``duration`` seconds, each request one mixture instance (2D/3D, sizes
+    log-uniform in [lo, hi], eps the median 4th-NN distance, minpts in [4, 32]).
+
+    Requests draw their instance uniformly from a pool of ``pool`` generated
+    instances, so a long stream needs no more host memory than the pool.
+    Returns (pool instances, arrival times in seconds, pool index per request)."""
+    insts = batch4096(seed=seed + 1, count=pool, lo=lo, hi=hi, workers=workers)
+    t = poisson_arrivals(seed + 2, rate, duration)
+    which = _rng(seed + 3).integers(0, pool, size=t.shape[0])
+    return insts, t, which
+
+
 def write_csv(path: str, points: np.ndarray) -> None:
     """Write points in the reference's input format (no header, ',' separated)."""
     np.savetxt(path, points, delimiter=",", fmt="%.17g")

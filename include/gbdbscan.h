@@ -162,6 +162,58 @@ gd_status gd_batch_dbscan(gd_ctx* ctx, int32_t count, const gd_instance* inst,
                           const double* coords, int32_t on_device, int32_t* labels,
                           int64_t* cluster_counts, gd_stats* stats);
 
+/* ---- request server with continuous batching ---------------------------- */
+/* No counterpart in the reference.  A server queues clustering requests (one
+   instance each, host buffers) and runs them on `workers` threads, each with
+   its own context and CUDA stream.  A free worker takes every queued request
+   it may admit, first in first out, up to max_batch requests while the
+   estimated device memory of all requests in flight stays within
+   hbm_budget_bytes (a request larger than the budget runs alone), and
+   clusters them together with gd_batch_dbscan.  Each request's labels equal
+   gd_dbscan's on that request alone. */
+typedef struct gd_server gd_server;
+
+typedef struct gd_server_config {
+  int32_t device;
+  int32_t workers;          /* 1..16 */
+  int32_t max_batch;        /* requests per batch, >= 1 */
+  int32_t precision;        /* gd_precision */
+  int64_t hbm_budget_bytes; /* admission limit for requests in flight */
+} gd_server_config;
+
+typedef struct gd_request_info {
+  int64_t n_clusters;
+  int32_t status;     /* gd_status of the batch that ran the request */
+  int32_t batch_size; /* requests in that batch */
+  double submit_ms;   /* times since the server was created */
+  double start_ms;
+  double done_ms;
+} gd_request_info;
+
+typedef struct gd_server_stats {
+  int64_t submitted;
+  int64_t completed;
+  int64_t failed;
+  int64_t batches;
+  int64_t points;
+  int64_t max_batch_seen;
+  int64_t queued;
+  int64_t inflight_bytes;
+} gd_server_stats;
+
+gd_status gd_server_create(const gd_server_config* cfg, gd_server** out);
+/* Finishes every queued request, then stops the workers. */
+void gd_server_destroy(gd_server* srv);
+/* coords (n x dim float64, host) must stay valid and labels (n int32, host)
+   unread until gd_server_wait returns for the request. */
+gd_status gd_server_submit(gd_server* srv, const gd_instance* inst, const double* coords,
+                           int32_t* labels, int64_t* request_id);
+/* Waits for a request (timeout_ms < 0: no limit) and forgets it; returns the
+   request's status, or GD_ETIMEOUT while it is unfinished.  info may be NULL. */
+gd_status gd_server_wait(gd_server* srv, int64_t request_id, double timeout_ms,
+                         gd_request_info* info);
+gd_status gd_server_get_stats(gd_server* srv, gd_server_stats* stats);
+
 /* ---- exact DBSCAN without any memory allocation ------------------------ */
 /* No counterpart in the reference.  For callers that may not allocate device
    memory -- code running while a CUDA graph is captured, real-time loops whose

@@ -93,6 +93,21 @@ def test_context_without_gpu_reports_nodev(built_lib, gd):
     assert e.value.status == 7
 
 
+def test_server_argument_checks(built_lib, gd):
+    import torch
+    with pytest.raises(gd.GdError) as e:
+        gd.Server(0, workers=0)
+    assert e.value.status == 1
+    with pytest.raises(gd.GdError) as e:
+        gd.Server(0, hbm_budget_bytes=0)
+    assert e.value.status == 1
+    if torch.cuda.is_available():
+        return
+    with pytest.raises(gd.GdError) as e:
+        gd.Server(0)
+    assert e.value.status == 7
+
+
 def test_cli_usage(built_lib):
     exe = os.path.join(os.path.dirname(built_lib), "gbdbscan_main")
     r = subprocess.run([exe], capture_output=True, text=True)
