@@ -56,9 +56,9 @@ METRIC = "points/sec at exact labels"
 PHASE_KERNELS = {
     "ms_index": "k_bbox_chunk, k_params_inst, k_layout, k_keys, radix sort, k_gather, "
                 "k_run_flags, scan, k_run_scatter, k_cell_counts, scan, k_row_hash",
-    "ms_core": "k_core_scan + k_core_heavy",
+    "ms_core": "k_core_point + k_core_heavy",
     "ms_union": "k_parent_init, k_union_scan x2, k_union_heavy x2, k_asym_resolve, k_compress",
-    "ms_label": "k_roots, scan, k_label, k_border_scan, k_border_heavy, k_scatter_labels",
+    "ms_label": "k_roots, scan, k_label, k_border_point, k_border_heavy, k_scatter_labels",
 }
 
 
@@ -131,8 +131,10 @@ class ClockSampler:
                 "samples": len(self.rows)}
 
 
-def make_workload(name: str):
+def make_workload(name: str, scale: float = 1.0):
     ds = importlib.import_module(PKG + ".datasets")
+    if scale != 1.0:
+        return getattr(ds, name)(seed=0, scale=scale)
     return getattr(ds, name)(seed=0)
 
 
@@ -490,6 +492,8 @@ def main():
                     help="batch4096 workload: number of instances")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32band"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="single-instance workloads: density-preserving size factor (profiling)")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: arrivals per second")
     ap.add_argument("--duration", type=float, default=60.0, help="serve: stream seconds")
     ap.add_argument("--pool", type=int, default=512, help="serve: distinct request instances")
@@ -530,7 +534,7 @@ def main():
         return
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    inst = make_workload(args.workload)
+    inst = make_workload(args.workload, args.scale)
     n, dim = inst.n, inst.dim
     prec = gdm.GD_PREC_FP64 if args.precision == "fp64" else gdm.GD_PREC_FP32_BAND
 
@@ -646,7 +650,8 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if prec == gdm.GD_PREC_FP64 else "f32+f64band", "data": "synthetic",
-        "config": {"workload": args.workload, "points": n, "dim": dim, "eps": inst.eps,
+        "config": {"workload": args.workload + ("" if args.scale == 1.0 else f" scale {args.scale:g}"),
+                   "points": n, "dim": dim, "eps": inst.eps,
                    "minpts": inst.minpts, "precision": args.precision,
                    "parallelism": f"replicas{world}",
                    "l2": "512 MiB flush write between timed steps; inputs 160+ MB > L2"},

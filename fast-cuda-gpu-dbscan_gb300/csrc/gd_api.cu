@@ -144,6 +144,8 @@ struct gd_ctx {
     B.bbox = static_cast<long long*>(bbox.p);
     B.keys = skeys;
     B.ids = sids;
+    // the sort's other id buffer is free after the sort
+    B.blist = static_cast<uint32_t*>(sids == vals0.p ? vals1.p : vals0.p);
     B.reps = static_cast<int*>(reps.p);
     B.M = dM();
     B.runfl = static_cast<uint32_t*>(runfl.p);

@@ -93,7 +93,36 @@ struct DevParams {
   uint64_t kmask;      // mask of the local key bits
   int32_t LB;          // local key bits of the run (copied from BatchInfo)
   int32_t inst;        // instance index
+  // exact division of local keys by G[1] and G[2] (multiply-high method, see
+  // udiv_magic): multiplier and shift per divisor
+  uint64_t dm[2];
+  int32_t ds[2];
 };
+
+// Division by an invariant integer d >= 1 through a multiply-high (Granlund &
+// Montgomery, "Division by invariant integers using multiplication", 1994,
+// Fig. 4.1, N = 64): with l = ceil(log2 d) and m = floor(2^64 (2^l - d) / d) + 1,
+// q = (t + ((k - t) >> 1)) >> (l - 1), t = mulhi(m, k), for every 64-bit k
+// (l = 0, i.e. d = 1: q = k).  The multiplier is found by long division.
+__host__ __device__ inline void udiv_magic(uint64_t d, uint64_t& m, int32_t& l) {
+  l = 0;
+  while (l < 64 && (1ull << l) < d) ++l;
+  if (l == 0) { m = 0; return; }
+  // floor((2^l - d) * 2^64 / d); exact for d < 2^63 (the remainder never overflows)
+  uint64_t r = (l == 64 ? 0ull : (1ull << l)) - d, q = 0;
+  for (int i = 0; i < 64; ++i) {
+    r <<= 1;
+    q <<= 1;
+    if (r >= d) { r -= d; q |= 1; }
+  }
+  m = q + 1;
+}
+
+__device__ __forceinline__ uint64_t udiv_by(uint64_t k, uint64_t m, int32_t l) {
+  if (l == 0) return k;
+  const uint64_t t = __umul64hi(m, k);
+  return (t + ((k - t) >> 1)) >> (l - 1);
+}
 
 // The predicate constants a cell kernel keeps in registers.
 struct PredParams {
@@ -139,6 +168,8 @@ enum Counter {
   kCtrHeavyUnion,       // cells queued for warp-cooperative link searches
   kCtrHeavyBorder,      // cells queued for warp-cooperative border search
   kCtrCells2D,          // cells of 2D instances (they sort first)
+  kCtrBorder2,          // non-core points of 2D instances listed for the border search
+  kCtrBorder3,          // non-core points of 3D instances (listed from the back)
   kCtrCount = 16
 };
 

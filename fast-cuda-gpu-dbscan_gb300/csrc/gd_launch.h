@@ -46,6 +46,8 @@ struct Bufs {
   int* cellcid = nullptr;       // per rep: cluster id of the cell's core points
   int* lab = nullptr;           // label per sorted position
   int* asym = nullptr;          // kAsymCap (from, to) sorted-position pairs
+  uint32_t* blist = nullptr;    // non-core sorted positions for the border search (n):
+                                // 2D instances' from the front, 3D instances' from the back
   int* hv_cell = nullptr;       // heavy-work list: cell index m (capacity n)
   unsigned long long* hv_mask = nullptr;  // heavy-work list: stencil offsets still open
   unsigned long long* ctr = nullptr;      // gd::Counter

@@ -212,6 +212,7 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   }
   B.keys = skeys;
   B.ids = vb[r];
+  B.blist = vb[1 - r];  // the sort's other id buffer is free after the sort
   B.X = reinterpret_cast<double*>(base + kOffX);
   B.Xf = reinterpret_cast<float*>(base + kOffXf);
   B.runfl = reinterpret_cast<uint32_t*>(base + kOffRunfl);

@@ -6,7 +6,7 @@
 //   thrust::sort_by_key           main.cu:332               -> gdprim::radix_sort_pairs
 //   INDEXING_ADJUSTMENT           indexing.cu:23-51         -> k_run_flags/k_run_scatter/
 //                                                              k_cell_counts + scan / k_row_hash
-//   DBSCAN kernel + searchPoints  dbscan.cu:254-474         -> k_core_scan, k_core_heavy
+//   DBSCAN kernel + searchPoints  dbscan.cu:254-474         -> k_core_point, k_core_heavy
 //   MarkAsCandidate + host merge  dbscan.cu:189-222, 25-187 -> k_union_scan, k_union_heavy,
 //                                                              k_asym_resolve (device union-find)
 //   GetDbscanResult               dbscan.cu:225-251         -> k_roots, k_label, k_border_*,
@@ -137,6 +137,8 @@ __global__ void k_params_inst(const gdl::Bufs B, int K, double mult2, double mul
   if (limit < dense_floor) limit = dense_floor;
   p.sparse = (cells > (double)limit || C > limit) ? 1 : 0;
   p.C = C;
+  udiv_magic((uint64_t)p.G[1], p.dm[0], p.ds[0]);
+  udiv_magic((uint64_t)p.G[2], p.dm[1], p.ds[1]);
   int bits = 0;
   while (bits < 63 && (C - 1) >> bits) ++bits;
   p.key_bits = bits;
@@ -465,13 +467,15 @@ __device__ __forceinline__ CellXYZ<D> decompose(uint64_t key, const DevParams& P
   CellXYZ<D> r;
   uint64_t k = key;
   if (D == 3) {
-    r.c[2] = (int64_t)(k % (uint64_t)P.G[2]);
-    k /= (uint64_t)P.G[2];
+    const uint64_t k2 = udiv_by(k, P.dm[1], P.ds[1]);
+    r.c[2] = (int64_t)(k - k2 * (uint64_t)P.G[2]);
+    k = k2;
   } else {
     r.c[2] = 0;
   }
-  r.c[1] = (int64_t)(k % (uint64_t)P.G[1]);
-  r.c[0] = (int64_t)(k / (uint64_t)P.G[1]);
+  const uint64_t k1 = udiv_by(k, P.dm[0], P.ds[0]);
+  r.c[1] = (int64_t)(k - k1 * (uint64_t)P.G[1]);
+  r.c[0] = (int64_t)k1;
   return r;
 }
 
@@ -910,59 +914,21 @@ __device__ __forceinline__ int classify(const float* u, int ox, int oy, int oz, 
   return 0;
 }
 
-// Per-axis terms of the classification for one point: mx[k][o+2] is the
-// squared largest distance (plus uerr) along axis k from the point to the cell
-// slab at offset o, mn[k][o+2] the squared smallest one (minus uerr).  A cell's
-// test then costs two sums of D table entries.
-template <int D>
-struct PointCls {
-  float mx[D][5];
-  float mn[D][5];
-};
-
-template <int D, class PP>
-__device__ __forceinline__ void point_cls(const float* u, const PP& P, PointCls<D>& pc) {
-#pragma unroll
-  for (int k = 0; k < D; ++k)
-#pragma unroll
-    for (int o = -2; o <= 2; ++o) {
-      const float a = u[k] - (float)o;
-      const float b = a - 1.0f;
-      const float mx = fmaxf(fabsf(a), fabsf(b)) + P.uerr;
-      const float mn = fmaxf(fmaxf(-a, b) - P.uerr, 0.0f);
-      pc.mx[k][o + 2] = mx * mx;
-      pc.mn[k][o + 2] = mn * mn;
-    }
-}
-
-template <int D, class PP>
-__device__ __forceinline__ int cls_of(const PointCls<D>& pc, int ox, int oy, int oz, const PP& P) {
-  float smax = pc.mx[0][ox + 2] + pc.mx[1][oy + 2];
-  float smin = pc.mn[0][ox + 2] + pc.mn[1][oy + 2];
-  if (D == 3) {
-    smax += pc.mx[2][oz + 2];
-    smin += pc.mn[2][oz + 2];
-  }
-  if (smax <= P.thr_in) return 1;
-  if (smin >= P.thr_out) return -1;
-  return 0;
-}
-
-// ------------------------------------------------- thread-per-cell front ends
-// Most cells need little work: isolated noise points whose stencil holds fewer
+// ------------------------------------------------------- thread front ends
+// Most work items need little: isolated noise points whose stencil holds fewer
 // than minpts points, cells whose neighbour links are found by the first test,
-// border points with a handful of candidate cores.  The *_scan kernels give one
-// thread to each cell and finish those cases inline (bounded work per thread);
-// a cell that needs more is appended to the heavy list and handled by the
+// border points with a handful of candidate cores.  The front-end kernels give
+// one thread to each point (k_core_point, k_border_point) or core cell
+// (k_union_scan) and finish those cases inline (bounded work per thread); a
+// cell that needs more is appended to the heavy list and handled by the
 // warp-cooperative *_heavy kernel that follows.  The stencil is walked row by
 // row (5 rows in 2D, 25 in 3D, own row first); a row is one contiguous range of
 // sorted points, and its non-empty cells are visited through the run structure,
 // so empty cells cost nothing.
 constexpr int kScanThreadsPerBlock = 256;
-constexpr int kInlineCoreTests = 256;    // pair tests one thread spends on a cell's points
+constexpr int kInlineCoreTests = 256;    // pair tests one thread spends on a point's core count
 constexpr int kInlineLinkTests = 48;     // tests before a link search goes to a warp
-constexpr int kInlineBorderTests = 160;  // tests one thread spends on a cell's borders
-constexpr int kDeferCells = 8;           // undecided cells queued by the core count
+constexpr int kInlineBorderTests = 160;  // tests one thread spends on a border point
 
 // warp-aggregated append to the heavy list (all 32 lanes must call it)
 __device__ __forceinline__ void heavy_push(const gdl::Bufs& B, int slot, bool push, int64_t m,
@@ -1017,103 +983,162 @@ __device__ __forceinline__ int cell_end(const gdl::Bufs& B, int q) {
   return B.reps[B.runpos[q] + 1];
 }
 
+// Squared largest / smallest distance (plus / minus the position error) along
+// one axis from a point at in-cell position a (cell units) to the cell slab at
+// offset o.
+template <class PP>
+__device__ __forceinline__ void axis_terms(float a, int o, const PP& P, float& mx2, float& mn2) {
+  const float x = a - (float)o, y = x - 1.0f;
+  const float mx = fmaxf(fabsf(x), fabsf(y)) + P.uerr;
+  const float mn = fmaxf(fmaxf(-x, y) - P.uerr, 0.0f);
+  mx2 = mx * mx;
+  mn2 = mn * mn;
+}
+
+// a[d + 2] for d in [-2, 2], by selects (the array stays in registers)
+__device__ __forceinline__ float sel5(const float (&a)[5], int d) {
+  float r = a[0];
+  r = d == -1 ? a[1] : r;
+  r = d == 0 ? a[2] : r;
+  r = d == 1 ? a[3] : r;
+  r = d == 2 ? a[4] : r;
+  return r;
+}
+
+constexpr int kCoreQueue = 8;  // undecided cells a point queues before testing them
+
+// Core flags, one thread per point.  Neighbouring lanes hold neighbouring
+// sorted points, mostly of one cell, so they walk the same stencil rows in
+// step: their loads coincide and their branches agree.  A point of a cell with
+// at least minpts points is core at once.  Otherwise the walk goes row by row,
+// own row first: with cell classification, cells wholly inside eps count
+// without tests, cells wholly outside are skipped, and undecided cells are
+// queued (shared memory) and tested only when the queue fills or the walk ends
+// short of minpts.  The classification's per-axis terms are formed per row for
+// the fixed axes and per point for the last axis (five values in registers).
+// A point whose tests pass the budget sends its cell to the warp kernel,
+// which recomputes the whole cell.  Per-cell core counts and smallest core
+// indices are warp-aggregated atomics (cleared before the launch).
 template <int D, bool F32, bool KEY64>
-__global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_scan(const gdl::Bufs B, int64_t n) {
+__global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_point(const gdl::Bufs B, int64_t n) {
+  __shared__ int2 sq[kCoreQueue][kScanThreadsPerBlock];
   const OffTab& T = kRows[D - 2];
   const int lane = threadIdx.x & 31;
   const int LB = B.Bi->LB;
   int64_t mlo, mhi;
   dim_range<D>(B, mlo, mhi);
+  const int64_t plo = B.reps[mlo], phi = B.reps[mhi];
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   Tally t;
-  for (int64_t m0 = mlo + (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); m0 < mhi;
-       m0 += stride) {
-    const int64_t m = m0 + lane;
-    bool push = false;
-    if (m < mhi) {
-      const int b = B.reps[m], e = B.reps[m + 1], sz = e - b;
+  unsigned long long dense = 0;
+  for (int64_t i0 = plo + (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); i0 < phi;
+       i0 += stride) {
+    const int64_t i = i0 + lane;
+    const bool valid = i < phi;
+    int m = -1, b = 0;
+    bool isc = false, over = false;
+    if (valid) {
+      m = (int)(B.runpos[i] + B.runfl[i]) - 1;
+      b = B.reps[m];
+      const int e = B.reps[m + 1], sz = e - b;
       const CellCtx cx = cell_ctx<KEY64>(B, b, LB);
       const DevParams& P = *cx.P;
       const PredParams Q = pred_params(P);
       if (sz >= Q.minpts) {
-        push = true;  // dense: the warp kernel marks it
+        isc = true;
+        if (i == b) ++dense;
       } else {
         const GridView gv = view_of(B, P);
         const bool prune = Q.prune != 0;
         RowWalk<D> rw;
         rw.init(decompose<D>(cx.local, P), P);
-        float o[D];
-        if (prune) cell_origin32<D>(rw.cc, P, o);
-        int ncore = 0, mn = INT_MAX;
-        int budget = kInlineCoreTests;
-        for (int i = b; i < e && !push; ++i) {
-          double px[D];
-          float pf[D], u[D];
-          load_point<D, F32>(px, pf, B, n, i, prune);
-          PointCls<D> pc;
-          if (prune) {
-            frac_pos<D>(pf, o, Q, u);
-            point_cls<D>(u, Q, pc);
-          }
-          // One walk, own row first: cells wholly inside count at once, cells
-          // wholly outside are skipped, undecided cells are queued and tested
-          // only when the queue fills or the walk ends short of minpts.
-          int cnt = 0, ptot = 0, nq = 0;
-          int qb[kDeferCells], qe_[kDeferCells];
-          auto flush = [&](void) {
-            for (int j = 0; j < nq && cnt < Q.minpts && !push; ++j)
-              for (int qq = qb[j]; qq < qe_[j] && cnt < Q.minpts; ++qq) {
-                if (budget-- == 0) {
-                  push = true;  // too much for one thread
-                  break;
-                }
-                Cand<D, F32> cd;
-                load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
-                cnt += pair_test<D, F32>(px, pf, cd, B.X, n, qq, true, Q, t) ? 1 : 0;
+        double px[D];
+        float pf[D];
+        load_point<D, F32>(px, pf, B, n, i, prune);
+        float u[D], lmx[5], lmn[5];
+        if (prune) {
+          float o[D];
+          cell_origin32<D>(rw.cc, P, o);
+          frac_pos<D>(pf, o, Q, u);
+#pragma unroll
+          for (int j = 0; j < 5; ++j) axis_terms(u[D - 1], j - 2, Q, lmx[j], lmn[j]);
+        }
+        int cnt = 0, ptot = 0, nq = 0, budget = kInlineCoreTests;
+        auto flush = [&](void) {
+          for (int j = 0; j < nq && cnt < Q.minpts && !over; ++j) {
+            const int2 c = sq[j][threadIdx.x];
+            for (int qq = c.x; qq < c.y && cnt < Q.minpts; ++qq) {
+              if (budget-- == 0) {
+                over = true;
+                break;
               }
-            nq = 0;
-          };
-          for (int r = 0; r < T.n && cnt < Q.minpts && !push; ++r) {
-            const int64_t rk = rw.rowkey(T, r, P);
-            if (rk < 0) continue;
-            const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
-            for (int q = sp.x; q < sp.y && cnt < Q.minpts && !push;) {
-              const int qe = cell_end<KEY64>(B, q);
-              int cls = 0;
-              if (prune) {
-                const int d = (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
-                cls = D == 3 ? cls_of<D>(pc, T.o[r][0], T.o[r][1], d, Q)
-                             : cls_of<D>(pc, T.o[r][0], d, 0, Q);
-              }
-              if (cls > 0) {
-                cnt += qe - q;
-              } else if (cls == 0) {
-                if (nq == kDeferCells) flush();
-                qb[nq] = q;
-                qe_[nq] = qe;
-                ++nq;
-                ptot += qe - q;
-              }
-              q = qe;
+              Cand<D, F32> cd;
+              load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
+              cnt += pair_test<D, F32>(px, pf, cd, B.X, n, qq, true, Q, t) ? 1 : 0;
             }
           }
-          if (cnt < Q.minpts && cnt + ptot >= Q.minpts) flush();
-          const bool isc = cnt >= Q.minpts;
-          B.core[i] = isc ? 1 : 0;
-          if (isc) {
-            ++ncore;
-            mn = min(mn, (int)B.ids[i]);
+          nq = 0;
+        };
+        for (int r = 0; r < T.n && cnt < Q.minpts && !over; ++r) {
+          const int64_t rk = rw.rowkey(T, r, P);
+          if (rk < 0) continue;
+          float rmx = 0.0f, rmn = 0.0f;
+          if (prune) {
+#pragma unroll
+            for (int k = 0; k < D - 1; ++k) {
+              float a2, b2;
+              axis_terms(u[k], (int)T.o[r][k], Q, a2, b2);
+              rmx += a2;
+              rmn += b2;
+            }
+          }
+          const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
+          for (int q = sp.x; q < sp.y && cnt < Q.minpts && !over;) {
+            const int qe = cell_end<KEY64>(B, q);
+            int cls = 0;
+            if (prune) {
+              const int d =
+                  (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
+              const float smax = rmx + sel5(lmx, d), smin = rmn + sel5(lmn, d);
+              cls = smax <= Q.thr_in ? 1 : (smin >= Q.thr_out ? -1 : 0);
+            }
+            if (cls > 0) {
+              cnt += qe - q;
+            } else if (cls == 0) {
+              if (nq == kCoreQueue) flush();
+              sq[nq][threadIdx.x] = make_int2(q, qe);
+              ++nq;
+              ptot += qe - q;
+            }
+            q = qe;
           }
         }
-        if (!push) {
-          B.cellcore[b] = ncore;
-          B.cellmin[b] = mn;
-        }
+        if (!over && cnt < Q.minpts && cnt + ptot >= Q.minpts) flush();
+        isc = !over && cnt >= Q.minpts;
+      }
+      if (!over) B.core[i] = isc ? 1 : 0;
+    }
+    // per-cell core count and smallest core index, one atomic pair per cell
+    // and warp
+    const unsigned cm = __ballot_sync(kFull, isc);
+    if (isc) {
+      const unsigned grp = __match_any_sync(cm, b);
+      const unsigned mn = __reduce_min_sync(grp, (unsigned)B.ids[i]);
+      if (lane == __ffs(grp) - 1) {
+        atomicAdd(B.cellcore + b, __popc(grp));
+        atomicMin(reinterpret_cast<unsigned*>(B.cellmin) + b, mn);
       }
     }
-    heavy_push(B, kCtrHeavyCore, push, m, 0);
+    // cells with an undecided point, once per warp
+    const unsigned om = __ballot_sync(kFull, over);
+    bool lead = false;
+    if (over) lead = lane == __ffs(__match_any_sync(om, m)) - 1;
+    heavy_push(B, kCtrHeavyCore, lead, m, 0);
   }
   flush_tally(t, B.ctr);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) dense += __shfl_xor_sync(kFull, dense, o);
+  if (lane == 0 && dense) atomicAdd(B.ctr + kCtrDenseCells, dense);
 }
 
 // Bounded link search between the core points of cells A and B by one thread:
@@ -1252,84 +1277,102 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
   flush_tally(t, B.ctr);
 }
 
+// Border labels, one thread per listed non-core point (k_label lists them,
+// consecutive lanes holding consecutive sorted points).  Each point walks its
+// stencil and takes the smallest cluster id among the cells whose core points
+// have it in their neighbourhood (centre = the core point, as the reference's
+// expansion queries from the core point).  Cells whose id cannot improve on
+// the best so far are skipped; with classification, a cell wholly inside eps
+// gives its id without tests and one wholly outside is skipped.  A point whose
+// tests pass the budget sends its cell to the warp kernel.
 template <int D, bool F32, bool KEY64>
-__global__ void __launch_bounds__(kScanThreadsPerBlock) k_border_scan(const gdl::Bufs B, int64_t n) {
+__global__ void __launch_bounds__(kScanThreadsPerBlock) k_border_point(const gdl::Bufs B, int64_t n) {
   const OffTab& T = kRows[D - 2];
   const int lane = threadIdx.x & 31;
   const int LB = B.Bi->LB;
-  int64_t mlo, mhi;
-  dim_range<D>(B, mlo, mhi);
+  const int64_t L = (int64_t)B.ctr[D == 2 ? kCtrBorder2 : kCtrBorder3];
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   Tally t;
-  for (int64_t m0 = mlo + (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); m0 < mhi;
-       m0 += stride) {
-    const int64_t m = m0 + lane;
-    bool push = false;
-    if (m < mhi) {
-      const int b = B.reps[m], e = B.reps[m + 1];
-      const int nnc = (e - b) - B.cellcore[b];
-      if (nnc > 0) {
-        const CellCtx cx = cell_ctx<KEY64>(B, b, LB);
-        const DevParams& P = *cx.P;
-        const PredParams Q = pred_params(P);
-        const GridView gv = view_of(B, P);
-        const bool prune = Q.prune != 0;
-        RowWalk<D> rw;
-        rw.init(decompose<D>(cx.local, P), P);
+  for (int64_t j0 = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); j0 < L; j0 += stride) {
+    const int64_t j = j0 + lane;
+    int m = -1;
+    bool over = false;
+    if (j < L) {
+      const int64_t i = D == 2 ? (int64_t)B.blist[j] : (int64_t)B.blist[n - 1 - j];
+      m = (int)(B.runpos[i] + B.runfl[i]) - 1;
+      const int b = B.reps[m];
+      const CellCtx cx = cell_ctx<KEY64>(B, b, LB);
+      const DevParams& P = *cx.P;
+      const PredParams Q = pred_params(P);
+      const GridView gv = view_of(B, P);
+      const bool prune = Q.prune != 0;
+      RowWalk<D> rw;
+      rw.init(decompose<D>(cx.local, P), P);
+      double px[D];
+      float pf[D];
+      load_point<D, F32>(px, pf, B, n, i, prune);
+      float u[D], lmx[5], lmn[5];
+      if (prune) {
         float o[D];
-        if (prune) cell_origin32<D>(rw.cc, P, o);
-        int budget = kInlineBorderTests;
-        for (int i = b; i < e && !push; ++i) {
-          if (B.core[i]) continue;
-          double px[D];
-          float pf[D], u[D];
-          load_point<D, F32>(px, pf, B, n, i, prune);
-          PointCls<D> pc;
-          if (prune) {
-            frac_pos<D>(pf, o, Q, u);
-            point_cls<D>(u, Q, pc);
+        cell_origin32<D>(rw.cc, P, o);
+        frac_pos<D>(pf, o, Q, u);
+#pragma unroll
+        for (int k = 0; k < 5; ++k) axis_terms(u[D - 1], k - 2, Q, lmx[k], lmn[k]);
+      }
+      int best = INT_MAX, budget = kInlineBorderTests;
+      for (int r = 0; r < T.n && !over; ++r) {
+        const int64_t rk = rw.rowkey(T, r, P);
+        if (rk < 0) continue;
+        float rmx = 0.0f, rmn = 0.0f;
+        if (prune) {
+#pragma unroll
+          for (int k = 0; k < D - 1; ++k) {
+            float a2, b2;
+            axis_terms(u[k], (int)T.o[r][k], Q, a2, b2);
+            rmx += a2;
+            rmn += b2;
           }
-          int best = INT_MAX;
-          for (int r = 0; r < T.n && !push; ++r) {
-            const int64_t rk = rw.rowkey(T, r, P);
-            if (rk < 0) continue;
-            const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
-            for (int q = sp.x; q < sp.y && !push;) {
-              const int qe = cell_end<KEY64>(B, q);
-              const int cB = B.cellcore[q] > 0 ? B.cellcid[q] : INT_MAX;
-              if (cB < best) {
-                int cls = 0;
-                if (prune) {
-                  const int d = (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
-                  cls = D == 3 ? cls_of<D>(pc, T.o[r][0], T.o[r][1], d, Q)
-                               : cls_of<D>(pc, T.o[r][0], d, 0, Q);
+        }
+        const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
+        for (int q = sp.x; q < sp.y && !over;) {
+          const int qe = cell_end<KEY64>(B, q);
+          const int cB = B.cellcore[q] > 0 ? B.cellcid[q] : INT_MAX;
+          if (cB < best) {
+            int cls = 0;
+            if (prune) {
+              const int d =
+                  (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
+              const float smax = rmx + sel5(lmx, d), smin = rmn + sel5(lmn, d);
+              cls = smax <= Q.thr_in ? 1 : (smin >= Q.thr_out ? -1 : 0);
+            }
+            if (cls > 0) {
+              best = cB;  // every point of that cell, a core among them, is in reach
+            } else if (cls == 0) {
+              for (int qq = q; qq < qe; ++qq) {
+                if (!B.core[qq]) continue;
+                if (budget-- == 0) {
+                  over = true;
+                  break;
                 }
-                if (cls > 0) {
-                  best = cB;  // every point of that cell, a core among them, is in reach
-                } else if (cls == 0) {
-                  for (int qq = q; qq < qe; ++qq) {
-                    if (!B.core[qq]) continue;
-                    if (budget-- == 0) {
-                      push = true;  // too much for one thread
-                      break;
-                    }
-                    Cand<D, F32> cd;
-                    load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
-                    if (pair_test<D, F32>(px, pf, cd, B.X, n, qq, false, Q, t)) {
-                      best = cB;
-                      break;
-                    }
-                  }
+                Cand<D, F32> cd;
+                load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
+                if (pair_test<D, F32>(px, pf, cd, B.X, n, qq, false, Q, t)) {
+                  best = cB;
+                  break;
                 }
               }
-              q = qe;
             }
           }
-          if (!push && best != INT_MAX) B.lab[i] = best;
+          q = qe;
         }
       }
+      if (!over && best != INT_MAX) B.lab[i] = best;
     }
-    heavy_push(B, kCtrHeavyBorder, push, m, 0);
+    // cells with an undecided point, once per warp
+    const unsigned om = __ballot_sync(kFull, over);
+    bool lead = false;
+    if (over) lead = lane == __ffs(__match_any_sync(om, m)) - 1;
+    heavy_push(B, kCtrHeavyBorder, lead, m, 0);
   }
   flush_tally(t, B.ctr);
 }
@@ -1610,16 +1653,40 @@ __global__ void k_roots(const gdl::Bufs B) {
 template <bool KEY64>
 __global__ void k_label(const gdl::Bufs B, int64_t n) {
   const int LB = B.Bi->LB;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int b = rep_of(B, i);
-    int cl = INT_MAX;
-    if (B.cellcore[b] > 0) {
-      const int64_t pt_off = B.Pv[(int)(key_at<KEY64>(B, i) >> LB)].pt_off;
-      cl = (int)(B.Fmark[B.cellmin[uf_find(B.parent, b)]] - B.Fmark[pt_off]);
+  const int lane = threadIdx.x & 31;
+  // first sorted position of a 3D instance (n when there is none)
+  const int64_t p3 = B.reps[(int64_t)B.ctr[kCtrCells2D]];
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); i0 < n;
+       i0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = i0 + lane;
+    bool nc = false;
+    if (i < n) {
+      const int b = rep_of(B, i);
+      int cl = INT_MAX;
+      if (B.cellcore[b] > 0) {
+        const int64_t pt_off = B.Pv[(int)(key_at<KEY64>(B, i) >> LB)].pt_off;
+        cl = (int)(B.Fmark[B.cellmin[uf_find(B.parent, b)]] - B.Fmark[pt_off]);
+      }
+      if (i == b) B.cellcid[b] = cl;
+      nc = !B.core[i];
+      B.lab[i] = nc ? kNoise : cl;
     }
-    if (i == b) B.cellcid[b] = cl;
-    B.lab[i] = B.core[i] ? cl : kNoise;
+    // list the non-core points for the border search: 2D instances' from the
+    // front, 3D instances' from the back
+    const bool is3 = i >= p3;
+    const unsigned b2 = __ballot_sync(kFull, nc && !is3), b3 = __ballot_sync(kFull, nc && is3);
+    unsigned long long at2 = 0, at3 = 0;
+    if (lane == 0) {
+      if (b2) at2 = atomicAdd(B.ctr + kCtrBorder2, (unsigned long long)__popc(b2));
+      if (b3) at3 = atomicAdd(B.ctr + kCtrBorder3, (unsigned long long)__popc(b3));
+    }
+    at2 = __shfl_sync(kFull, at2, 0);
+    at3 = __shfl_sync(kFull, at3, 0);
+    if (nc) {
+      const unsigned below = (1u << lane) - 1u;
+      if (!is3) B.blist[at2 + __popc(b2 & below)] = (uint32_t)i;
+      else B.blist[n - 1 - (int64_t)(at3 + __popc(b3 & below))] = (uint32_t)i;
+    }
   }
 }
 
@@ -1843,7 +1910,10 @@ int launches_per_cell_phase(int dims) { return ((dims & 1) ? 1 : 0) + ((dims & 2
 
 void core(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s) {
   cudaMemsetAsync(B.ctr + kCtrHeavyCore, 0, 8, s);
-  GD_LAUNCH_DIMS(dims, f32, key64, k_core_scan, sms * 8, kScanThreadsPerBlock, B, n);
+  // per-cell core counts (0) and smallest core indices (0xffffffff as unsigned)
+  cudaMemsetAsync(B.cellcore, 0, (size_t)n * 4, s);
+  cudaMemsetAsync(B.cellmin, 0xff, (size_t)n * 4, s);
+  GD_LAUNCH_DIMS(dims, f32, key64, k_core_point, sms * 8, kScanThreadsPerBlock, B, n);
   GD_LAUNCH_DIMS(dims, f32, key64, k_core_heavy, sms * 8, kCellThreads, B, n);
 }
 
@@ -1863,13 +1933,14 @@ void roots(const Bufs& B, int64_t n, int sms, cudaStream_t s) {
 }
 
 void label(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) {
+  cudaMemsetAsync(B.ctr + kCtrBorder2, 0, 16, s);
   if (key64) k_label<true><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
   else k_label<false><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
 }
 
 void border(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s) {
   cudaMemsetAsync(B.ctr + kCtrHeavyBorder, 0, 8, s);
-  GD_LAUNCH_DIMS(dims, f32, key64, k_border_scan, sms * 8, kScanThreadsPerBlock, B, n);
+  GD_LAUNCH_DIMS(dims, f32, key64, k_border_point, sms * 8, kScanThreadsPerBlock, B, n);
   GD_LAUNCH_DIMS(dims, f32, key64, k_border_heavy, sms * 8, kCellThreads, B, n);
 }
 
