@@ -152,6 +152,10 @@ struct gd_ctx {
     B.runpos = static_cast<uint32_t*>(runpos.p);
     B.start = static_cast<uint32_t*>(table.p);
     B.occ = static_cast<uint32_t*>(occ.p);
+    if (bi.table_total) {
+      B.occ_words = bi.table_total / 32 + 1;
+      B.cocc = B.occ + B.occ_words;  // second half of the occupancy buffer
+    }
     B.hkeys = static_cast<unsigned long long*>(hkeys.p);
     B.hvals = static_cast<uint32_t*>(hvals.p);
     B.hmask = hmask;
@@ -238,7 +242,7 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
   if (ctx->xf) GD_TRY(ctx->ensure(ctx->Xf, (size_t)n * maxd * 4, "f32 coordinates"));
   if (bi.table_total) {
     GD_TRY(ctx->ensure(ctx->table, bi.table_total * 4, "cell tables"));
-    GD_TRY(ctx->ensure(ctx->occ, (bi.table_total / 32 + 1) * 4, "cell occupancy"));
+    GD_TRY(ctx->ensure(ctx->occ, 2 * (bi.table_total / 32 + 1) * 4, "cell occupancy"));
   }
   uint64_t hcap = 1024;
   if (bi.any_sparse) {
@@ -332,8 +336,8 @@ gd_status expand_run(gd_ctx* ctx) {
   GD_CUDA(cudaGetLastError(), "expand launch");
   const int cp = gdl::launches_per_cell_phase(ctx->dims);
   // core, parent init, 2 union passes, compress, merge replay, roots, scan,
-  // label, border
-  ctx->launches += 2 * cp + 1 + 4 * cp + 1 + 1 + 1 + 3 + 1 + 2 * cp;
+  // label, core occupancy (with tables), border
+  ctx->launches += 2 * cp + 1 + 4 * cp + 1 + 1 + 1 + 3 + 1 + (ctx->bi.table_total ? 1 : 0) + 2 * cp;
   ctx->stage = 2;
   return GD_OK;
 }

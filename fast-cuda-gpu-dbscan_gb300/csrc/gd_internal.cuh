@@ -76,11 +76,13 @@ struct DevParams {
   float eps2_hi32;     // float32 d2 above this: certainly not a neighbour
   int64_t G[3];        // cells per dimension
   uint64_t C;          // total cells (G0*G1[*G2])
+  uint64_t rows;       // rows: C / G[dim-1]
   int32_t dim;
   int32_t minpts;
   int32_t key_bits;
   int32_t flags;       // kFlag*
-  int32_t sparse;      // 1: hash of occupied cells (64-bit keys); 0: dense table
+  int32_t sparse;      // grid lookup: 0 dense cell table; 2 dense row table (cells
+                       // inside a row by binary search); 1 hash of occupied rows
   int32_t prune;       // 1: cell-level inside/outside classification enabled
   float inv_f32;       // fl32(1 / f)
   float uerr;          // bound on the error of a point's in-cell position (cell units)
@@ -146,6 +148,10 @@ __device__ __forceinline__ PredParams pred_params(const DevParams& P) {
   q.prune = P.prune;
   return q;
 }
+
+// A grid too large for a cell table takes a table of its rows when there are at
+// most this many times the cell-table limit's points-per-cell rows per point.
+constexpr uint64_t kRowTablePerCell = 8;
 
 constexpr int kFlagNonFinite = 1;     // NaN or Inf coordinate
 constexpr int kFlagGridTooLarge = 2;  // keys would not fit 62 bits

@@ -31,7 +31,10 @@ struct Bufs {
   uint32_t* runfl = nullptr;    // 1 where a cell starts (per sorted position)
   uint32_t* runpos = nullptr;   // exclusive scan of runfl: cell index = runpos+runfl-1
   uint32_t* start = nullptr;    // dense grids: cell tables of all dense instances
-  uint32_t* occ = nullptr;      // dense grids: occupancy bit per cell-table entry
+  uint32_t* occ = nullptr;      // occupancy bit per cell- or row-table entry
+  uint32_t* cocc = nullptr;     // the same for entries holding a core point (after the
+                                // core phase; border search)
+  uint64_t occ_words = 0;       // words of occ (and of cocc); 0 without tables
   unsigned long long* hkeys = nullptr;  // sparse grids: row hash slots (key of the row's first cell)
   uint32_t* hvals = nullptr;            // sparse grids: row hash slots (begin, end) pairs
   uint32_t hmask = 0;                   // sparse grids: slots - 1

@@ -59,7 +59,7 @@ constexpr size_t kOffX = kOffVals1 + up(kMaxPoints * 4);
 constexpr size_t kOffXf = kOffX + up(kMaxPoints * 3 * 8);
 constexpr size_t kOffTable = kOffXf + up(kMaxPoints * 3 * 4);
 constexpr size_t kOffOcc = kOffTable + up((kTableCells + 1) * 4);
-constexpr size_t kOffHkeys = kOffOcc + up((kTableCells / 32 + 1) * 4);
+constexpr size_t kOffHkeys = kOffOcc + up(2 * (kTableCells / 32 + 1) * 4);  // occupancy, core occupancy
 constexpr size_t kOffHvals = kOffHkeys + up(kHashSlots * 8);
 constexpr size_t kOffReps = kOffHvals + up(kHashSlots * 8);
 constexpr size_t kOffRunfl = kOffReps + up((kMaxPoints + 1) * 4);
@@ -220,6 +220,10 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   B.reps = reinterpret_cast<int*>(base + kOffReps);
   B.start = reinterpret_cast<uint32_t*>(base + kOffTable);
   B.occ = reinterpret_cast<uint32_t*>(base + kOffOcc);
+  if (bi.table_total) {
+    B.occ_words = bi.table_total / 32 + 1;
+    B.cocc = B.occ + B.occ_words;
+  }
   B.hkeys = reinterpret_cast<unsigned long long*>(base + kOffHkeys);
   B.hvals = reinterpret_cast<uint32_t*>(base + kOffHvals);
   B.hmask = (uint32_t)(kHashSlots - 1);

@@ -135,8 +135,16 @@ __global__ void k_params_inst(const gdl::Bufs B, int K, double mult2, double mul
   if (!(cells < 4.0e18)) fl |= kFlagGridTooLarge;
   uint64_t limit = (uint64_t)I.n * dense_per_point;
   if (limit < dense_floor) limit = dense_floor;
-  p.sparse = (cells > (double)limit || C > limit) ? 1 : 0;
   p.C = C;
+  p.rows = C / (uint64_t)p.G[D - 1];
+  if (!(cells > (double)limit || C > limit)) {
+    p.sparse = 0;
+  } else {
+    // a grid too large for a cell table may still take a table of its rows
+    uint64_t rlimit = (uint64_t)I.n * dense_per_point * kRowTablePerCell;
+    if (rlimit < dense_floor) rlimit = dense_floor;
+    p.sparse = (fl & kFlagGridTooLarge) || p.rows > rlimit ? 1 : 2;
+  }
   udiv_magic((uint64_t)p.G[1], p.dm[0], p.ds[0]);
   udiv_magic((uint64_t)p.G[2], p.dm[1], p.ds[1]);
   int bits = 0;
@@ -217,7 +225,7 @@ __global__ void __launch_bounds__(1024) k_layout(const gdl::Bufs B, int K) {
     const DevParams& p = B.Pv[i];
     if (p.n > 0) lb = max(lb, p.key_bits);
     fl |= p.flags;
-    sp |= p.sparse;
+    sp |= p.sparse == 1;
     xf |= p.prune;
     if (p.n > 0 && !(p.eps2_lo32 > 0.0f)) xf |= 2;
     md = max(md, p.dim);
@@ -271,9 +279,10 @@ __global__ void __launch_bounds__(1024) k_layout(const gdl::Bufs B, int K) {
   for (int base = 0; base < K; base += 1024) {
     const int i = base + threadIdx.x;
     unsigned long long v = 0;
-    // a dense instance's table has C+1 entries; a sparse instance keeps one
-    // entry holding its point count, so the scan stays in sorted-position units
-    if (i < K) v = B.Pv[i].sparse ? 1 : B.Pv[i].C + 1;
+    // a dense instance's table has C+1 entries (rows+1 for a row table); a
+    // hashed instance keeps one entry holding its point count, so the scan
+    // stays in sorted-position units
+    if (i < K) v = B.Pv[i].sparse == 1 ? 1 : (B.Pv[i].sparse == 2 ? B.Pv[i].rows : B.Pv[i].C) + 1;
     unsigned long long inc = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -392,22 +401,31 @@ __global__ void k_split(const gdl::Bufs B) {
 }
 
 // Cell counts into the instances' table slices (scanned afterwards into start
-// positions).  A sparse instance's one-entry slice holds its point count.
+// positions): per cell for a cell table, per row for a row table.  A hashed
+// instance's one-entry slice holds its point count.
 template <class Key>
 __global__ void k_cell_counts(const gdl::Bufs B) {
   const Key* keys = static_cast<const Key*>(B.keys);
   const int LB = B.Bi->LB;
   const int K = B.Bi->K;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x)
-    if (B.Pv[i].sparse) B.start[B.Pv[i].table_off] = (uint32_t)B.Pv[i].n;
+    if (B.Pv[i].sparse == 1) B.start[B.Pv[i].table_off] = (uint32_t)B.Pv[i].n;
   const int64_t M = *B.M;
   for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
        m += (int64_t)gridDim.x * blockDim.x) {
     const int b = B.reps[m], e = B.reps[m + 1];
     const Key key = keys[b];
     const DevParams& P = B.Pv[inst_of(key, LB)];
-    if (P.sparse) continue;
-    const uint64_t idx = P.table_off + ((uint64_t)key & P.kmask);
+    if (P.sparse == 1) continue;
+    const uint64_t local = (uint64_t)key & P.kmask;
+    if (P.sparse == 2) {
+      const int a = P.dim - 2;
+      const uint64_t idx = P.table_off + udiv_by(local, P.dm[a], P.ds[a]);
+      atomicAdd(B.start + idx, (uint32_t)(e - b));
+      atomicOr(B.occ + (idx >> 5), 1u << (idx & 31));
+      continue;
+    }
+    const uint64_t idx = P.table_off + local;
     B.start[idx] = (uint32_t)(e - b);
     atomicOr(B.occ + (idx >> 5), 1u << (idx & 31));
   }
@@ -427,7 +445,7 @@ __global__ void k_row_hash(const gdl::Bufs B) {
     const uint64_t key = (uint64_t)keys[B.reps[m]];
     const int inst = (int)(key >> LB);
     const DevParams& P = B.Pv[inst];
-    if (!P.sparse) continue;
+    if (P.sparse != 1) continue;
     const uint64_t Gl = (uint64_t)P.G[P.dim - 1];
     const uint64_t hi = key & ~P.kmask;
     const uint64_t local = key & P.kmask;
@@ -634,23 +652,31 @@ __device__ __forceinline__ int warp_min_i32(int v) {
 struct GridView {
   const uint32_t* start;
   const uint32_t* occ;
+  const uint32_t* cocc;    // core occupancy (valid in the border search only)
   const unsigned long long* hkeys;
   const uint32_t* hvals;   // per slot: row begin, row end
   const int* reps;
   const void* keys;
   uint32_t hmask;
-  int sparse;
+  int sparse;              // DevParams::sparse
   int key64;
   uint64_t table_off;
   uint64_t hi;             // instance id << LB
   int64_t Gl;              // cells along the last axis
+  uint64_t glm;            // division by Gl (udiv_by)
+  int32_t gls;
 
   __device__ __forceinline__ uint64_t gkey(int64_t i) const {
     return key64 ? static_cast<const unsigned long long*>(keys)[i]
                  : (uint64_t) static_cast<const uint32_t*>(keys)[i];
   }
-  // sparse grids: points [begin, end) of the row whose first cell is rowkey
+  // row table or hash: points [begin, end) of the row whose first cell is rowkey
   __device__ __forceinline__ int2 row(uint64_t rowkey) const {
+    if (sparse == 2) {
+      const uint64_t idx = table_off + udiv_by(rowkey, glm, gls);
+      if (!((occ[idx >> 5] >> (idx & 31)) & 1u)) return make_int2(0, 0);
+      return make_int2((int)start[idx], (int)start[idx + 1]);
+    }
     const unsigned long long k = hi | rowkey;
     uint32_t h = hash_key(k) & hmask;
     for (uint32_t probe = 0; probe <= hmask; ++probe) {
@@ -660,6 +686,21 @@ struct GridView {
       h = (h + 1) & hmask;
     }
     return make_int2(0, 0);
+  }
+  // core occupancy bits of cells z0..z1 of a cell-table row (bit z - z0)
+  __device__ __forceinline__ uint32_t core_cells(uint64_t rowkey, int64_t z0, int64_t z1) const {
+    const uint64_t i0 = table_off + rowkey + (uint64_t)z0;
+    const int len = (int)(z1 - z0) + 1;  // <= 5
+    const uint64_t w = i0 >> 5;
+    const int sh = (int)(i0 & 31);
+    uint64_t bits = cocc[w] >> sh;
+    if (sh + len > 32) bits |= (uint64_t)cocc[w + 1] << (32 - sh);
+    return (uint32_t)bits & ((1u << len) - 1u);
+  }
+  // row table: whether the row whose first cell is rowkey holds a core point
+  __device__ __forceinline__ bool core_row(uint64_t rowkey) const {
+    const uint64_t idx = table_off + udiv_by(rowkey, glm, gls);
+    return (cocc[idx >> 5] >> (idx & 31)) & 1u;
   }
   // first sorted position in [b, e) whose key is >= g
   __device__ __forceinline__ int lower(int b, int e, uint64_t g) const {
@@ -688,21 +729,23 @@ struct GridView {
       if (!((occ[idx >> 5] >> (idx & 31)) & 1u)) return make_int2(0, 0);
       return make_int2((int)start[idx], (int)start[idx + 1]);
     }
-    const int64_t z = (int64_t)(k % (uint64_t)Gl);
+    const int64_t z = (int64_t)(k - udiv_by(k, glm, gls) * (uint64_t)Gl);
     return span_row(k - (uint64_t)z, z, z);
   }
   // points of the cells k0..k1 (consecutive local keys along one row)
   __device__ __forceinline__ int2 span(uint64_t k0, uint64_t k1) const {
     if (!sparse)
       return make_int2((int)start[table_off + k0], (int)start[table_off + k1 + 1]);
-    const int64_t z0 = (int64_t)(k0 % (uint64_t)Gl);
+    const int64_t z0 = (int64_t)(k0 - udiv_by(k0, glm, gls) * (uint64_t)Gl);
     return span_row(k0 - (uint64_t)z0, z0, z0 + (int64_t)(k1 - k0));
   }
 };
 
 __device__ __forceinline__ GridView view_of(const gdl::Bufs& B, const DevParams& P) {
-  return GridView{B.start, B.occ, B.hkeys, B.hvals, B.reps, B.keys, B.hmask, P.sparse,
-                  B.Bi->key64, P.table_off, (uint64_t)P.inst << P.LB, P.G[P.dim - 1]};
+  const int a = P.dim - 2;
+  return GridView{B.start, B.occ, B.cocc, B.hkeys, B.hvals, B.reps, B.keys, B.hmask, P.sparse,
+                  B.Bi->key64, P.table_off, (uint64_t)P.inst << P.LB, P.G[P.dim - 1],
+                  P.dm[a], P.ds[a]};
 }
 
 template <bool KEY64>
@@ -926,6 +969,13 @@ __device__ __forceinline__ int classify(const float* u, int ox, int oy, int oz, 
 // sorted points, and its non-empty cells are visited through the run structure,
 // so empty cells cost nothing.
 constexpr int kScanThreadsPerBlock = 256;
+// Resident 256-thread blocks per SM the front-end kernels are compiled for
+// (register budget 65536 / (256 * blocks) per thread).  These kernels are
+// bound by memory latency, so occupancy beats registers; the counts were
+// measured on GB300 (a few spilled bytes cost less than a lost block).
+constexpr int core_min_blocks(int D) { return D == 2 ? 2 : 3; }
+constexpr int kUnionMinBlocks = 4;
+constexpr int kBorderMinBlocks = 3;
 constexpr int kInlineCoreTests = 256;    // pair tests one thread spends on a point's core count
 constexpr int kInlineLinkTests = 48;     // tests before a link search goes to a warp
 constexpr int kInlineBorderTests = 160;  // tests one thread spends on a border point
@@ -1020,7 +1070,7 @@ constexpr int kCoreQueue = 8;  // undecided cells a point queues before testing 
 // which recomputes the whole cell.  Per-cell core counts and smallest core
 // indices are warp-aggregated atomics (cleared before the launch).
 template <int D, bool F32, bool KEY64>
-__global__ void __launch_bounds__(kScanThreadsPerBlock) k_core_point(const gdl::Bufs B, int64_t n) {
+__global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_core_point(const gdl::Bufs B, int64_t n) {
   __shared__ int2 sq[kCoreQueue][kScanThreadsPerBlock];
   const OffTab& T = kRows[D - 2];
   const int lane = threadIdx.x & 31;
@@ -1201,7 +1251,7 @@ __device__ __forceinline__ int half_bit(int pass, int ox, int oy, int oz) {
 }
 
 template <int D, bool F32, bool KEY64>
-__global__ void __launch_bounds__(kScanThreadsPerBlock)
+__global__ void __launch_bounds__(kScanThreadsPerBlock, kUnionMinBlocks)
 k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
   const OffTab& T = kRows[D - 2];
   const int lane = threadIdx.x & 31;
@@ -1286,7 +1336,7 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
 // gives its id without tests and one wholly outside is skipped.  A point whose
 // tests pass the budget sends its cell to the warp kernel.
 template <int D, bool F32, bool KEY64>
-__global__ void __launch_bounds__(kScanThreadsPerBlock) k_border_point(const gdl::Bufs B, int64_t n) {
+__global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_border_point(const gdl::Bufs B, int64_t n) {
   const OffTab& T = kRows[D - 2];
   const int lane = threadIdx.x & 31;
   const int LB = B.Bi->LB;
@@ -1333,6 +1383,43 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock) k_border_point(const gdl
             rmn += b2;
           }
         }
+        if (gv.sparse == 0) {
+          // cell table: visit only the cells holding a core point
+          uint32_t cm = gv.core_cells((uint64_t)rk, rw.l0, rw.l1);
+          while (cm && !over) {
+            const int z = __ffs(cm) - 1;
+            cm &= cm - 1;
+            const uint64_t idx = gv.table_off + (uint64_t)rk + (uint64_t)(rw.l0 + z);
+            const int q = (int)gv.start[idx], qe = (int)gv.start[idx + 1];
+            const int cB = B.cellcid[q];
+            if (cB >= best) continue;
+            int cls = 0;
+            if (prune) {
+              const int d = (int)(rw.l0 + z - rw.cl);
+              const float smax = rmx + sel5(lmx, d), smin = rmn + sel5(lmn, d);
+              cls = smax <= Q.thr_in ? 1 : (smin >= Q.thr_out ? -1 : 0);
+            }
+            if (cls > 0) {
+              best = cB;
+            } else if (cls == 0) {
+              for (int qq = q; qq < qe; ++qq) {
+                if (!B.core[qq]) continue;
+                if (budget-- == 0) {
+                  over = true;
+                  break;
+                }
+                Cand<D, F32> cd;
+                load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
+                if (pair_test<D, F32>(px, pf, cd, B.X, n, qq, false, Q, t)) {
+                  best = cB;
+                  break;
+                }
+              }
+            }
+          }
+          continue;
+        }
+        if (gv.sparse == 2 && !gv.core_row((uint64_t)rk)) continue;
         const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
         for (int q = sp.x; q < sp.y && !over;) {
           const int qe = cell_end<KEY64>(B, q);
@@ -1650,6 +1737,26 @@ __global__ void k_roots(const gdl::Bufs B) {
 // and the provisional label of every point: its cluster if core, NOISE otherwise.
 // Cluster numbers restart at 0 in every instance: the scan value at the
 // instance's first point counts the clusters of the instances before it.
+// Core occupancy: one bit per cell-table (row-table) entry whose cell (row)
+// holds a core point, so the border search skips the rest without lookups.
+template <bool KEY64>
+__global__ void k_core_occ(const gdl::Bufs B) {
+  const int LB = B.Bi->LB;
+  const int64_t M = *B.M;
+  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
+       m += (int64_t)gridDim.x * blockDim.x) {
+    const int b = B.reps[m];
+    if (B.cellcore[b] <= 0) continue;
+    const uint64_t key = key_at<KEY64>(B, b);
+    const DevParams& P = B.Pv[(int)(key >> LB)];
+    if (P.sparse == 1) continue;
+    const uint64_t local = key & P.kmask;
+    const int a = P.dim - 2;
+    const uint64_t idx = P.table_off + (P.sparse == 2 ? udiv_by(local, P.dm[a], P.ds[a]) : local);
+    atomicOr(B.cocc + (idx >> 5), 1u << (idx & 31));
+  }
+}
+
 template <bool KEY64>
 __global__ void k_label(const gdl::Bufs B, int64_t n) {
   const int LB = B.Bi->LB;
@@ -1940,6 +2047,11 @@ void label(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) {
 
 void border(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s) {
   cudaMemsetAsync(B.ctr + kCtrHeavyBorder, 0, 8, s);
+  if (B.occ_words) {
+    cudaMemsetAsync(B.cocc, 0, B.occ_words * 4, s);
+    if (key64) k_core_occ<true><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
+    else k_core_occ<false><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
+  }
   GD_LAUNCH_DIMS(dims, f32, key64, k_border_point, sms * 8, kScanThreadsPerBlock, B, n);
   GD_LAUNCH_DIMS(dims, f32, key64, k_border_heavy, sms * 8, kCellThreads, B, n);
 }

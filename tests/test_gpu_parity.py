@@ -169,18 +169,24 @@ def test_cli_end_to_end(built_lib, tmp_path, ds, oracle):
 
 
 @pytest.mark.parametrize("prec", PRECISIONS)
-@pytest.mark.parametrize("d", [2, 3])
-def test_sparse_grid_vs_oracle(gpu_ctx, oracle, prec, d):
-    """Far-apart blobs: the eps-cell grid exceeds the dense table and the
-    occupied cells are looked up through the hash (64-bit keys)."""
+@pytest.mark.parametrize("d,extent,hashed", [(2, 1e4, False), (2, 1e7, True),
+                                             (3, 1e2, False), (3, 1e4, True)])
+def test_sparse_grid_vs_oracle(gpu_ctx, oracle, prec, d, extent, hashed):
+    """Far-apart blobs: the eps-cell grid exceeds the dense cell table.  Rows
+    are then looked up through a table of rows when there are few enough of
+    them, else through the hash of occupied rows (64-bit keys)."""
     rng = np.random.default_rng(31 + d)
-    centres = rng.uniform(-1e4, 1e4, (6, d))
+    centres = rng.uniform(-extent, extent, (6, d))
     pts = np.concatenate([c + rng.normal(0, 0.2, (3000, d)) for c in centres] +
-                         [rng.uniform(-1e4, 1e4, (500, d))])
+                         [rng.uniform(-extent, extent, (500, d))])
     pts = pts[rng.permutation(len(pts))]
     lab, core = run(gpu_ctx, pts, 0.05, 6, prec)
     st = gpu_ctx.stats()
-    assert st["grid_cells"] > 10 ** 9 or st["key_bits"] > 32
+    assert st["key_bits"] > 26                      # beyond the dense cell table
+    if hashed:
+        assert st["grid_cells"] == 1                # one-entry slice: the hash
+    else:
+        assert 1 < st["grid_cells"] < 2 ** 27       # rows + 1
     olab, ocore, _ = oracle.oracle_dbscan(pts, 0.05, 6)
     assert np.array_equal(core, ocore)
     assert np.array_equal(lab, olab)
