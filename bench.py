@@ -234,6 +234,12 @@ def run_batch(args, rank, world, local, dist):
     stream = torch.cuda.current_stream(dev)
     ctx = gdm.Context(local, precision=prec)
     ctx.set_stream(stream.cuda_stream)
+    tuning, tune_s, tune_ms = ctx.get_tuning(), 0.0, None
+    if not args.no_autotune:
+        # autotune on a sample: the first 256 instances (about 1/16 of the points)
+        t0 = time.perf_counter()
+        tuning, tune_ms = ctx.autotune([(i.points, i.eps, i.minpts) for i in insts[:256]])
+        tune_s = time.perf_counter() - t0
     d_flat = torch.from_numpy(flat).to(dev)
     d_lab = torch.empty(ntot, dtype=torch.int32, device=dev)
     kc = np.zeros(K, dtype=np.int64)
@@ -315,6 +321,9 @@ def run_batch(args, rank, world, local, dist):
                             "3": int(sum(i.dim == 3 for i in insts))},
                    "precision": args.precision, "parallelism": f"replicas{world}",
                    "generation_s": round(gen_s, 1),
+                   "tuning": tuning, "autotune": None if args.no_autotune else
+                   {"sample": "first 256 instances", "seconds": round(tune_s, 2),
+                    "sample_device_ms": tune_ms},
                    "l2": "512 MiB flush write between timed steps"},
         "e2e": {"value": world * ntot / t_e2e, "unit": "points/s",
                 "h2d_bytes_per_step": int(flat.nbytes), "d2h_bytes_per_step": ntot * 4,
@@ -492,6 +501,8 @@ def main():
                     help="batch4096 workload: number of instances")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32band"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batch4096: keep the default tuning instead of autotuning on a sample")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="single-instance workloads: density-preserving size factor (profiling)")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: arrivals per second")

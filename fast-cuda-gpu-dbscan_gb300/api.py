@@ -61,6 +61,15 @@ class GdStats(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class GdTuning(ctypes.Structure):
+    _fields_ = [("mult2d", ctypes.c_double), ("mult3d", ctypes.c_double),
+                ("core_tests", ctypes.c_int32), ("link_tests", ctypes.c_int32),
+                ("border_tests", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
+
+
 class GdServerConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("workers", ctypes.c_int32),
                 ("max_batch", ctypes.c_int32), ("precision", ctypes.c_int32),
@@ -109,6 +118,11 @@ SIGNATURES = [
     ("gd_get_stats", ctypes.c_int, [_P, ctypes.POINTER(GdStats)]),
     ("gd_batch_dbscan", ctypes.c_int, [_P, ctypes.c_int32, _P, _P, ctypes.c_int32, _P, _P,
                                        ctypes.POINTER(GdStats)]),
+    ("gd_ctx_set_graphs", ctypes.c_int, [_P, ctypes.c_int32]),
+    ("gd_ctx_set_tuning", ctypes.c_int, [_P, ctypes.POINTER(GdTuning)]),
+    ("gd_ctx_get_tuning", ctypes.c_int, [_P, ctypes.POINTER(GdTuning)]),
+    ("gd_autotune", ctypes.c_int, [_P, ctypes.c_int32, _P, _P, ctypes.c_int32, ctypes.c_int32,
+                                   ctypes.POINTER(GdTuning), ctypes.POINTER(ctypes.c_double)]),
     ("gd_server_create", ctypes.c_int, [ctypes.POINTER(GdServerConfig), ctypes.POINTER(_P)]),
     ("gd_server_destroy", None, [_P]),
     ("gd_server_submit", ctypes.c_int, [_P, ctypes.POINTER(GdInstance), _P, _P,
@@ -147,6 +161,21 @@ def _check(status: int) -> None:
     if status != GD_OK:
         lib = load_library()
         raise GdError(status, lib.gd_last_error().decode(errors="replace"))
+
+
+def _instances(instances):
+    """(gd_instance array, concatenated row-major float64 coordinates)."""
+    desc = (GdInstance * max(len(instances), 1))()
+    parts = []
+    for i, (pts, eps, mp) in enumerate(instances):
+        a = np.ascontiguousarray(pts, dtype=np.float64)
+        desc[i].n = a.shape[0]
+        desc[i].dim = a.shape[1]
+        desc[i].minpts = int(mp)
+        desc[i].eps = float(eps)
+        parts.append(a.reshape(-1))
+    coords = np.concatenate(parts) if parts else np.zeros(1)
+    return desc, coords
 
 
 def _is_torch(x) -> bool:
@@ -216,24 +245,16 @@ class Context:
 
         ``instances``: list of (points (n, dim) float64, eps, minpts).  Returns a
         list of per-instance label arrays (cluster ids restart at 0 in each)."""
-        desc = (GdInstance * len(instances))()
-        parts = []
-        for i, (pts, eps, mp) in enumerate(instances):
-            a = np.ascontiguousarray(pts, dtype=np.float64)
-            desc[i].n = a.shape[0]
-            desc[i].dim = a.shape[1]
-            desc[i].minpts = int(mp)
-            desc[i].eps = float(eps)
-            parts.append(a.reshape(-1))
-        coords = np.concatenate(parts) if parts else np.zeros(0)
-        total = int(sum(d.n for d in desc))
+        desc, coords = _instances(instances)
+        desc_list = list(desc)[: len(instances)]
+        total = int(sum(d.n for d in desc_list))
         lab = np.empty(max(total, 1), dtype=np.int32)
         kc = np.zeros(max(len(instances), 1), dtype=np.int64)
         st = GdStats()
         _check(self._lib.gd_batch_dbscan(self._ctx, len(instances), desc, coords.ctypes.data, 0,
                                          lab.ctypes.data, kc.ctypes.data, ctypes.byref(st)))
         out, off = [], 0
-        for d in desc:
+        for d in desc_list:
             out.append(lab[off: off + d.n].copy())
             off += d.n
         if with_stats:
@@ -242,6 +263,31 @@ class Context:
 
     def trim(self) -> None:
         _check(self._lib.gd_ctx_trim(self._ctx))
+
+    def set_graphs(self, enable: bool) -> None:
+        """Replay the expand launches as a CUDA graph on repeated gd_expand calls."""
+        _check(self._lib.gd_ctx_set_graphs(self._ctx, 1 if enable else 0))
+
+    # ---- tuning --------------------------------------------------------------
+    def get_tuning(self) -> dict:
+        t = GdTuning()
+        _check(self._lib.gd_ctx_get_tuning(self._ctx, ctypes.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, mult2d: float = 0.0, mult3d: float = 0.0, core_tests: int = 256,
+                   link_tests: int = 48, border_tests: int = 160) -> None:
+        t = GdTuning(mult2d, mult3d, core_tests, link_tests, border_tests, 0)
+        _check(self._lib.gd_ctx_set_tuning(self._ctx, ctypes.byref(t)))
+
+    def autotune(self, instances, repeats: int = 2) -> tuple[dict, float]:
+        """Pick the fastest tuning for a sample of instances (list of (points,
+        eps, minpts)); it is set on the context.  Returns (tuning, device ms)."""
+        desc, coords = _instances(instances)
+        t = GdTuning()
+        ms = ctypes.c_double()
+        _check(self._lib.gd_autotune(self._ctx, len(instances), desc, coords.ctypes.data, 0,
+                                     int(repeats), ctypes.byref(t), ctypes.byref(ms)))
+        return t.as_dict(), ms.value
 
     # ---- staged pipeline ---------------------------------------------------
     def _points(self, points):

@@ -57,6 +57,9 @@ struct DevBuf {
 };
 
 constexpr double kDefaultCellMult = 0.5 * (1.0 + 1.0 / 65536.0);
+// pair tests one thread spends before handing its work to a warp
+constexpr int kDefaultCoreTests = 256, kDefaultLinkTests = 48, kDefaultBorderTests = 160;
+constexpr int kMaxTests = 65536;
 // largest multipliers allowed: cell diagonal below eps (1 - 2^-20)
 constexpr double kMaxCellMult2 = 0.70710678118654752 * (1.0 - 1.0 / 1048576.0);
 constexpr double kMaxCellMult3 = 0.57735026918962576 * (1.0 - 1.0 / 1048576.0);
@@ -76,6 +79,7 @@ struct gd_ctx {
   cudaStream_t stream = nullptr;
   int precision = GD_PREC_FP64;
   double mult2 = kDefaultCellMult, mult3 = kDefaultCellMult;
+  int tn_core = kDefaultCoreTests, tn_link = kDefaultLinkTests, tn_border = kDefaultBorderTests;
 
   DevBuf coords, inst, chunks, Pv, Bi, bbox, keys0, keys1, vals0, vals1, X, Xf, table, occ, hkeys,
       hvals, reps, runfl, runpos, core, cellcore, cellmin, parent, Fmark, cellcid, lab, asym,
@@ -95,6 +99,16 @@ struct gd_ctx {
   uint32_t* sids = nullptr;
   uint32_t hmask = 0;
   cudaEvent_t ev[8] = {};
+  // CUDA graph of the expand launches, captured on the second gd_expand of one
+  // index build and replayed by later ones (minpts sweeps)
+  bool graphs = true;
+  cudaGraphExec_t xgraph = nullptr;
+  int expands_on_index = 0;
+  void drop_graph() {
+    if (xgraph) cudaGraphExecDestroy(xgraph);
+    xgraph = nullptr;
+    expands_on_index = 0;
+  }
   gd_stats st{};
   int launches = 0;
 
@@ -172,6 +186,9 @@ struct gd_ctx {
     B.hv_cell = static_cast<int*>(hvcell.p);
     B.hv_mask = static_cast<unsigned long long*>(hvmask.p);
     B.ctr = dCtr();
+    B.tn_core = tn_core;
+    B.tn_link = tn_link;
+    B.tn_border = tn_border;
     return B;
   }
 };
@@ -195,6 +212,7 @@ void make_chunks(const std::vector<gd::InstDesc>& desc, std::vector<gd::Chunk>& 
 // Build stage of a run: ctx->hdesc (internal order, 2D instances first) and
 // ctx->coords_ptr (device) are set by the caller.
 gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point) {
+  ctx->drop_graph();
   cudaStream_t s = ctx->stream;
   const int K = (int)ctx->hdesc.size();
   ctx->K = K;
@@ -304,6 +322,32 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
   return GD_OK;
 }
 
+// The expand launches (no allocation, no host synchronisation, so they can be
+// captured).  Returns the first error; never leaves early.
+cudaError_t launch_expand(gd_ctx* ctx, bool capturing) {
+  cudaStream_t s = ctx->stream;
+  const int64_t n = ctx->n;
+  const unsigned evf = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+  cudaError_t e = cudaSuccess;
+  auto keep = [&](cudaError_t r) { if (e == cudaSuccess && r != cudaSuccess) e = r; };
+  // counters of this stage (the build's cell counts and 2D/3D split stay)
+  keep(cudaMemsetAsync(ctx->dCtr() + gd::kCtrTests64, 0,
+                       (gd::kCtrHeavyBorder - gd::kCtrTests64 + 1) * 8, s));
+  gdl::Bufs B = ctx->bufs();
+  keep(cudaEventRecordWithFlags(ctx->ev[3], s, evf));
+  gdl::core(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, s);
+  keep(cudaEventRecordWithFlags(ctx->ev[4], s, evf));
+  gdl::unite(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, s);
+  keep(cudaEventRecordWithFlags(ctx->ev[5], s, evf));
+  keep(cudaMemsetAsync(B.Fmark, 0, (n + 1) * 4, s));
+  gdl::roots(B, n, ctx->sms, s);
+  gdprim::exclusive_scan_u32(B.Fmark, B.Fmark, n + 1, ctx->scantemp.p, ctx->dK(), s);
+  gdl::label(B, ctx->key64, n, ctx->sms, s);
+  gdl::border(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, s);
+  keep(cudaGetLastError());
+  return e;
+}
+
 gd_status expand_run(gd_ctx* ctx) {
   cudaStream_t s = ctx->stream;
   const int64_t n = ctx->n;
@@ -319,26 +363,42 @@ gd_status expand_run(gd_ctx* ctx) {
   GD_TRY(ctx->ensure(ctx->hvmask, n * 8, "heavy-work masks"));
   GD_TRY(ctx->ensure(ctx->scantemp, std::max(gdprim::scan_temp_bytes(n + 1), ctx->scantemp.bytes),
                      "scan temp"));
-  // counters of this stage (the build's cell counts and 2D/3D split stay)
-  GD_CUDA(cudaMemsetAsync(ctx->dCtr() + gd::kCtrTests64, 0,
-                          (gd::kCtrHeavyBorder - gd::kCtrTests64 + 1) * 8, s), "clear counters");
-  gdl::Bufs B = ctx->bufs();
-  cudaEventRecord(ctx->ev[3], s);
-  gdl::core(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, s);
-  cudaEventRecord(ctx->ev[4], s);
-  gdl::unite(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, s);
-  cudaEventRecord(ctx->ev[5], s);
-  GD_CUDA(cudaMemsetAsync(B.Fmark, 0, (n + 1) * 4, s), "clear marks");
-  gdl::roots(B, n, ctx->sms, s);
-  gdprim::exclusive_scan_u32(B.Fmark, B.Fmark, n + 1, ctx->scantemp.p, ctx->dK(), s);
-  gdl::label(B, ctx->key64, n, ctx->sms, s);
-  gdl::border(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, s);
-  GD_CUDA(cudaGetLastError(), "expand launch");
   const int cp = gdl::launches_per_cell_phase(ctx->dims);
   // core, parent init, 2 union passes, compress, merge replay, roots, scan,
   // label, core occupancy (with tables), border
   ctx->launches += 2 * cp + 1 + 4 * cp + 1 + 1 + 1 + 3 + 1 + (ctx->bi.table_total ? 1 : 0) + 2 * cp;
   ctx->stage = 2;
+  if (ctx->graphs && ctx->xgraph) {
+    GD_CUDA(cudaGraphLaunch(ctx->xgraph, s), "expand graph launch");
+    return GD_OK;
+  }
+  // capture on the second expand of this index build: a first one is often
+  // the only one (gd_dbscan), and capturing costs more than launching once
+  bool capture = ctx->graphs && ctx->expands_on_index >= 1;
+  ++ctx->expands_on_index;
+  if (capture && cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();
+    capture = false;
+  }
+  cudaError_t e = launch_expand(ctx, capture);
+  if (!capture) {
+    if (e != cudaSuccess) return cuda_fail(e, "expand launch");
+    return GD_OK;
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t ec = cudaStreamEndCapture(s, &g);
+  if (e == cudaSuccess && ec == cudaSuccess && g) ec = cudaGraphInstantiate(&ctx->xgraph, g, 0);
+  if (g) cudaGraphDestroy(g);
+  if (e != cudaSuccess || ec != cudaSuccess) {
+    // nothing captured ran: give up graphs for this context and launch directly
+    cudaGetLastError();
+    ctx->xgraph = nullptr;
+    ctx->graphs = false;
+    e = launch_expand(ctx, false);
+    if (e != cudaSuccess) return cuda_fail(e, "expand launch");
+    return GD_OK;
+  }
+  GD_CUDA(cudaGraphLaunch(ctx->xgraph, s), "expand graph launch");
   return GD_OK;
 }
 
@@ -486,6 +546,7 @@ void gd_ctx_destroy(gd_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  ctx->drop_graph();
   ctx->free_all(false);
   for (auto& ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
@@ -522,10 +583,106 @@ gd_status gd_ctx_set_cell_mults(gd_ctx* ctx, double mult2d, double mult3d) {
   return GD_OK;
 }
 
+gd_status gd_ctx_set_graphs(gd_ctx* ctx, int32_t enable) {
+  if (!ctx) return fail(GD_EINVAL, "gd_ctx_set_graphs: NULL context");
+  ctx->drop_graph();
+  ctx->graphs = enable != 0;
+  return GD_OK;
+}
+
+gd_status gd_ctx_set_tuning(gd_ctx* ctx, const gd_tuning* t) {
+  if (!ctx || !t) return fail(GD_EINVAL, "gd_ctx_set_tuning: NULL argument");
+  auto ok = [](int32_t v) { return v >= 0 && v <= kMaxTests; };
+  if (!ok(t->core_tests) || !ok(t->link_tests) || !ok(t->border_tests) || t->reserved != 0)
+    return fail(GD_EINVAL, "gd_ctx_set_tuning: test budgets must lie in [0, 65536], reserved 0");
+  GD_TRY(gd_ctx_set_cell_mults(ctx, t->mult2d, t->mult3d));
+  ctx->tn_core = t->core_tests;
+  ctx->tn_link = t->link_tests;
+  ctx->tn_border = t->border_tests;
+  ctx->drop_graph();  // the captured launches carry the budgets
+  return GD_OK;
+}
+
+gd_status gd_ctx_get_tuning(gd_ctx* ctx, gd_tuning* t) {
+  if (!ctx || !t) return fail(GD_EINVAL, "gd_ctx_get_tuning: NULL argument");
+  *t = gd_tuning{ctx->mult2, ctx->mult3, ctx->tn_core, ctx->tn_link, ctx->tn_border, 0};
+  return GD_OK;
+}
+
+gd_status gd_autotune(gd_ctx* ctx, int32_t count, const gd_instance* inst, const double* coords,
+                      int32_t on_device, int32_t repeats, gd_tuning* best, double* best_ms) {
+  if (!ctx || (count > 0 && !inst)) return fail(GD_EINVAL, "gd_autotune: NULL argument");
+  if (repeats < 1 || repeats > 100) return fail(GD_EINVAL, "gd_autotune: repeats must be 1..100");
+  bool has2 = false, has3 = false;
+  int64_t pts = 0;
+  for (int i = 0; i < count; ++i) {
+    has2 |= inst[i].dim == 2 && inst[i].n > 0;
+    has3 |= inst[i].dim == 3 && inst[i].n > 0;
+    pts += inst[i].n > 0 ? inst[i].n : 0;
+  }
+  gd_tuning cur;
+  GD_TRY(gd_ctx_get_tuning(ctx, &cur));
+  // labels go to a scratch buffer in the sample's memory space
+  std::vector<int32_t> hlab;
+  void* dlab = nullptr;
+  if (on_device) {
+    if (pts > 0) GD_CUDA(cudaMalloc(&dlab, (size_t)pts * 4), "autotune label buffer");
+  } else {
+    hlab.resize((size_t)std::max<int64_t>(pts, 1));
+  }
+  int32_t* lab = on_device ? static_cast<int32_t*>(dlab) : hlab.data();
+  // device time of one tuning: best of `repeats` runs after one warm-up
+  auto eval = [&](const gd_tuning& t, double& ms) -> gd_status {
+    GD_TRY(gd_ctx_set_tuning(ctx, &t));
+    ms = 1e300;
+    for (int r = 0; r <= repeats; ++r) {
+      gd_stats st;
+      GD_TRY(gd_batch_dbscan(ctx, count, inst, coords, on_device, lab, nullptr, &st));
+      if (r > 0) ms = std::min(ms, st.ms_total);
+    }
+    return GD_OK;
+  };
+  double cur_ms = 0;
+  gd_status st = eval(cur, cur_ms);
+  // coordinate descent over the multipliers, then the budgets
+  const double m2c[] = {kDefaultCellMult, 0.55, 0.6, 0.65, kMaxCellMult2};
+  const double m3c[] = {kDefaultCellMult, 0.53, 0.555, kMaxCellMult3};
+  const double scale[] = {0.25, 0.5, 2.0, 4.0};
+  for (int axis = 0; axis < 3 && st == GD_OK; ++axis) {
+    if ((axis == 0 && !has2) || (axis == 1 && !has3)) continue;
+    const int nc = axis == 0 ? 5 : 4;
+    const gd_tuning base = cur;
+    for (int c = 0; c < nc && st == GD_OK; ++c) {
+      gd_tuning t = base;
+      if (axis == 0) t.mult2d = m2c[c];
+      else if (axis == 1) t.mult3d = m3c[c];
+      else {
+        auto sc = [&](int v) { return std::min(kMaxTests, std::max(1, (int)(v * scale[c]))); };
+        t.core_tests = sc(base.core_tests);
+        t.link_tests = sc(base.link_tests);
+        t.border_tests = sc(base.border_tests);
+      }
+      double ms = 0;
+      st = eval(t, ms);
+      if (st == GD_OK && ms < cur_ms) {
+        cur = t;
+        cur_ms = ms;
+      }
+    }
+  }
+  if (dlab) cudaFree(dlab);
+  if (st != GD_OK) return st;
+  GD_TRY(gd_ctx_set_tuning(ctx, &cur));
+  if (best) *best = cur;
+  if (best_ms) *best_ms = cur_ms;
+  return GD_OK;
+}
+
 gd_status gd_ctx_trim(gd_ctx* ctx) {
   if (!ctx) return fail(GD_EINVAL, "NULL context");
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  ctx->drop_graph();
   ctx->free_all(true);
   ctx->stage = 0;
   return GD_OK;

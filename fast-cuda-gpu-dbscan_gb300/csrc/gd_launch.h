@@ -54,6 +54,9 @@ struct Bufs {
   int* hv_cell = nullptr;       // heavy-work list: cell index m (capacity n)
   unsigned long long* hv_mask = nullptr;  // heavy-work list: stencil offsets still open
   unsigned long long* ctr = nullptr;      // gd::Counter
+  // pair-test budgets of one thread before its work goes to a warp kernel
+  // (core count per point, link search per cell pair, border search per point)
+  int tn_core = 256, tn_link = 48, tn_border = 160;
 };
 
 // per-instance bounding boxes, grids and the run layout

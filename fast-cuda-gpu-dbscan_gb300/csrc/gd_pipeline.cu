@@ -976,9 +976,9 @@ constexpr int kScanThreadsPerBlock = 256;
 constexpr int core_min_blocks(int D) { return D == 2 ? 2 : 3; }
 constexpr int kUnionMinBlocks = 4;
 constexpr int kBorderMinBlocks = 3;
-constexpr int kInlineCoreTests = 256;    // pair tests one thread spends on a point's core count
-constexpr int kInlineLinkTests = 48;     // tests before a link search goes to a warp
-constexpr int kInlineBorderTests = 160;  // tests one thread spends on a border point
+// The pair-test budgets of one thread (core count per point, link search per
+// cell pair, border search per point) come with the buffers (Bufs::tn_*): the
+// context sets them, the autotuner varies them.
 
 // warp-aggregated append to the heavy list (all 32 lanes must call it)
 __device__ __forceinline__ void heavy_push(const gdl::Bufs& B, int slot, bool push, int64_t m,
@@ -1113,7 +1113,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
 #pragma unroll
           for (int j = 0; j < 5; ++j) axis_terms(u[D - 1], j - 2, Q, lmx[j], lmn[j]);
         }
-        int cnt = 0, ptot = 0, nq = 0, budget = kInlineCoreTests;
+        int cnt = 0, ptot = 0, nq = 0, budget = B.tn_core;
         auto flush = [&](void) {
           for (int j = 0; j < nq && cnt < Q.minpts && !over; ++j) {
             const int2 c = sq[j][threadIdx.x];
@@ -1200,7 +1200,7 @@ __device__ __forceinline__ int inline_link(const gdl::Bufs& B, int64_t n, int bA
                                            int eB, const float* oA, int ox, int oy, int oz,
                                            const PredParams& Q, Tally& t) {
   const bool prune = Q.prune != 0;
-  int budget = kInlineLinkTests;
+  int budget = B.tn_link;
   for (int a = bA; a < eA; ++a) {
     if (!B.core[a]) continue;
     double ax[D];
@@ -1369,7 +1369,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
 #pragma unroll
         for (int k = 0; k < 5; ++k) axis_terms(u[D - 1], k - 2, Q, lmx[k], lmn[k]);
       }
-      int best = INT_MAX, budget = kInlineBorderTests;
+      int best = INT_MAX, budget = B.tn_border;
       for (int r = 0; r < T.n && !over; ++r) {
         const int64_t rk = rw.rowkey(T, r, P);
         if (rk < 0) continue;

@@ -79,8 +79,9 @@ typedef struct gd_stats {
   int64_t tests_fp32;       /* float32 pair evaluations */
   int64_t band_retests;     /* float32 evaluations re-tested in float64 */
   int64_t asym_pairs;       /* core pairs that are neighbours in one direction only
-                               (possible only at the last bit of eps; see DESIGN) */
-  int64_t grid_cells;       /* cells of the dense cell table */
+                               (the box test and the distance test disagree at the
+                               last bit; their merges are replayed in order) */
+  int64_t grid_cells;       /* entries of the cell / row tables (1 per hashed grid) */
   int32_t precision_used;   /* gd_precision actually run */
   int32_t key_bits;         /* radix-sort key width */
   int32_t launches;         /* kernel launches of the last pipeline run */
@@ -110,6 +111,11 @@ gd_status gd_ctx_set_cell_mult(gd_ctx* ctx, double mult);
 gd_status gd_ctx_set_cell_mults(gd_ctx* ctx, double mult2d, double mult3d);
 /* Frees the context's cached device buffers (they regrow on the next call). */
 gd_status gd_ctx_trim(gd_ctx* ctx);
+/* No counterpart in the reference.  With graphs enabled (the default), the
+   second gd_expand on one index build captures the expand launches into a CUDA
+   graph and later gd_expand calls on that index (other minpts) replay it with
+   one launch.  A new index build, a tuning change or gd_ctx_trim drops it. */
+gd_status gd_ctx_set_graphs(gd_ctx* ctx, int32_t enable);
 
 /* ---- the pipeline, stage by stage ---------------------------------------- */
 /* Replaces main.cu:166-338: host min/max + bin widths (main.cu:166-207), the
@@ -161,6 +167,32 @@ typedef struct gd_instance {
 gd_status gd_batch_dbscan(gd_ctx* ctx, int32_t count, const gd_instance* inst,
                           const double* coords, int32_t on_device, int32_t* labels,
                           int64_t* cluster_counts, gd_stats* stats);
+
+/* ---- tuning --------------------------------------------------------------- */
+/* No counterpart in the reference (whose launch shape and partition count are
+   compile-time constants, common.h:10-25).  Parameters that change speed but
+   never labels: the cell side as a multiple of eps per dimension (see
+   gd_ctx_set_cell_mults) and the pair tests one thread spends on a core
+   count, a link search and a border search before the work goes to a warp. */
+typedef struct gd_tuning {
+  double mult2d;          /* (0.5, 1/sqrt(2)); 0 = default */
+  double mult3d;          /* (0.5, 1/sqrt(3)); 0 = default */
+  int32_t core_tests;     /* 0..65536; defaults 256, 48, 160 */
+  int32_t link_tests;
+  int32_t border_tests;
+  int32_t reserved;       /* 0 */
+} gd_tuning;
+
+gd_status gd_ctx_set_tuning(gd_ctx* ctx, const gd_tuning* t);
+gd_status gd_ctx_get_tuning(gd_ctx* ctx, gd_tuning* t);
+/* Autotuner: clusters the given sample (same arguments as gd_batch_dbscan,
+   labels discarded) under candidate tunings, coordinate by coordinate (2D cell
+   multiplier if 2D instances are present, 3D multiplier if 3D ones are, then
+   the three test budgets scaled together), keeps the one with the smallest
+   device time (best of `repeats` runs each, CUDA events), sets it on the
+   context and returns it (best and best_ms may be NULL). */
+gd_status gd_autotune(gd_ctx* ctx, int32_t count, const gd_instance* inst, const double* coords,
+                      int32_t on_device, int32_t repeats, gd_tuning* best, double* best_ms);
 
 /* ---- request server with continuous batching ---------------------------- */
 /* No counterpart in the reference.  A server queues clustering requests (one
