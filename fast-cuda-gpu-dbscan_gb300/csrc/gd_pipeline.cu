@@ -1056,24 +1056,46 @@ __device__ __forceinline__ float sel5(const float (&a)[5], int d) {
 }
 
 constexpr int kCoreQueue = 8;  // undecided cells a point queues before testing them
+constexpr int kCoreWarps = kScanThreadsPerBlock / 32;
+
+// Per-warp staging of the final flush: the points whose core decision waits on
+// their queued cells, with their predicate constants (lanes of one warp may
+// belong to different instances).
+template <int D>
+struct CoreFlushStage {
+  double x[32][D];
+  float f[32][D];
+  PredParams q[32];
+  int cnt[32];    // neighbours counted so far
+  int incl[32];   // inclusive prefix of the queued candidate counts
+  int nq[32];
+};
 
 // Core flags, one thread per point.  Neighbouring lanes hold neighbouring
 // sorted points, mostly of one cell, so they walk the same stencil rows in
 // step: their loads coincide and their branches agree.  A point of a cell with
 // at least minpts points is core at once.  Otherwise the walk goes row by row,
-// own row first: with cell classification, cells wholly inside eps count
-// without tests, cells wholly outside are skipped, and undecided cells are
-// queued (shared memory) and tested only when the queue fills or the walk ends
-// short of minpts.  The classification's per-axis terms are formed per row for
-// the fixed axes and per point for the last axis (five values in registers).
-// A point whose tests pass the budget sends its cell to the warp kernel,
-// which recomputes the whole cell.  Per-cell core counts and smallest core
-// indices are warp-aggregated atomics (cleared before the launch).
+// own row first: with cell classification, rows and cells wholly inside eps
+// count without tests, those wholly outside are skipped, and undecided cells
+// are queued (shared memory).  The classification's per-axis terms are formed
+// per row for the fixed axes and per point for the last axis (five values in
+// registers).  A full queue is tested by its own thread; what is queued when
+// the walk ends is tested by the whole warp together: the lanes whose decision
+// depends on their queue pool its candidates and every lane tests one
+// candidate per round (one owner's point against one queued point), so the
+// float64 tests run on full warps, and owners stop consuming once they reach
+// minpts.  A point whose tests pass the budget (or a warp whose pooled
+// candidates pass 32 budgets) sends its cell to the warp kernel, which
+// recomputes the whole cell.  Per-cell core counts and smallest core indices
+// are warp-aggregated atomics (cleared before the launch).
 template <int D, bool F32, bool KEY64>
 __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_core_point(const gdl::Bufs B, int64_t n) {
   __shared__ int2 sq[kCoreQueue][kScanThreadsPerBlock];
+  __shared__ CoreFlushStage<D> stage[kCoreWarps];
   const OffTab& T = kRows[D - 2];
   const int lane = threadIdx.x & 31;
+  const int wbase = threadIdx.x & ~31;
+  CoreFlushStage<D>& S = stage[threadIdx.x >> 5];
   const int LB = B.Bi->LB;
   int64_t mlo, mhi;
   dim_range<D>(B, mlo, mhi);
@@ -1081,12 +1103,12 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   Tally t;
   unsigned long long dense = 0;
-  for (int64_t i0 = plo + (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); i0 < phi;
-       i0 += stride) {
+  for (int64_t i0 = plo + (int64_t)blockIdx.x * blockDim.x + wbase; i0 < phi; i0 += stride) {
     const int64_t i = i0 + lane;
     const bool valid = i < phi;
     int m = -1, b = 0;
-    bool isc = false, over = false;
+    bool isc = false, over = false, pend = false;
+    int cnt = 0, nq = 0, minpts = 0;
     if (valid) {
       m = (int)(B.runpos[i] + B.runfl[i]) - 1;
       b = B.reps[m];
@@ -1094,6 +1116,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
       const CellCtx cx = cell_ctx<KEY64>(B, b, LB);
       const DevParams& P = *cx.P;
       const PredParams Q = pred_params(P);
+      minpts = Q.minpts;
       if (sz >= Q.minpts) {
         isc = true;
         if (i == b) ++dense;
@@ -1113,7 +1136,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
 #pragma unroll
           for (int j = 0; j < 5; ++j) axis_terms(u[D - 1], j - 2, Q, lmx[j], lmn[j]);
         }
-        int cnt = 0, ptot = 0, nq = 0, budget = B.tn_core;
+        int ptot = 0, budget = B.tn_core;
         auto flush = [&](void) {
           for (int j = 0; j < nq && cnt < Q.minpts && !over; ++j) {
             const int2 c = sq[j][threadIdx.x];
@@ -1128,10 +1151,9 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
             }
           }
           nq = 0;
+          ptot = 0;
         };
         for (int r = 0; r < T.n && cnt < Q.minpts && !over; ++r) {
-          const int64_t rk = rw.rowkey(T, r, P);
-          if (rk < 0) continue;
           float rmx = 0.0f, rmn = 0.0f;
           if (prune) {
 #pragma unroll
@@ -1141,7 +1163,10 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
               rmx += a2;
               rmn += b2;
             }
+            if (rmn >= Q.thr_out) continue;  // the whole row is beyond eps
           }
+          const int64_t rk = rw.rowkey(T, r, P);
+          if (rk < 0) continue;
           const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
           for (int q = sp.x; q < sp.y && cnt < Q.minpts && !over;) {
             const int qe = cell_end<KEY64>(B, q);
@@ -1163,11 +1188,82 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
             q = qe;
           }
         }
-        if (!over && cnt < Q.minpts && cnt + ptot >= Q.minpts) flush();
+        // what is still queued decides only if it can lift the count to minpts
+        pend = !over && cnt < Q.minpts && nq > 0 && cnt + ptot >= Q.minpts;
+        if (pend) {
+#pragma unroll
+          for (int k = 0; k < D; ++k) {
+            S.x[lane][k] = px[k];
+            S.f[lane][k] = pf[k];
+          }
+          S.q[lane] = Q;
+        }
         isc = !over && cnt >= Q.minpts;
       }
-      if (!over) B.core[i] = isc ? 1 : 0;
     }
+    // ---- warp-cooperative final flush
+    const unsigned pm = __ballot_sync(kFull, pend);
+    if (pm) {
+      int tot = 0;
+      if (pend)
+        for (int j = 0; j < nq; ++j) tot += sq[j][threadIdx.x].y - sq[j][threadIdx.x].x;
+      int incl = tot;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += v;
+      }
+      const int total = __shfl_sync(kFull, incl, 31);
+      S.incl[lane] = incl;
+      S.nq[lane] = pend ? nq : 0;
+      S.cnt[lane] = cnt;
+      __syncwarp();
+      if (total > 32 * B.tn_core) {
+        if (pend) over = true;  // too much for the warp: the warp kernel takes the cell
+      } else {
+        for (int base = 0; base < total; base += 32) {
+          const int c = base + lane;
+          if (c < total) {
+            // owner: the first lane whose inclusive prefix passes c
+            int lo = 0, hi = 31;
+            while (lo < hi) {
+              const int mid = (lo + hi) >> 1;
+              if (S.incl[mid] > c) hi = mid;
+              else lo = mid + 1;
+            }
+            const int ow = lo;
+            const PredParams& Qo = S.q[ow];
+            if (S.cnt[ow] < Qo.minpts) {
+              int k = c - (ow > 0 ? S.incl[ow - 1] : 0);  // candidate index within the owner's queue
+              int qq = -1;
+              for (int j = 0; j < S.nq[ow]; ++j) {
+                const int2 sg = sq[j][wbase + ow];
+                const int len = sg.y - sg.x;
+                if (k < len) {
+                  qq = sg.x + k;
+                  break;
+                }
+                k -= len;
+              }
+              if (qq >= 0) {
+                Cand<D, F32> cd;
+                load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
+                if (pair_test<D, F32>(S.x[ow], S.f[ow], cd, B.X, n, qq, true, Qo, t))
+                  atomicAdd(&S.cnt[ow], 1);
+              }
+            }
+          }
+          __syncwarp();
+          if (__all_sync(kFull, !pend || S.cnt[lane] >= minpts)) break;
+        }
+        if (pend) {
+          cnt = S.cnt[lane];
+          isc = cnt >= minpts;
+        }
+      }
+      __syncwarp();
+    }
+    if (valid && !over) B.core[i] = isc ? 1 : 0;
     // per-cell core count and smallest core index, one atomic pair per cell
     // and warp
     const unsigned cm = __ballot_sync(kFull, isc);
@@ -1371,8 +1467,6 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
       }
       int best = INT_MAX, budget = B.tn_border;
       for (int r = 0; r < T.n && !over; ++r) {
-        const int64_t rk = rw.rowkey(T, r, P);
-        if (rk < 0) continue;
         float rmx = 0.0f, rmn = 0.0f;
         if (prune) {
 #pragma unroll
@@ -1382,7 +1476,10 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
             rmx += a2;
             rmn += b2;
           }
+          if (rmn >= Q.thr_out) continue;  // the whole row is beyond eps
         }
+        const int64_t rk = rw.rowkey(T, r, P);
+        if (rk < 0) continue;
         if (gv.sparse == 0) {
           // cell table: visit only the cells holding a core point
           uint32_t cm = gv.core_cells((uint64_t)rk, rw.l0, rw.l1);
