@@ -60,6 +60,10 @@ constexpr double kDefaultCellMult = 0.5 * (1.0 + 1.0 / 65536.0);
 // pair tests one thread spends before handing its work to a warp
 constexpr int kDefaultCoreTests = 256, kDefaultLinkTests = 48, kDefaultBorderTests = 160;
 constexpr int kMaxTests = 65536;
+// A grid takes a cell table (one occupancy bit, one core bit and one prefix bit
+// per cell) when it has at most this many cells per point (or 2^26 cells for a
+// single instance, 4096 per instance in a batch).
+constexpr uint64_t kCellsPerPoint = 64;
 // largest multipliers allowed: cell diagonal below eps (1 - 2^-20)
 constexpr double kMaxCellMult2 = 0.70710678118654752 * (1.0 - 1.0 / 1048576.0);
 constexpr double kMaxCellMult3 = 0.57735026918962576 * (1.0 - 1.0 / 1048576.0);
@@ -166,9 +170,11 @@ struct gd_ctx {
     B.runpos = static_cast<uint32_t*>(runpos.p);
     B.start = static_cast<uint32_t*>(table.p);
     B.occ = static_cast<uint32_t*>(occ.p);
-    if (bi.table_total) {
-      B.occ_words = bi.table_total / 32 + 1;
-      B.cocc = B.occ + B.occ_words;  // second half of the occupancy buffer
+    if (bi.occ_total) {
+      // one buffer: occupancy | core occupancy | word prefix counts
+      B.occ_words = bi.occ_total / 32 + 1;
+      B.cocc = B.occ + B.occ_words;
+      B.wpre = B.occ + gdl::occ_wpre_offset(B.occ_words);
     }
     B.hkeys = static_cast<unsigned long long*>(hkeys.p);
     B.hvals = static_cast<uint32_t*>(hvals.p);
@@ -258,10 +264,9 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
   GD_TRY(ctx->ensure(ctx->vals1, n * 4, "ids"));
   GD_TRY(ctx->ensure(ctx->X, (size_t)n * maxd * 8, "sorted coordinates"));
   if (ctx->xf) GD_TRY(ctx->ensure(ctx->Xf, (size_t)n * maxd * 4, "f32 coordinates"));
-  if (bi.table_total) {
-    GD_TRY(ctx->ensure(ctx->table, bi.table_total * 4, "cell tables"));
-    GD_TRY(ctx->ensure(ctx->occ, 2 * (bi.table_total / 32 + 1) * 4, "cell occupancy"));
-  }
+  const uint64_t W = bi.occ_total ? bi.occ_total / 32 + 1 : 0;
+  GD_TRY(ctx->ensure(ctx->table, std::max<uint64_t>(bi.start_total, 1) * 4, "row tables"));
+  if (W) GD_TRY(ctx->ensure(ctx->occ, gdl::occ_buffer_words(W) * 4, "cell occupancy"));
   uint64_t hcap = 1024;
   if (bi.any_sparse) {
     while (hcap < 2 * (uint64_t)n) hcap <<= 1;
@@ -273,8 +278,9 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
   GD_TRY(ctx->ensure(ctx->runfl, n * 4, "run flags"));
   GD_TRY(ctx->ensure(ctx->runpos, n * 4, "run positions"));
   GD_TRY(ctx->ensure(ctx->sorttemp, gdprim::sort_temp_bytes(n), "sort temp"));
-  size_t sc = std::max(gdprim::scan_temp_bytes(n + 1),
-                       gdprim::scan_temp_bytes((int64_t)bi.table_total));
+  size_t sc = std::max({gdprim::scan_temp_bytes(n + 1),
+                        gdprim::scan_temp_bytes((int64_t)bi.start_total),
+                        gdprim::scan_temp_bytes((int64_t)W)});
   GD_TRY(ctx->ensure(ctx->scantemp, sc, "scan temp"));
   const int key_bits = bi.LB + bi.IB;
   int r;
@@ -297,15 +303,14 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
   gdl::run_flags(ctx->skeys, ctx->key64, n, B.runfl, ctx->sms, s);
   gdprim::exclusive_scan_u32(B.runfl, B.runpos, n, ctx->scantemp.p, ctx->dM(), s);
   gdl::run_scatter(B, ctx->key64, n, ctx->sms, s);
-  int table_launches = 0;
-  if (bi.table_total) {
-    GD_CUDA(cudaMemsetAsync(ctx->table.p, 0, bi.table_total * 4, s), "clear cell tables");
-    GD_CUDA(cudaMemsetAsync(ctx->occ.p, 0, (bi.table_total / 32 + 1) * 4, s), "clear occupancy");
-    gdl::cell_counts(B, ctx->key64, n, ctx->sms, s);
-    gdprim::exclusive_scan_u32(B.start, B.start, (int64_t)bi.table_total, ctx->scantemp.p,
-                               nullptr, s);
-    table_launches += 4;
-  }
+  // occupancy bits, row-table starts, occupancy ranks
+  GD_CUDA(cudaMemsetAsync(ctx->table.p, 0, bi.start_total * 4, s), "clear row tables");
+  if (W) GD_CUDA(cudaMemsetAsync(ctx->occ.p, 0, W * 4, s), "clear occupancy");
+  gdl::cell_counts(B, ctx->key64, n, ctx->sms, s);
+  gdprim::exclusive_scan_u32(B.start, B.start, (int64_t)bi.start_total, ctx->scantemp.p, nullptr,
+                             s);
+  gdl::occ_rank(B, ctx->K, ctx->scantemp.p, s);
+  int table_launches = 4 + (W ? 5 : 0);
   if (bi.any_sparse) {
     GD_CUDA(cudaMemsetAsync(ctx->hkeys.p, 0xff, hcap * 8, s), "clear row hash");
     gdl::hash_insert(B, ctx->key64, n, ctx->sms, s);
@@ -316,7 +321,7 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
   // bbox init+chunks, params, layout, keys, sort, gather, run flags, scan,
   // run scatter + split, tables
   ctx->launches = 4 + 1 + (passes ? passes * 5 : 1) + 1 + 1 + 3 + 2 + table_launches;
-  ctx->st.grid_cells = (int64_t)bi.table_total;
+  ctx->st.grid_cells = (int64_t)bi.occ_total;
   ctx->st.key_bits = key_bits;
   ctx->stage = 1;
   return GD_OK;
@@ -366,7 +371,7 @@ gd_status expand_run(gd_ctx* ctx) {
   const int cp = gdl::launches_per_cell_phase(ctx->dims);
   // core, parent init, 2 union passes, compress, merge replay, roots, scan,
   // label, core occupancy (with tables), border
-  ctx->launches += 2 * cp + 1 + 4 * cp + 1 + 1 + 1 + 3 + 1 + (ctx->bi.table_total ? 1 : 0) + 2 * cp;
+  ctx->launches += 2 * cp + 1 + 4 * cp + 1 + 1 + 1 + 3 + 1 + (ctx->bi.occ_total ? 1 : 0) + 2 * cp;
   ctx->stage = 2;
   if (ctx->graphs && ctx->xgraph) {
     GD_CUDA(cudaGraphLaunch(ctx->xgraph, s), "expand graph launch");
@@ -711,7 +716,7 @@ gd_status gd_index_build(gd_ctx* ctx, const gd_points* pts, double eps) {
     ctx->stage = 1;
     return GD_OK;
   }
-  GD_TRY(build_run(ctx, (uint64_t)1 << 26, 8));
+  GD_TRY(build_run(ctx, (uint64_t)1 << 26, kCellsPerPoint));
   cudaEventRecord(ctx->ev[2], ctx->stream);
   return GD_OK;
 }
@@ -808,7 +813,7 @@ gd_status gd_batch_dbscan(gd_ctx* ctx, int32_t count, const gd_instance* inst,
     if (stats) *stats = ctx->st;
     return GD_OK;
   }
-  GD_TRY(build_run(ctx, 4096, 8));
+  GD_TRY(build_run(ctx, 4096, kCellsPerPoint));
   cudaEventRecord(ctx->ev[2], ctx->stream);
   GD_TRY(expand_run(ctx));
   GD_TRY(finish_run(ctx, labels, nullptr, on_device));

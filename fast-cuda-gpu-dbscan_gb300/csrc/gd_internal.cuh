@@ -51,7 +51,9 @@ struct BatchInfo {
   int32_t LB;          // local key bits (widest instance grid)
   int32_t IB;          // instance-id bits
   int32_t key64;       // 1: keys are 64-bit
-  uint64_t table_total;// entries of all dense cell tables together
+  uint64_t occ_total;  // occupancy bits of all instances (cells of cell tables,
+                       // rows of row tables)
+  uint64_t start_total;// entries of all start tables (rows+1 per row table, 1 otherwise)
   int32_t any_sparse;  // some instance uses the hash of occupied cells
   int32_t flags;       // OR of the instances' kFlag* bits
   int32_t any_xf;      // some instance wants the centred float32 copy
@@ -91,7 +93,11 @@ struct DevParams {
   int64_t pt_off;      // first point (global index)
   int64_t n;           // points
   int64_t co_off;      // first coordinate in the concatenated buffer
-  uint64_t table_off;  // dense grids: first entry of this instance's cell table
+  uint64_t occ_off;    // first occupancy bit of this instance (cell table: C+1 bits,
+                       // row table: rows+1)
+  uint64_t start_off;  // first start-table entry (row table: rows+1 entries, else 1)
+  int64_t m0;          // first non-empty cell of the instance (index into reps)
+  int64_t rank_off;    // cell table: a cell's index into reps = occupancy rank + rank_off
   uint64_t kmask;      // mask of the local key bits
   int32_t LB;          // local key bits of the run (copied from BatchInfo)
   int32_t inst;        // instance index
@@ -149,9 +155,9 @@ __device__ __forceinline__ PredParams pred_params(const DevParams& P) {
   return q;
 }
 
-// A grid too large for a cell table takes a table of its rows when there are at
-// most this many times the cell-table limit's points-per-cell rows per point.
-constexpr uint64_t kRowTablePerCell = 8;
+// A grid too large for a cell table takes a table of its rows when it has at
+// most this many rows per point (or the table floor).
+constexpr uint64_t kRowsPerPoint = 64;
 
 constexpr int kFlagNonFinite = 1;     // NaN or Inf coordinate
 constexpr int kFlagGridTooLarge = 2;  // keys would not fit 62 bits

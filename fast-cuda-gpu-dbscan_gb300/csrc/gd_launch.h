@@ -30,11 +30,13 @@ struct Bufs {
   uint32_t* M = nullptr;        // number of non-empty cells (device scalar)
   uint32_t* runfl = nullptr;    // 1 where a cell starts (per sorted position)
   uint32_t* runpos = nullptr;   // exclusive scan of runfl: cell index = runpos+runfl-1
-  uint32_t* start = nullptr;    // dense grids: cell tables of all dense instances
-  uint32_t* occ = nullptr;      // occupancy bit per cell- or row-table entry
-  uint32_t* cocc = nullptr;     // the same for entries holding a core point (after the
-                                // core phase; border search)
-  uint64_t occ_words = 0;       // words of occ (and of cocc); 0 without tables
+  uint32_t* start = nullptr;    // row tables: first sorted position per row (scanned);
+                                // other instances: one entry holding n
+  uint32_t* occ = nullptr;      // occupancy bit per cell (cell tables) or row (row tables)
+  uint32_t* cocc = nullptr;     // the same for cells / rows holding a core point (after
+                                // the core phase; border search)
+  uint32_t* wpre = nullptr;     // per occ word: set bits in the words before it
+  uint64_t occ_words = 0;       // words of occ (and of cocc, wpre); 0 without tables
   unsigned long long* hkeys = nullptr;  // sparse grids: row hash slots (key of the row's first cell)
   uint32_t* hvals = nullptr;            // sparse grids: row hash slots (begin, end) pairs
   uint32_t hmask = 0;                   // sparse grids: slots - 1
@@ -59,6 +61,11 @@ struct Bufs {
   int tn_core = 256, tn_link = 48, tn_border = 160;
 };
 
+// Words of the occupancy buffer (occ | cocc | wpre) for W occupancy words, and
+// the offset of wpre: 256-byte aligned, as the scan reads it in 16-byte vectors.
+inline uint64_t occ_wpre_offset(uint64_t W) { return (2 * W + 63) & ~uint64_t(63); }
+inline uint64_t occ_buffer_words(uint64_t W) { return occ_wpre_offset(W) + W; }
+
 // per-instance bounding boxes, grids and the run layout
 void grids(const Bufs& B, int K, int nchunks, double mult2, double mult3, uint64_t dense_floor,
            uint64_t dense_per_point, cudaStream_t s);
@@ -68,8 +75,11 @@ void gather(const Bufs& B, bool key64, int64_t n, bool xf, int sms, cudaStream_t
 void run_flags(const void* keys, bool key64, int64_t n, uint32_t* fl, int sms, cudaStream_t s);
 // cell starts (reps), cell count, and the split between 2D and 3D cells
 void run_scatter(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
-// cell counts into the instances' table slices (scan them afterwards)
+// occupancy bits, row-table counts (scan them afterwards) and each instance's first cell
 void cell_counts(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
+// occupancy ranks: word prefix counts (scan temp: scan_temp_bytes(occ_words)) and each
+// cell table's rank offset
+void occ_rank(const Bufs& B, int K, void* scan_temp, cudaStream_t s);
 // sparse instances: hash of occupied rows (clear the slots first)
 void hash_insert(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
 // cell phases; dims: bit 0 = 2D instances present, bit 1 = 3D

@@ -59,7 +59,8 @@ constexpr size_t kOffX = kOffVals1 + up(kMaxPoints * 4);
 constexpr size_t kOffXf = kOffX + up(kMaxPoints * 3 * 8);
 constexpr size_t kOffTable = kOffXf + up(kMaxPoints * 3 * 4);
 constexpr size_t kOffOcc = kOffTable + up((kTableCells + 1) * 4);
-constexpr size_t kOffHkeys = kOffOcc + up(2 * (kTableCells / 32 + 1) * 4);  // occupancy, core occupancy
+// occupancy, core occupancy, word prefix counts
+constexpr size_t kOffHkeys = kOffOcc + up((3 * (kTableCells / 32 + 1) + 64) * 4);
 constexpr size_t kOffHvals = kOffHkeys + up(kHashSlots * 8);
 constexpr size_t kOffReps = kOffHvals + up(kHashSlots * 8);
 constexpr size_t kOffRunfl = kOffReps + up((kMaxPoints + 1) * 4);
@@ -220,9 +221,10 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   B.reps = reinterpret_cast<int*>(base + kOffReps);
   B.start = reinterpret_cast<uint32_t*>(base + kOffTable);
   B.occ = reinterpret_cast<uint32_t*>(base + kOffOcc);
-  if (bi.table_total) {
-    B.occ_words = bi.table_total / 32 + 1;
+  if (bi.occ_total) {
+    B.occ_words = bi.occ_total / 32 + 1;
     B.cocc = B.occ + B.occ_words;
+    B.wpre = B.occ + gdl::occ_wpre_offset(B.occ_words);
   }
   B.hkeys = reinterpret_cast<unsigned long long*>(base + kOffHkeys);
   B.hvals = reinterpret_cast<uint32_t*>(base + kOffHvals);
@@ -231,13 +233,12 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   gdl::run_flags(skeys, key64, n, B.runfl, sms, s);
   gdprim::exclusive_scan_u32(B.runfl, B.runpos, n, base + kOffScanTemp, dM, s);
   gdl::run_scatter(B, key64, n, sms, s);
-  if (bi.table_total) {
-    NA_CUDA(cudaMemsetAsync(B.start, 0, bi.table_total * 4, s), "clear cell table");
-    NA_CUDA(cudaMemsetAsync(B.occ, 0, (bi.table_total / 32 + 1) * 4, s), "clear occupancy");
-    gdl::cell_counts(B, key64, n, sms, s);
-    gdprim::exclusive_scan_u32(B.start, B.start, (int64_t)bi.table_total, base + kOffScanTemp,
-                               nullptr, s);
-  }
+  NA_CUDA(cudaMemsetAsync(B.start, 0, bi.start_total * 4, s), "clear row table");
+  if (B.occ_words) NA_CUDA(cudaMemsetAsync(B.occ, 0, B.occ_words * 4, s), "clear occupancy");
+  gdl::cell_counts(B, key64, n, sms, s);
+  gdprim::exclusive_scan_u32(B.start, B.start, (int64_t)bi.start_total, base + kOffScanTemp,
+                             nullptr, s);
+  gdl::occ_rank(B, 1, base + kOffScanTemp, s);
   if (bi.any_sparse) {
     NA_CUDA(cudaMemsetAsync(B.hkeys, 0xff, kHashSlots * 8, s), "clear row hash");
     gdl::hash_insert(B, key64, n, sms, s);

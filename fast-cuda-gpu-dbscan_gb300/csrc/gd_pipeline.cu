@@ -29,6 +29,7 @@
 //                rounding band around eps^2 are re-tested with the float64
 //                predicate.  Outside the band the float32 decision provably
 //                equals the float64 one, so labels stay bit-exact.
+#include <algorithm>
 #include <cfloat>
 #include <climits>
 
@@ -141,7 +142,7 @@ __global__ void k_params_inst(const gdl::Bufs B, int K, double mult2, double mul
     p.sparse = 0;
   } else {
     // a grid too large for a cell table may still take a table of its rows
-    uint64_t rlimit = (uint64_t)I.n * dense_per_point * kRowTablePerCell;
+    uint64_t rlimit = dense_per_point ? (uint64_t)I.n * kRowsPerPoint : 0;
     if (rlimit < dense_floor) rlimit = dense_floor;
     p.sparse = (fl & kFlagGridTooLarge) || p.rows > rlimit ? 1 : 2;
   }
@@ -207,7 +208,10 @@ __global__ void k_params_inst(const gdl::Bufs B, int K, double mult2, double mul
     p.prune = (!(fl & kFlagNoShortcut) && uerr <= 1.0 / 256.0 && R < 1e30 && e2 > 1e-30) ? 1 : 0;
   }
   p.flags = fl;
-  p.table_off = 0;
+  p.occ_off = 0;
+  p.start_off = 0;
+  p.m0 = 0;
+  p.rank_off = 0;
   p.kmask = 0;
   p.LB = 0;
   B.Pv[i] = p;
@@ -216,9 +220,9 @@ __global__ void k_params_inst(const gdl::Bufs B, int K, double mult2, double mul
 // One block: the run layout -- key widths, cell-table offsets (exclusive scan
 // over every instance's table length), flags.
 __global__ void __launch_bounds__(1024) k_layout(const gdl::Bufs B, int K) {
-  __shared__ unsigned long long s_part[32];
+  __shared__ unsigned long long s_part[32], s_part2[32];
   __shared__ int s_red[4][32];
-  __shared__ unsigned long long s_carry;
+  __shared__ unsigned long long s_carry, s_carry2;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int lb = 0, fl = 0, sp = 0, xf = 0, md = 2, k2 = 0;
   for (int i = threadIdx.x; i < K; i += blockDim.x) {
@@ -268,51 +272,75 @@ __global__ void __launch_bounds__(1024) k_layout(const gdl::Bufs B, int K) {
     bi.max_dim = MD;
     bi.K2 = K2;
     bi.band_off = (F >> 18) & 1;
-    bi.table_total = 0;
+    bi.occ_total = 0;
+    bi.start_total = 0;
     *B.Bi = bi;
     s_carry = 0;
+    s_carry2 = 0;
   }
   __syncthreads();
   const int LB = B.Bi->LB;
   const uint64_t kmask = LB >= 64 ? ~0ull : ((1ull << LB) - 1ull);
-  // exclusive scan of the dense-table sizes, 1024 instances at a time
+  // exclusive scans of the table sizes, 1024 instances at a time: occupancy
+  // bits (C+1 per cell table, rows+1 per row table, none for the hash) and
+  // start entries (rows+1 per row table, else one entry holding the point
+  // count, so the start scan stays in sorted-position units)
   for (int base = 0; base < K; base += 1024) {
     const int i = base + threadIdx.x;
-    unsigned long long v = 0;
-    // a dense instance's table has C+1 entries (rows+1 for a row table); a
-    // hashed instance keeps one entry holding its point count, so the scan
-    // stays in sorted-position units
-    if (i < K) v = B.Pv[i].sparse == 1 ? 1 : (B.Pv[i].sparse == 2 ? B.Pv[i].rows : B.Pv[i].C) + 1;
-    unsigned long long inc = v;
+    unsigned long long vo = 0, vs = 0;
+    if (i < K) {
+      const DevParams& p = B.Pv[i];
+      vo = p.sparse == 1 ? 0 : (p.sparse == 2 ? p.rows : p.C) + 1;
+      vs = p.sparse == 2 ? p.rows + 1 : 1;
+    }
+    unsigned long long io = vo, is = vs;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      unsigned long long t = __shfl_up_sync(kFull, inc, o);
-      if (lane >= o) inc += t;
+      const unsigned long long t = __shfl_up_sync(kFull, io, o), u = __shfl_up_sync(kFull, is, o);
+      if (lane >= o) {
+        io += t;
+        is += u;
+      }
     }
-    if (lane == 31) s_part[w] = inc;
+    if (lane == 31) {
+      s_part[w] = io;
+      s_part2[w] = is;
+    }
     __syncthreads();
     if (w == 0) {
-      unsigned long long t = s_part[lane];
-      unsigned long long ti = t;
+      const unsigned long long t = s_part[lane], u = s_part2[lane];
+      unsigned long long ti = t, ui = u;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        unsigned long long u = __shfl_up_sync(kFull, ti, o);
-        if (lane >= o) ti += u;
+        const unsigned long long a = __shfl_up_sync(kFull, ti, o), c = __shfl_up_sync(kFull, ui, o);
+        if (lane >= o) {
+          ti += a;
+          ui += c;
+        }
       }
       s_part[lane] = ti - t;
+      s_part2[lane] = ui - u;
     }
     __syncthreads();
-    const unsigned long long ex = s_carry + s_part[w] + inc - v;
+    const unsigned long long eo = s_carry + s_part[w] + io - vo;
+    const unsigned long long es = s_carry2 + s_part2[w] + is - vs;
     if (i < K) {
-      B.Pv[i].table_off = ex;
+      B.Pv[i].occ_off = eo;
+      B.Pv[i].start_off = es;
       B.Pv[i].kmask = kmask;
       B.Pv[i].LB = LB;
     }
     __syncthreads();
-    if (threadIdx.x == 1023) s_carry = ex + v;
+    if (threadIdx.x == 1023) {
+      s_carry = eo + vo;
+      s_carry2 = es + vs;
+    }
     __syncthreads();
   }
-  if (threadIdx.x == 0) B.Bi->table_total = s_carry;
+  if (threadIdx.x == 0) {
+    B.Bi->occ_total = s_carry;
+    B.Bi->start_total = s_carry2;
+  }
 }
 
 // ------------------------------------------------------------------ keys
@@ -400,34 +428,58 @@ __global__ void k_split(const gdl::Bufs B) {
   B.ctr[kCtrCells2D] = (unsigned long long)lo;
 }
 
-// Cell counts into the instances' table slices (scanned afterwards into start
-// positions): per cell for a cell table, per row for a row table.  A hashed
-// instance's one-entry slice holds its point count.
+// Cell tables: one occupancy bit per non-empty cell (a cell's points are then
+// found by rank, see GridView::rank).  Row tables: one occupancy bit and a
+// point count per non-empty row (the counts are scanned into start positions
+// afterwards).  Every other instance's one-entry start slice holds its point
+// count.  Also records each instance's first cell.
 template <class Key>
 __global__ void k_cell_counts(const gdl::Bufs B) {
   const Key* keys = static_cast<const Key*>(B.keys);
   const int LB = B.Bi->LB;
   const int K = B.Bi->K;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x)
-    if (B.Pv[i].sparse == 1) B.start[B.Pv[i].table_off] = (uint32_t)B.Pv[i].n;
+    if (B.Pv[i].sparse != 2) B.start[B.Pv[i].start_off] = (uint32_t)B.Pv[i].n;
   const int64_t M = *B.M;
   for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
        m += (int64_t)gridDim.x * blockDim.x) {
     const int b = B.reps[m], e = B.reps[m + 1];
     const Key key = keys[b];
-    const DevParams& P = B.Pv[inst_of(key, LB)];
+    const int inst = inst_of(key, LB);
+    DevParams& P = B.Pv[inst];
+    if (m == 0 || inst_of(keys[B.reps[m - 1]], LB) != inst) P.m0 = m;
     if (P.sparse == 1) continue;
     const uint64_t local = (uint64_t)key & P.kmask;
     if (P.sparse == 2) {
       const int a = P.dim - 2;
-      const uint64_t idx = P.table_off + udiv_by(local, P.dm[a], P.ds[a]);
-      atomicAdd(B.start + idx, (uint32_t)(e - b));
+      const uint64_t row = udiv_by(local, P.dm[a], P.ds[a]);
+      atomicAdd(B.start + P.start_off + row, (uint32_t)(e - b));
+      const uint64_t idx = P.occ_off + row;
       atomicOr(B.occ + (idx >> 5), 1u << (idx & 31));
       continue;
     }
-    const uint64_t idx = P.table_off + local;
-    B.start[idx] = (uint32_t)(e - b);
+    const uint64_t idx = P.occ_off + local;
     atomicOr(B.occ + (idx >> 5), 1u << (idx & 31));
+  }
+}
+
+// Occupancy ranks: set bits per word, scanned afterwards into wpre.
+__global__ void k_occ_popc(const gdl::Bufs B) {
+  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < (int64_t)B.occ_words;
+       w += (int64_t)gridDim.x * blockDim.x)
+    B.wpre[w] = (uint32_t)__popc(B.occ[w]);
+}
+
+// A cell table's cells appear in reps in table order from the instance's first
+// cell on, so a cell's index into reps is its occupancy rank minus the rank of
+// the table's first bit plus that first cell.
+__global__ void k_rank_off(const gdl::Bufs B, int K) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x) {
+    DevParams& P = B.Pv[i];
+    if (P.sparse != 0 || P.n == 0) continue;
+    const uint64_t idx = P.occ_off, w = idx >> 5;
+    const int64_t r = (int64_t)B.wpre[w] + __popc(B.occ[w] & ((1u << (idx & 31)) - 1u));
+    P.rank_off = P.m0 - r;
   }
 }
 
@@ -653,6 +705,7 @@ struct GridView {
   const uint32_t* start;
   const uint32_t* occ;
   const uint32_t* cocc;    // core occupancy (valid in the border search only)
+  const uint32_t* wpre;
   const unsigned long long* hkeys;
   const uint32_t* hvals;   // per slot: row begin, row end
   const int* reps;
@@ -660,7 +713,9 @@ struct GridView {
   uint32_t hmask;
   int sparse;              // DevParams::sparse
   int key64;
-  uint64_t table_off;
+  uint64_t occ_off;
+  uint64_t start_off;
+  int64_t rank_off;
   uint64_t hi;             // instance id << LB
   int64_t Gl;              // cells along the last axis
   uint64_t glm;            // division by Gl (udiv_by)
@@ -670,12 +725,22 @@ struct GridView {
     return key64 ? static_cast<const unsigned long long*>(keys)[i]
                  : (uint64_t) static_cast<const uint32_t*>(keys)[i];
   }
+  // cell table: index into reps of the first non-empty cell at or after
+  // local key k (its rank among the occupied cells)
+  __device__ __forceinline__ int64_t rank(uint64_t k) const {
+    const uint64_t idx = occ_off + k, w = idx >> 5;
+    return (int64_t)wpre[w] + __popc(occ[w] & ((1u << (idx & 31)) - 1u)) + rank_off;
+  }
+  __device__ __forceinline__ bool occupied(uint64_t k) const {
+    const uint64_t idx = occ_off + k;
+    return (occ[idx >> 5] >> (idx & 31)) & 1u;
+  }
   // row table or hash: points [begin, end) of the row whose first cell is rowkey
   __device__ __forceinline__ int2 row(uint64_t rowkey) const {
     if (sparse == 2) {
-      const uint64_t idx = table_off + udiv_by(rowkey, glm, gls);
+      const uint64_t r = udiv_by(rowkey, glm, gls), idx = occ_off + r;
       if (!((occ[idx >> 5] >> (idx & 31)) & 1u)) return make_int2(0, 0);
-      return make_int2((int)start[idx], (int)start[idx + 1]);
+      return make_int2((int)start[start_off + r], (int)start[start_off + r + 1]);
     }
     const unsigned long long k = hi | rowkey;
     uint32_t h = hash_key(k) & hmask;
@@ -689,7 +754,7 @@ struct GridView {
   }
   // core occupancy bits of cells z0..z1 of a cell-table row (bit z - z0)
   __device__ __forceinline__ uint32_t core_cells(uint64_t rowkey, int64_t z0, int64_t z1) const {
-    const uint64_t i0 = table_off + rowkey + (uint64_t)z0;
+    const uint64_t i0 = occ_off + rowkey + (uint64_t)z0;
     const int len = (int)(z1 - z0) + 1;  // <= 5
     const uint64_t w = i0 >> 5;
     const int sh = (int)(i0 & 31);
@@ -699,7 +764,7 @@ struct GridView {
   }
   // row table: whether the row whose first cell is rowkey holds a core point
   __device__ __forceinline__ bool core_row(uint64_t rowkey) const {
-    const uint64_t idx = table_off + udiv_by(rowkey, glm, gls);
+    const uint64_t idx = occ_off + udiv_by(rowkey, glm, gls);
     return (cocc[idx >> 5] >> (idx & 31)) & 1u;
   }
   // first sorted position in [b, e) whose key is >= g
@@ -715,7 +780,7 @@ struct GridView {
   // contiguous range, because no other key sorts between them
   __device__ __forceinline__ int2 span_row(uint64_t rowkey, int64_t z0, int64_t z1) const {
     if (!sparse)
-      return make_int2((int)start[table_off + rowkey + z0], (int)start[table_off + rowkey + z1 + 1]);
+      return make_int2(reps[rank(rowkey + z0)], reps[rank(rowkey + z1 + 1)]);
     const int2 r = row(rowkey);
     if (r.x == r.y) return r;
     const int a = lower(r.x, r.y, hi | (rowkey + (uint64_t)z0));
@@ -725,17 +790,16 @@ struct GridView {
   // points of the cell with local key k: [x, y)
   __device__ __forceinline__ int2 cell(uint64_t k) const {
     if (!sparse) {
-      const uint64_t idx = table_off + k;
-      if (!((occ[idx >> 5] >> (idx & 31)) & 1u)) return make_int2(0, 0);
-      return make_int2((int)start[idx], (int)start[idx + 1]);
+      if (!occupied(k)) return make_int2(0, 0);
+      const int64_t r = rank(k);
+      return make_int2(reps[r], reps[r + 1]);
     }
     const int64_t z = (int64_t)(k - udiv_by(k, glm, gls) * (uint64_t)Gl);
     return span_row(k - (uint64_t)z, z, z);
   }
   // points of the cells k0..k1 (consecutive local keys along one row)
   __device__ __forceinline__ int2 span(uint64_t k0, uint64_t k1) const {
-    if (!sparse)
-      return make_int2((int)start[table_off + k0], (int)start[table_off + k1 + 1]);
+    if (!sparse) return make_int2(reps[rank(k0)], reps[rank(k1 + 1)]);
     const int64_t z0 = (int64_t)(k0 - udiv_by(k0, glm, gls) * (uint64_t)Gl);
     return span_row(k0 - (uint64_t)z0, z0, z0 + (int64_t)(k1 - k0));
   }
@@ -743,9 +807,9 @@ struct GridView {
 
 __device__ __forceinline__ GridView view_of(const gdl::Bufs& B, const DevParams& P) {
   const int a = P.dim - 2;
-  return GridView{B.start, B.occ, B.cocc, B.hkeys, B.hvals, B.reps, B.keys, B.hmask, P.sparse,
-                  B.Bi->key64, P.table_off, (uint64_t)P.inst << P.LB, P.G[P.dim - 1],
-                  P.dm[a], P.ds[a]};
+  return GridView{B.start, B.occ, B.cocc, B.wpre, B.hkeys, B.hvals, B.reps, B.keys, B.hmask,
+                  P.sparse, B.Bi->key64, P.occ_off, P.start_off, P.rank_off,
+                  (uint64_t)P.inst << P.LB, P.G[P.dim - 1], P.dm[a], P.ds[a]};
 }
 
 template <bool KEY64>
@@ -1486,8 +1550,8 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
           while (cm && !over) {
             const int z = __ffs(cm) - 1;
             cm &= cm - 1;
-            const uint64_t idx = gv.table_off + (uint64_t)rk + (uint64_t)(rw.l0 + z);
-            const int q = (int)gv.start[idx], qe = (int)gv.start[idx + 1];
+            const int64_t rq = gv.rank((uint64_t)rk + (uint64_t)(rw.l0 + z));
+            const int q = gv.reps[rq], qe = gv.reps[rq + 1];
             const int cB = B.cellcid[q];
             if (cB >= best) continue;
             int cls = 0;
@@ -1849,7 +1913,7 @@ __global__ void k_core_occ(const gdl::Bufs B) {
     if (P.sparse == 1) continue;
     const uint64_t local = key & P.kmask;
     const int a = P.dim - 2;
-    const uint64_t idx = P.table_off + (P.sparse == 2 ? udiv_by(local, P.dm[a], P.ds[a]) : local);
+    const uint64_t idx = P.occ_off + (P.sparse == 2 ? udiv_by(local, P.dm[a], P.ds[a]) : local);
     atomicOr(B.cocc + (idx >> 5), 1u << (idx & 31));
   }
 }
@@ -2085,6 +2149,14 @@ void run_scatter(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) 
 void cell_counts(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) {
   if (key64) k_cell_counts<unsigned long long><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
   else k_cell_counts<uint32_t><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
+}
+
+void occ_rank(const Bufs& B, int K, void* scan_temp, cudaStream_t s) {
+  if (!B.occ_words) return;
+  const int g = (int)std::min<int64_t>(((int64_t)B.occ_words + 255) / 256, 4096);
+  k_occ_popc<<<g, 256, 0, s>>>(B);
+  gdprim::exclusive_scan_u32(B.wpre, B.wpre, (int64_t)B.occ_words, scan_temp, nullptr, s);
+  k_rank_off<<<(K + 127) / 128, 128, 0, s>>>(B, K);
 }
 
 void hash_insert(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) {

@@ -81,7 +81,8 @@ typedef struct gd_stats {
   int64_t asym_pairs;       /* core pairs that are neighbours in one direction only
                                (the box test and the distance test disagree at the
                                last bit; their merges are replayed in order) */
-  int64_t grid_cells;       /* entries of the cell / row tables (1 per hashed grid) */
+  int64_t grid_cells;       /* occupancy-table entries: cells of cell tables, rows of
+                               row tables (a hashed grid has none) */
   int32_t precision_used;   /* gd_precision actually run */
   int32_t key_bits;         /* radix-sort key width */
   int32_t launches;         /* kernel launches of the last pipeline run */

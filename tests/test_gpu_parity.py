@@ -184,9 +184,9 @@ def test_sparse_grid_vs_oracle(gpu_ctx, oracle, prec, d, extent, hashed):
     st = gpu_ctx.stats()
     assert st["key_bits"] > 26                      # beyond the dense cell table
     if hashed:
-        assert st["grid_cells"] == 1                # one-entry slice: the hash
+        assert st["grid_cells"] == 0                # no occupancy table: the hash
     else:
-        assert 1 < st["grid_cells"] < 2 ** 27       # rows + 1
+        assert 1 < st["grid_cells"] < 2 ** 27       # one occupancy bit per row (+1)
     olab, ocore, _ = oracle.oracle_dbscan(pts, 0.05, 6)
     assert np.array_equal(core, ocore)
     assert np.array_equal(lab, olab)
