@@ -752,6 +752,21 @@ struct GridView {
     }
     return make_int2(0, 0);
   }
+  // cell table: occupancy bits of cells z0..z1 (at most 5) of the row whose
+  // first cell is rowkey (bit z - z0), and the reps index of the first
+  // occupied one (the others follow it in reps)
+  __device__ __forceinline__ uint32_t occ_cells(uint64_t rowkey, int64_t z0, int64_t z1,
+                                                int64_t& r0) const {
+    const uint64_t i0 = occ_off + rowkey + (uint64_t)z0, w = i0 >> 5;
+    const int len = (int)(z1 - z0) + 1;
+    const int sh = (int)(i0 & 31);
+    const uint32_t lo = occ[w];
+    uint64_t bits = lo >> sh;
+    if (sh + len > 32) bits |= (uint64_t)occ[w + 1] << (32 - sh);
+    const uint32_t mask = (uint32_t)bits & ((1u << len) - 1u);
+    if (mask) r0 = (int64_t)wpre[w] + __popc(lo & ((1u << sh) - 1u)) + rank_off;
+    return mask;
+  }
   // core occupancy bits of cells z0..z1 of a cell-table row (bit z - z0)
   __device__ __forceinline__ uint32_t core_cells(uint64_t rowkey, int64_t z0, int64_t z1) const {
     const uint64_t i0 = occ_off + rowkey + (uint64_t)z0;
@@ -1231,13 +1246,10 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
           }
           const int64_t rk = rw.rowkey(T, r, P);
           if (rk < 0) continue;
-          const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
-          for (int q = sp.x; q < sp.y && cnt < Q.minpts && !over;) {
-            const int qe = cell_end<KEY64>(B, q);
+          // one non-empty cell [q, qe) at last-axis offset d from the point's cell
+          auto visit = [&](int q, int qe, int d) {
             int cls = 0;
             if (prune) {
-              const int d =
-                  (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
               const float smax = rmx + sel5(lmx, d), smin = rmn + sel5(lmn, d);
               cls = smax <= Q.thr_in ? 1 : (smin >= Q.thr_out ? -1 : 0);
             }
@@ -1249,6 +1261,26 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
               ++nq;
               ptot += qe - q;
             }
+          };
+          if (gv.sparse == 0) {
+            // cell table: the row's occupied cells from its occupancy bits
+            int64_t rr = 0;
+            uint32_t mask = gv.occ_cells((uint64_t)rk, rw.l0, rw.l1, rr);
+            while (mask && cnt < Q.minpts && !over) {
+              const int z = __ffs(mask) - 1;
+              mask &= mask - 1;
+              visit(B.reps[rr], B.reps[rr + 1], (int)(rw.l0 + z - rw.cl));
+              ++rr;
+            }
+            continue;
+          }
+          const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
+          for (int q = sp.x; q < sp.y && cnt < Q.minpts && !over;) {
+            const int qe = cell_end<KEY64>(B, q);
+            const int d = prune ? (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) -
+                                        rw.cl)
+                                : 0;
+            visit(q, qe, d);
             q = qe;
           }
         }
@@ -1464,10 +1496,8 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
           z0 = z0 < rw.l0 ? rw.l0 : z0;
           z1 = z1 > rw.l1 ? rw.l1 : z1;
           if (z0 > z1) continue;
-          const int2 sp = gv.span_row((uint64_t)rk, z0, z1);
-          for (int q = sp.x; q < sp.y;) {
-            const int qe = cell_end<KEY64>(B, q);
-            const int d = (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
+          // one non-empty cell [q, qe) at last-axis offset d
+          auto visit = [&](int q, int qe, int d) {
             const int bit = D == 3 ? half_bit<D>(pass, ox, oy, d) : half_bit<D>(pass, ox, d, 0);
             if (bit >= 0 && B.cellcore[q] > 0 &&
                 uf_find(B.parent, b) != uf_find(B.parent, q)) {
@@ -1476,6 +1506,23 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
               if (res > 0) uf_union(B.parent, B.cellmin, b, q);
               else if (res < 0) open |= 1ull << bit;
             }
+          };
+          if (gv.sparse == 0) {
+            // cell table: the occupied cells from the occupancy bits
+            int64_t rr = 0;
+            uint32_t mask = gv.occ_cells((uint64_t)rk, z0, z1, rr);
+            while (mask) {
+              const int z = __ffs(mask) - 1;
+              mask &= mask - 1;
+              visit(B.reps[rr], B.reps[rr + 1], (int)(z0 + z - rw.cl));
+              ++rr;
+            }
+            continue;
+          }
+          const int2 sp = gv.span_row((uint64_t)rk, z0, z1);
+          for (int q = sp.x; q < sp.y;) {
+            const int qe = cell_end<KEY64>(B, q);
+            visit(q, qe, (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl));
             q = qe;
           }
           }
