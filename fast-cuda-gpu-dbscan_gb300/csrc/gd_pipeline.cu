@@ -1274,12 +1274,16 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
             }
             continue;
           }
-          const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
-          for (int q = sp.x; q < sp.y && cnt < Q.minpts && !over;) {
+          // row table or hash: the row's points, from the first cell at or
+          // after the stencil's first last-axis cell to the first beyond it
+          const int2 rp = gv.row((uint64_t)rk);
+          if (rp.x == rp.y) continue;
+          const int dmax = (int)(rw.l1 - rw.cl);
+          for (int q = gv.lower(rp.x, rp.y, gv.hi | ((uint64_t)rk + (uint64_t)rw.l0));
+               q < rp.y && cnt < Q.minpts && !over;) {
+            const int d = (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
+            if (d > dmax) break;
             const int qe = cell_end<KEY64>(B, q);
-            const int d = prune ? (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) -
-                                        rw.cl)
-                                : 0;
             visit(q, qe, d);
             q = qe;
           }
@@ -1468,6 +1472,7 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
         rw.init(decompose<D>(cx.local, P), P);
         float oA[D];
         if (Q.prune) cell_origin32<D>(rw.cc, P, oA);
+        int ra = uf_find(B.parent, b);
         for (int r = 0; r < T.n; ++r) {
           const int ox = T.o[r][0], oy = T.o[r][1];
           // rows with a negative leading offset hold no half-stencil cell
@@ -1499,12 +1504,19 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
           // one non-empty cell [q, qe) at last-axis offset d
           auto visit = [&](int q, int qe, int d) {
             const int bit = D == 3 ? half_bit<D>(pass, ox, oy, d) : half_bit<D>(pass, ox, d, 0);
-            if (bit >= 0 && B.cellcore[q] > 0 &&
-                uf_find(B.parent, b) != uf_find(B.parent, q)) {
-              const int res = D == 3 ? inline_link<D, F32>(B, n, b, e, q, qe, oA, ox, oy, d, Q, t)
-                                     : inline_link<D, F32>(B, n, b, e, q, qe, oA, ox, d, 0, Q, t);
-              if (res > 0) uf_union(B.parent, B.cellmin, b, q);
-              else if (res < 0) open |= 1ull << bit;
+            if (bit < 0 || B.cellcore[q] <= 0) return;
+            // ra: a root of A's set, refreshed only when q's root differs
+            const int rq = uf_find(B.parent, q);
+            if (rq == ra) return;
+            ra = uf_find(B.parent, ra);
+            if (rq == ra) return;
+            const int res = D == 3 ? inline_link<D, F32>(B, n, b, e, q, qe, oA, ox, oy, d, Q, t)
+                                   : inline_link<D, F32>(B, n, b, e, q, qe, oA, ox, d, 0, Q, t);
+            if (res > 0) {
+              uf_union(B.parent, B.cellmin, b, q);
+              ra = uf_find(B.parent, ra);
+            } else if (res < 0) {
+              open |= 1ull << bit;
             }
           };
           if (gv.sparse == 0) {
@@ -1628,15 +1640,18 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
           continue;
         }
         if (gv.sparse == 2 && !gv.core_row((uint64_t)rk)) continue;
-        const int2 sp = gv.span_row((uint64_t)rk, rw.l0, rw.l1);
-        for (int q = sp.x; q < sp.y && !over;) {
+        const int2 rp = gv.row((uint64_t)rk);
+        if (rp.x == rp.y) continue;
+        const int dmax = (int)(rw.l1 - rw.cl);
+        for (int q = gv.lower(rp.x, rp.y, gv.hi | ((uint64_t)rk + (uint64_t)rw.l0));
+             q < rp.y && !over;) {
+          const int d = (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
+          if (d > dmax) break;
           const int qe = cell_end<KEY64>(B, q);
           const int cB = B.cellcore[q] > 0 ? B.cellcid[q] : INT_MAX;
           if (cB < best) {
             int cls = 0;
             if (prune) {
-              const int d =
-                  (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
               const float smax = rmx + sel5(lmx, d), smin = rmn + sel5(lmn, d);
               cls = smax <= Q.thr_in ? 1 : (smin >= Q.thr_out ? -1 : 0);
             }
