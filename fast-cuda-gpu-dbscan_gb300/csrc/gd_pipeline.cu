@@ -362,7 +362,7 @@ __global__ void __launch_bounds__(256) k_keys(const gdl::Bufs B, Key* __restrict
     for (int k = 0; k < 3; ++k) {
       if (k >= D) break;
       const double t = __dmul_rn(__dsub_rn(pts[l * D + k], lo[k]), inv_f);
-      int64_t q = (int64_t)floor(t);
+      int64_t q = __double2ll_rd(t);  // floor and convert in one step (t is finite)
       q = q < 0 ? 0 : (q >= G[k] ? G[k] - 1 : q);
       key = key * (uint64_t)G[k] + (uint64_t)q;
     }

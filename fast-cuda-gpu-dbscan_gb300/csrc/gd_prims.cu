@@ -149,21 +149,23 @@ __global__ void __launch_bounds__(kRsThreads)
 k_rs_upsweep(const K* __restrict__ keys, int64_t n, int shift, uint32_t* __restrict__ hist,
              int64_t T) {
   constexpr int SEG = 32 * ITEMS, TILE = kRsThreads * ITEMS;
-  __shared__ uint32_t h[kRsBins];
+  // warp-private digit counts (shared-memory atomics), summed at the end
+  __shared__ uint32_t h[kRsWarps][kRsBins];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  h[threadIdx.x] = 0;
+#pragma unroll
+  for (int ww = 0; ww < kRsWarps; ++ww) h[ww][threadIdx.x] = 0;
   __syncthreads();
   const int64_t seg = (int64_t)blockIdx.x * TILE + w * SEG;
 #pragma unroll 4
   for (int i = 0; i < ITEMS; ++i) {
-    int64_t e = seg + i * 32 + lane;
-    bool valid = e < n;
-    uint32_t d = valid ? (uint32_t)(__ldg(keys + e) >> shift) & 0xffu : 0x100u;
-    unsigned peers = __match_any_sync(gd::kFull, d);
-    if (valid && lane == __ffs(peers) - 1) atomicAdd(&h[d], (uint32_t)__popc(peers));
+    const int64_t e = seg + i * 32 + lane;
+    if (e < n) atomicAdd(&h[w][(uint32_t)(__ldg(keys + e) >> shift) & 0xffu], 1u);
   }
   __syncthreads();
-  hist[(int64_t)threadIdx.x * T + blockIdx.x] = h[threadIdx.x];
+  uint32_t tot = 0;
+#pragma unroll
+  for (int ww = 0; ww < kRsWarps; ++ww) tot += h[ww][threadIdx.x];
+  hist[(int64_t)threadIdx.x * T + blockIdx.x] = tot;
 }
 
 template <class K, int ITEMS>
@@ -201,7 +203,13 @@ k_rs_downsweep(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
     uint32_t d = (uint32_t)(k[i] >> shift) & 0xffu;
-    unsigned peers = __match_any_sync(gd::kFull, d);
+    // lanes holding the same digit: one ballot per digit bit
+    unsigned peers = gd::kFull;
+#pragma unroll
+    for (int bit = 0; bit < 8; ++bit) {
+      const unsigned bb = __ballot_sync(gd::kFull, (d >> bit) & 1u);
+      peers &= ((d >> bit) & 1u) ? bb : ~bb;
+    }
     uint32_t b = s_cnt[w][d];
     __syncwarp();
     if (lane == __ffs(peers) - 1) s_cnt[w][d] = b + (uint32_t)__popc(peers);
