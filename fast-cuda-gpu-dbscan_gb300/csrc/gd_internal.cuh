@@ -105,6 +105,11 @@ struct DevParams {
   // udiv_magic): multiplier and shift per divisor
   uint64_t dm[2];
   int32_t ds[2];
+  // float32 cell origins without float64 arithmetic (cell_origin32): the cell
+  // side and lo - centre per axis as float pairs (hi + lo), valid when fast_origin
+  float f_hi, f_lo;
+  float b_hi[3], b_lo[3];
+  int32_t fast_origin;
 };
 
 // Division by an invariant integer d >= 1 through a multiply-high (Granlund &

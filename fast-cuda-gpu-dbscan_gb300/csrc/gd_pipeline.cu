@@ -178,7 +178,9 @@ __global__ void k_params_inst(const gdl::Bufs B, int K, double mult2, double mul
     // float64 predicate.  When the bound is not small every pair takes it.
     const double u32 = 1.0 / 16777216.0;               // 2^-24
     R = R * (1.0 + 1e-12) + 1e-300;
-    const double ea = R * u32 * (1.0 + 1e-8);          // |fl32(x - c) - (x - c)|
+    // |fl32(x - c) - (x - c)| and the error of a float32 cell origin (either
+    // way of computing it, see cell_origin32), with a small margin
+    const double ea = R * u32 * (1.0 + 1.0 / 65536.0);
     const double e2 = p.eps2;
     const double rs = sqrt(2.0 * e2) * sqrt((double)D);
     double bmax = (2.0 * e2 + 4.0 * ea * rs + 4.0 * D * ea * ea) * (D + 3) * u32
@@ -206,6 +208,20 @@ __global__ void k_params_inst(const gdl::Bufs B, int K, double mult2, double mul
     p.thr_in = __double2float_rd(inv_m2 * mi * mi * (1.0 - 1.0 / 65536.0));
     p.thr_out = __double2float_ru(inv_m2 * mo * mo * (1.0 + 1.0 / 65536.0));
     p.prune = (!(fl & kFlagNoShortcut) && uerr <= 1.0 / 256.0 && R < 1e30 && e2 > 1e-30) ? 1 : 0;
+  }
+  {
+    // float pairs for cell_origin32's float32 path: every cell index below 2^24
+    // (exact in float) and magnitudes far from float under- and overflow
+    bool fast = p.f >= 0x1p-60 && p.f <= 0x1p60;
+    p.f_hi = __double2float_rn(p.f);
+    p.f_lo = __double2float_rn(p.f - (double)p.f_hi);
+    for (int k = 0; k < 3; ++k) {
+      const double b = k < D ? p.lo[k] - p.centre[k] : 0.0;
+      fast = fast && p.G[k] < (1 << 24) && fabs(b) <= 0x1p60;
+      p.b_hi[k] = __double2float_rn(b);
+      p.b_lo[k] = __double2float_rn(b - (double)p.b_hi[k]);
+    }
+    p.fast_origin = fast ? 1 : 0;
   }
   p.flags = fl;
   p.occ_off = 0;
@@ -1003,6 +1019,28 @@ constexpr int kCellThreads = kWarpsPerBlock * 32;
 // Origin (low corner) of cell cc in the centred float32 frame.
 template <int D>
 __device__ __forceinline__ void cell_origin32(const CellXYZ<D>& cc, const DevParams& P, float* o) {
+  if (P.fast_origin) {
+    // o = fl32((lo - centre) + c f) from float pairs: c f_hi by an exact
+    // two-product (fma), added to b_hi by an exact two-sum, the small terms
+    // (product error, c f_lo, b_lo) summed in float; one final rounding.  The
+    // result is within |o| 2^-24 (1 + 2^-20) of the exact value (c < 2^24 is
+    // exact in float; the pairs carry 48 bits), which the position error
+    // bound (uerr, via ea) covers.
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      const float c = (float)(int)cc.c[k];
+      const float p = __fmul_rn(c, P.f_hi);
+      const float e = __fmaf_rn(c, P.f_hi, -p);
+      const float q = __fmul_rn(c, P.f_lo);
+      const float a = P.b_hi[k];
+      const float s = __fadd_rn(a, p);
+      const float v = __fsub_rn(s, a);
+      const float t = __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(p, v));
+      const float low = __fadd_rn(__fadd_rn(t, e), __fadd_rn(q, P.b_lo[k]));
+      o[k] = __fadd_rn(s, low);
+    }
+    return;
+  }
 #pragma unroll
   for (int k = 0; k < D; ++k)
     o[k] = __double2float_rn(
