@@ -1172,17 +1172,23 @@ __device__ __forceinline__ float sel5(const float (&a)[5], int d) {
   return r;
 }
 
-constexpr int kCoreQueue = 8;  // undecided cells a point queues before testing them
+// undecided cells a point queues before testing them: float64 tests are
+// costly off the warp-cooperative final flush, float32 ones are cheap enough
+// that an early exit matters more
+__host__ __device__ constexpr int core_queue(bool f32) { return f32 ? 8 : 16; }
 constexpr int kCoreWarps = kScanThreadsPerBlock / 32;
 
 // Per-warp staging of the final flush: the points whose core decision waits on
-// their queued cells, with their predicate constants (lanes of one warp may
-// belong to different instances).
-template <int D>
+// their queued cells, with their instances (lanes of one warp may belong to
+// different instances; the predicate constants are read from Pv).
+template <int D, bool F32>
 struct CoreFlushStage {
   double x[32][D];
   float f[32][D];
-  PredParams q[32];
+  // float32 mode (short queue): the predicate constants themselves; float64
+  // mode (long queue, less shared memory left): the instance, constants from Pv
+  PredParams q[F32 ? 32 : 1];
+  int inst[32];
   int cnt[32];    // neighbours counted so far
   int incl[32];   // inclusive prefix of the queued candidate counts
   int nq[32];
@@ -1207,12 +1213,12 @@ struct CoreFlushStage {
 // are warp-aggregated atomics (cleared before the launch).
 template <int D, bool F32, bool KEY64>
 __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_core_point(const gdl::Bufs B, int64_t n) {
-  __shared__ int2 sq[kCoreQueue][kScanThreadsPerBlock];
-  __shared__ CoreFlushStage<D> stage[kCoreWarps];
+  __shared__ int2 sq[core_queue(F32)][kScanThreadsPerBlock];
+  __shared__ CoreFlushStage<D, F32> stage[kCoreWarps];
   const OffTab& T = kRows[D - 2];
   const int lane = threadIdx.x & 31;
   const int wbase = threadIdx.x & ~31;
-  CoreFlushStage<D>& S = stage[threadIdx.x >> 5];
+  CoreFlushStage<D, F32>& S = stage[threadIdx.x >> 5];
   const int LB = B.Bi->LB;
   int64_t mlo, mhi;
   dim_range<D>(B, mlo, mhi);
@@ -1294,7 +1300,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
             if (cls > 0) {
               cnt += qe - q;
             } else if (cls == 0) {
-              if (nq == kCoreQueue) flush();
+              if (nq == core_queue(F32)) flush();
               sq[nq][threadIdx.x] = make_int2(q, qe);
               ++nq;
               ptot += qe - q;
@@ -1334,7 +1340,8 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
             S.x[lane][k] = px[k];
             S.f[lane][k] = pf[k];
           }
-          S.q[lane] = Q;
+          if constexpr (F32) S.q[lane] = Q;
+          else S.inst[lane] = P.inst;
         }
         isc = !over && cnt >= Q.minpts;
       }
@@ -1370,7 +1377,9 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
               else lo = mid + 1;
             }
             const int ow = lo;
-            const PredParams& Qo = S.q[ow];
+            PredParams Qo;
+            if constexpr (F32) Qo = S.q[ow];
+            else Qo = pred_params(B.Pv[S.inst[ow]]);
             if (S.cnt[ow] < Qo.minpts) {
               int k = c - (ow > 0 ? S.incl[ow - 1] : 0);  // candidate index within the owner's queue
               int qq = -1;
