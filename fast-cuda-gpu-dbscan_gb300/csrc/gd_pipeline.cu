@@ -751,6 +751,17 @@ struct GridView {
     const uint64_t idx = occ_off + k;
     return (occ[idx >> 5] >> (idx & 31)) & 1u;
   }
+  // row table: points [begin, end) of row ri
+  __device__ __forceinline__ int2 row_at(uint64_t ri) const {
+    const uint64_t idx = occ_off + ri;
+    if (!((occ[idx >> 5] >> (idx & 31)) & 1u)) return make_int2(0, 0);
+    return make_int2((int)start[start_off + ri], (int)start[start_off + ri + 1]);
+  }
+  // row table: whether row ri holds a core point
+  __device__ __forceinline__ bool core_row_at(uint64_t ri) const {
+    const uint64_t idx = occ_off + ri;
+    return (cocc[idx >> 5] >> (idx & 31)) & 1u;
+  }
   // row table or hash: points [begin, end) of the row whose first cell is rowkey
   __device__ __forceinline__ int2 row(uint64_t rowkey) const {
     if (sparse == 2) {
@@ -1142,6 +1153,16 @@ struct RowWalk {
     const int64_t k = offset_key<D>(cc, T.o[r][0], T.o[r][1], 0, P);
     return k < 0 ? k : k - cl;
   }
+  // index of row r among the grid's rows (its first cell's key is index * G[D-1]),
+  // or -1 when the row is outside the grid
+  __device__ __forceinline__ int64_t rowidx(const OffTab& T, int r, const DevParams& P) const {
+    const int64_t x = cc.c[0] + T.o[r][0];
+    if (x < 0 || x >= P.G[0]) return -1;
+    if (D == 2) return x;
+    const int64_t y = cc.c[1] + T.o[r][1];
+    if (y < 0 || y >= P.G[1]) return -1;
+    return x * P.G[1] + y;
+  }
 };
 
 // next cell of a row walk: [q, end), its last-axis offset from the cell in work
@@ -1288,8 +1309,9 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
             }
             if (rmn >= Q.thr_out) continue;  // the whole row is beyond eps
           }
-          const int64_t rk = rw.rowkey(T, r, P);
-          if (rk < 0) continue;
+          const int64_t ri = rw.rowidx(T, r, P);
+          if (ri < 0) continue;
+          const int64_t rk = ri * P.G[D - 1];  // key of the row's first cell
           // one non-empty cell [q, qe) at last-axis offset d from the point's cell
           auto visit = [&](int q, int qe, int d) {
             int cls = 0;
@@ -1320,7 +1342,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
           }
           // row table or hash: the row's points, from the first cell at or
           // after the stencil's first last-axis cell to the first beyond it
-          const int2 rp = gv.row((uint64_t)rk);
+          const int2 rp = gv.sparse == 2 ? gv.row_at((uint64_t)ri) : gv.row((uint64_t)rk);
           if (rp.x == rp.y) continue;
           const int dmax = (int)(rw.l1 - rw.cl);
           for (int q = gv.lower(rp.x, rp.y, gv.hi | ((uint64_t)rk + (uint64_t)rw.l0));
@@ -1648,8 +1670,9 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
           }
           if (rmn >= Q.thr_out) continue;  // the whole row is beyond eps
         }
-        const int64_t rk = rw.rowkey(T, r, P);
-        if (rk < 0) continue;
+        const int64_t ri = rw.rowidx(T, r, P);
+        if (ri < 0) continue;
+        const int64_t rk = ri * P.G[D - 1];  // key of the row's first cell
         if (gv.sparse == 0) {
           // cell table: visit only the cells holding a core point
           uint32_t cm = gv.core_cells((uint64_t)rk, rw.l0, rw.l1);
@@ -1686,8 +1709,8 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
           }
           continue;
         }
-        if (gv.sparse == 2 && !gv.core_row((uint64_t)rk)) continue;
-        const int2 rp = gv.row((uint64_t)rk);
+        if (gv.sparse == 2 && !gv.core_row_at((uint64_t)ri)) continue;
+        const int2 rp = gv.sparse == 2 ? gv.row_at((uint64_t)ri) : gv.row((uint64_t)rk);
         if (rp.x == rp.y) continue;
         const int dmax = (int)(rw.l1 - rw.cl);
         for (int q = gv.lower(rp.x, rp.y, gv.hi | ((uint64_t)rk + (uint64_t)rw.l0));
