@@ -85,7 +85,8 @@ struct gd_ctx {
   double mult2 = kDefaultCellMult, mult3 = kDefaultCellMult;
   int tn_core = kDefaultCoreTests, tn_link = kDefaultLinkTests, tn_border = kDefaultBorderTests;
 
-  DevBuf coords, inst, chunks, Pv, Bi, bbox, keys0, keys1, vals0, vals1, X, Xf, table, occ, hkeys,
+  DevBuf coords, inst, chunks, Pv, Bi, bbox, keys0, keys1, vals0, vals1, X, Xf, table, occ, cellz,
+      hkeys,
       hvals, reps, runfl, runpos, core, cellcore, cellmin, parent, Fmark, cellcid, lab, asym,
       hvcell, hvmask, out, coreout, sorttemp, scantemp, small, kcount;
 
@@ -133,7 +134,7 @@ struct gd_ctx {
 
   void free_all(bool keep_small) {
     DevBuf* a[] = {&coords, &inst,   &chunks,   &Pv,      &Bi,     &bbox,     &keys0,
-                   &keys1,  &vals0,  &vals1,    &X,       &Xf,     &table,    &occ, &hkeys,
+                   &keys1,  &vals0,  &vals1,    &X,       &Xf,     &table,    &occ, &cellz, &hkeys,
                    &hvals,  &reps,   &runfl,    &runpos,  &core,   &cellcore, &cellmin,
                    &parent, &Fmark,  &cellcid,  &lab,     &asym,   &hvcell,   &hvmask,
                    &out,    &coreout, &sorttemp, &scantemp, &small, &kcount};
@@ -170,6 +171,7 @@ struct gd_ctx {
     B.runpos = static_cast<uint32_t*>(runpos.p);
     B.start = static_cast<uint32_t*>(table.p);
     B.occ = static_cast<uint32_t*>(occ.p);
+    B.cellz = static_cast<uint32_t*>(cellz.p);
     if (bi.occ_total) {
       // one buffer: occupancy | core occupancy | word prefix counts
       B.occ_words = bi.occ_total / 32 + 1;
@@ -275,6 +277,7 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
   }
   ctx->hmask = (uint32_t)(hcap - 1);
   GD_TRY(ctx->ensure(ctx->reps, (n + 1) * 4, "cell reps"));
+  GD_TRY(ctx->ensure(ctx->cellz, n * 4, "cell coordinates"));
   GD_TRY(ctx->ensure(ctx->runfl, n * 4, "run flags"));
   GD_TRY(ctx->ensure(ctx->runpos, n * 4, "run positions"));
   GD_TRY(ctx->ensure(ctx->sorttemp, gdprim::sort_temp_bytes(n), "sort temp"));
@@ -307,10 +310,11 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
   GD_CUDA(cudaMemsetAsync(ctx->table.p, 0, bi.start_total * 4, s), "clear row tables");
   if (W) GD_CUDA(cudaMemsetAsync(ctx->occ.p, 0, W * 4, s), "clear occupancy");
   gdl::cell_counts(B, ctx->key64, n, ctx->sms, s);
+  gdl::start_fill(B, ctx->K, s);
   gdprim::exclusive_scan_u32(B.start, B.start, (int64_t)bi.start_total, ctx->scantemp.p, nullptr,
                              s);
   gdl::occ_rank(B, ctx->K, ctx->scantemp.p, s);
-  int table_launches = 4 + (W ? 5 : 0);
+  int table_launches = 5 + (W ? 5 : 0);
   if (bi.any_sparse) {
     GD_CUDA(cudaMemsetAsync(ctx->hkeys.p, 0xff, hcap * 8, s), "clear row hash");
     gdl::hash_insert(B, ctx->key64, n, ctx->sms, s);

@@ -97,6 +97,7 @@ struct DevParams {
                        // row table: rows+1)
   uint64_t start_off;  // first start-table entry (row table: rows+1 entries, else 1)
   int64_t m0;          // first non-empty cell of the instance (index into reps)
+  int64_t m1;          // last non-empty cell of the instance
   int64_t rank_off;    // cell table: a cell's index into reps = occupancy rank + rank_off
   uint64_t kmask;      // mask of the local key bits
   int32_t LB;          // local key bits of the run (copied from BatchInfo)

@@ -30,8 +30,9 @@ struct Bufs {
   uint32_t* M = nullptr;        // number of non-empty cells (device scalar)
   uint32_t* runfl = nullptr;    // 1 where a cell starts (per sorted position)
   uint32_t* runpos = nullptr;   // exclusive scan of runfl: cell index = runpos+runfl-1
-  uint32_t* start = nullptr;    // row tables: first sorted position per row (scanned);
-                                // other instances: one entry holding n
+  uint32_t* start = nullptr;    // row tables: first cell (index into reps) per row, after
+                                // the scan; other instances: one entry holding their cells
+  uint32_t* cellz = nullptr;    // per non-empty cell: its last-axis coordinate
   uint32_t* occ = nullptr;      // occupancy bit per cell (cell tables) or row (row tables)
   uint32_t* cocc = nullptr;     // the same for cells / rows holding a core point (after
                                 // the core phase; border search)
@@ -75,8 +76,10 @@ void gather(const Bufs& B, bool key64, int64_t n, bool xf, int sms, cudaStream_t
 void run_flags(const void* keys, bool key64, int64_t n, uint32_t* fl, int sms, cudaStream_t s);
 // cell starts (reps), cell count, and the split between 2D and 3D cells
 void run_scatter(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
-// occupancy bits, row-table counts (scan them afterwards) and each instance's first cell
+// occupancy bits, row-table cell counts, cellz, each instance's first and last cells
 void cell_counts(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
+// one-entry start slices (cell counts of instances without a row table); then scan
+void start_fill(const Bufs& B, int K, cudaStream_t s);
 // occupancy ranks: word prefix counts (scan temp: scan_temp_bytes(occ_words)) and each
 // cell table's rank offset
 void occ_rank(const Bufs& B, int K, void* scan_temp, cudaStream_t s);

@@ -63,7 +63,8 @@ constexpr size_t kOffOcc = kOffTable + up((kTableCells + 1) * 4);
 constexpr size_t kOffHkeys = kOffOcc + up((3 * (kTableCells / 32 + 1) + 64) * 4);
 constexpr size_t kOffHvals = kOffHkeys + up(kHashSlots * 8);
 constexpr size_t kOffReps = kOffHvals + up(kHashSlots * 8);
-constexpr size_t kOffRunfl = kOffReps + up((kMaxPoints + 1) * 4);
+constexpr size_t kOffCellz = kOffReps + up((kMaxPoints + 1) * 4);
+constexpr size_t kOffRunfl = kOffCellz + up(kMaxPoints * 4);
 constexpr size_t kOffRunpos = kOffRunfl + up(kMaxPoints * 4);
 constexpr size_t kOffCore = kOffRunpos + up(kMaxPoints * 4);
 constexpr size_t kOffCellcore = kOffCore + up(kMaxPoints);
@@ -219,6 +220,7 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   B.runfl = reinterpret_cast<uint32_t*>(base + kOffRunfl);
   B.runpos = reinterpret_cast<uint32_t*>(base + kOffRunpos);
   B.reps = reinterpret_cast<int*>(base + kOffReps);
+  B.cellz = reinterpret_cast<uint32_t*>(base + kOffCellz);
   B.start = reinterpret_cast<uint32_t*>(base + kOffTable);
   B.occ = reinterpret_cast<uint32_t*>(base + kOffOcc);
   if (bi.occ_total) {
@@ -236,6 +238,7 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   NA_CUDA(cudaMemsetAsync(B.start, 0, bi.start_total * 4, s), "clear row table");
   if (B.occ_words) NA_CUDA(cudaMemsetAsync(B.occ, 0, B.occ_words * 4, s), "clear occupancy");
   gdl::cell_counts(B, key64, n, sms, s);
+  gdl::start_fill(B, 1, s);
   gdprim::exclusive_scan_u32(B.start, B.start, (int64_t)bi.start_total, base + kOffScanTemp,
                              nullptr, s);
   gdl::occ_rank(B, 1, base + kOffScanTemp, s);

@@ -227,6 +227,7 @@ __global__ void k_params_inst(const gdl::Bufs B, int K, double mult2, double mul
   p.occ_off = 0;
   p.start_off = 0;
   p.m0 = 0;
+  p.m1 = -1;
   p.rank_off = 0;
   p.kmask = 0;
   p.LB = 0;
@@ -445,37 +446,44 @@ __global__ void k_split(const gdl::Bufs B) {
 }
 
 // Cell tables: one occupancy bit per non-empty cell (a cell's points are then
-// found by rank, see GridView::rank).  Row tables: one occupancy bit and a
-// point count per non-empty row (the counts are scanned into start positions
-// afterwards).  Every other instance's one-entry start slice holds its point
-// count.  Also records each instance's first cell.
+// found by rank, see GridView::rank).  Row tables: one occupancy bit and a cell
+// count per non-empty row (scanned afterwards into each row's first cell).
+// Every cell's last-axis coordinate goes to cellz, and each instance's first
+// and last cells are recorded (k_start_fill turns them into the one-entry start
+// slices of the other instances, so the scan stays in cell units).
 template <class Key>
 __global__ void k_cell_counts(const gdl::Bufs B) {
   const Key* keys = static_cast<const Key*>(B.keys);
   const int LB = B.Bi->LB;
-  const int K = B.Bi->K;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x)
-    if (B.Pv[i].sparse != 2) B.start[B.Pv[i].start_off] = (uint32_t)B.Pv[i].n;
   const int64_t M = *B.M;
   for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
        m += (int64_t)gridDim.x * blockDim.x) {
-    const int b = B.reps[m], e = B.reps[m + 1];
-    const Key key = keys[b];
+    const Key key = keys[B.reps[m]];
     const int inst = inst_of(key, LB);
     DevParams& P = B.Pv[inst];
     if (m == 0 || inst_of(keys[B.reps[m - 1]], LB) != inst) P.m0 = m;
-    if (P.sparse == 1) continue;
+    if (m == M - 1 || inst_of(keys[B.reps[m + 1]], LB) != inst) P.m1 = m;
     const uint64_t local = (uint64_t)key & P.kmask;
+    const int a = P.dim - 2;
+    const uint64_t row = udiv_by(local, P.dm[a], P.ds[a]);
+    B.cellz[m] = (uint32_t)(local - row * (uint64_t)P.G[P.dim - 1]);
+    if (P.sparse == 1) continue;
     if (P.sparse == 2) {
-      const int a = P.dim - 2;
-      const uint64_t row = udiv_by(local, P.dm[a], P.ds[a]);
-      atomicAdd(B.start + P.start_off + row, (uint32_t)(e - b));
+      atomicAdd(B.start + P.start_off + row, 1u);
       const uint64_t idx = P.occ_off + row;
       atomicOr(B.occ + (idx >> 5), 1u << (idx & 31));
       continue;
     }
     const uint64_t idx = P.occ_off + local;
     atomicOr(B.occ + (idx >> 5), 1u << (idx & 31));
+  }
+}
+
+// One-entry start slices (instances without a row table): their cell count.
+__global__ void k_start_fill(const gdl::Bufs B, int K) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x) {
+    const DevParams& P = B.Pv[i];
+    if (P.sparse != 2) B.start[P.start_off] = P.n > 0 ? (uint32_t)(P.m1 - P.m0 + 1) : 0u;
   }
 }
 
@@ -719,6 +727,7 @@ __device__ __forceinline__ int warp_min_i32(int v) {
 // it.  The probe loop is bounded by the table size.
 struct GridView {
   const uint32_t* start;
+  const uint32_t* cellz;   // per cell: last-axis coordinate
   const uint32_t* occ;
   const uint32_t* cocc;    // core occupancy (valid in the border search only)
   const uint32_t* wpre;
@@ -751,24 +760,28 @@ struct GridView {
     const uint64_t idx = occ_off + k;
     return (occ[idx >> 5] >> (idx & 31)) & 1u;
   }
-  // row table: points [begin, end) of row ri
-  __device__ __forceinline__ int2 row_at(uint64_t ri) const {
+  // row table: cells [begin, end) (indices into reps) of row ri
+  __device__ __forceinline__ int2 row_cells(uint64_t ri) const {
     const uint64_t idx = occ_off + ri;
     if (!((occ[idx >> 5] >> (idx & 31)) & 1u)) return make_int2(0, 0);
     return make_int2((int)start[start_off + ri], (int)start[start_off + ri + 1]);
+  }
+  // first cell in [b, e) (one row's cells) whose last-axis coordinate is >= z
+  __device__ __forceinline__ int zlower(int b, int e, int64_t z) const {
+    while (b < e) {
+      const int mid = (int)(((unsigned)b + (unsigned)e) >> 1);
+      if ((int64_t)cellz[mid] < z) b = mid + 1;
+      else e = mid;
+    }
+    return b;
   }
   // row table: whether row ri holds a core point
   __device__ __forceinline__ bool core_row_at(uint64_t ri) const {
     const uint64_t idx = occ_off + ri;
     return (cocc[idx >> 5] >> (idx & 31)) & 1u;
   }
-  // row table or hash: points [begin, end) of the row whose first cell is rowkey
+  // hash: points [begin, end) of the row whose first cell is rowkey
   __device__ __forceinline__ int2 row(uint64_t rowkey) const {
-    if (sparse == 2) {
-      const uint64_t r = udiv_by(rowkey, glm, gls), idx = occ_off + r;
-      if (!((occ[idx >> 5] >> (idx & 31)) & 1u)) return make_int2(0, 0);
-      return make_int2((int)start[start_off + r], (int)start[start_off + r + 1]);
-    }
     const unsigned long long k = hi | rowkey;
     uint32_t h = hash_key(k) & hmask;
     for (uint32_t probe = 0; probe <= hmask; ++probe) {
@@ -823,6 +836,12 @@ struct GridView {
   __device__ __forceinline__ int2 span_row(uint64_t rowkey, int64_t z0, int64_t z1) const {
     if (!sparse)
       return make_int2(reps[rank(rowkey + z0)], reps[rank(rowkey + z1 + 1)]);
+    if (sparse == 2) {
+      const int2 rc = row_cells(udiv_by(rowkey, glm, gls));
+      if (rc.x == rc.y) return make_int2(0, 0);
+      const int ma = zlower(rc.x, rc.y, z0), mb = zlower(ma, rc.y, z1 + 1);
+      return make_int2(reps[ma], reps[mb]);
+    }
     const int2 r = row(rowkey);
     if (r.x == r.y) return r;
     const int a = lower(r.x, r.y, hi | (rowkey + (uint64_t)z0));
@@ -849,7 +868,7 @@ struct GridView {
 
 __device__ __forceinline__ GridView view_of(const gdl::Bufs& B, const DevParams& P) {
   const int a = P.dim - 2;
-  return GridView{B.start, B.occ, B.cocc, B.wpre, B.hkeys, B.hvals, B.reps, B.keys, B.hmask,
+  return GridView{B.start, B.cellz, B.occ, B.cocc, B.wpre, B.hkeys, B.hvals, B.reps, B.keys, B.hmask,
                   P.sparse, B.Bi->key64, P.occ_off, P.start_off, P.rank_off,
                   (uint64_t)P.inst << P.LB, P.G[P.dim - 1], P.dm[a], P.ds[a]};
 }
@@ -1340,9 +1359,20 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
             }
             continue;
           }
-          // row table or hash: the row's points, from the first cell at or
-          // after the stencil's first last-axis cell to the first beyond it
-          const int2 rp = gv.sparse == 2 ? gv.row_at((uint64_t)ri) : gv.row((uint64_t)rk);
+          if (gv.sparse == 2) {
+            // row table: the row's cells from the first at or after l0 to l1
+            const int2 rc = gv.row_cells((uint64_t)ri);
+            for (int mq = gv.zlower(rc.x, rc.y, rw.l0); mq < rc.y && cnt < Q.minpts && !over;
+                 ++mq) {
+              const int64_t z = gv.cellz[mq];
+              if (z > rw.l1) break;
+              visit(B.reps[mq], B.reps[mq + 1], (int)(z - rw.cl));
+            }
+            continue;
+          }
+          // hash: the row's points, from the first cell at or after l0 to the
+          // first beyond l1
+          const int2 rp = gv.row((uint64_t)rk);
           if (rp.x == rp.y) continue;
           const int dmax = (int)(rw.l1 - rw.cl);
           for (int q = gv.lower(rp.x, rp.y, gv.hi | ((uint64_t)rk + (uint64_t)rw.l0));
@@ -1710,7 +1740,45 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
           continue;
         }
         if (gv.sparse == 2 && !gv.core_row_at((uint64_t)ri)) continue;
-        const int2 rp = gv.sparse == 2 ? gv.row_at((uint64_t)ri) : gv.row((uint64_t)rk);
+        // one non-empty cell [q, qe) at last-axis offset d
+        auto visitb = [&](int q, int qe, int d) {
+          const int cB = B.cellcore[q] > 0 ? B.cellcid[q] : INT_MAX;
+          if (cB >= best) return;
+          int cls = 0;
+          if (prune) {
+            const float smax = rmx + sel5(lmx, d), smin = rmn + sel5(lmn, d);
+            cls = smax <= Q.thr_in ? 1 : (smin >= Q.thr_out ? -1 : 0);
+          }
+          if (cls > 0) {
+            best = cB;  // every point of that cell, a core among them, is in reach
+          } else if (cls == 0) {
+            for (int qq = q; qq < qe; ++qq) {
+              if (!B.core[qq]) continue;
+              if (budget-- == 0) {
+                over = true;
+                break;
+              }
+              Cand<D, F32> cd;
+              load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
+              if (pair_test<D, F32>(px, pf, cd, B.X, n, qq, false, Q, t)) {
+                best = cB;
+                break;
+              }
+            }
+          }
+        };
+        if (gv.sparse == 2) {
+          // row table: the row's cells from the first at or after l0 to l1
+          const int2 rc = gv.row_cells((uint64_t)ri);
+          for (int mq = gv.zlower(rc.x, rc.y, rw.l0); mq < rc.y && !over; ++mq) {
+            const int64_t z = gv.cellz[mq];
+            if (z > rw.l1) break;
+            visitb(B.reps[mq], B.reps[mq + 1], (int)(z - rw.cl));
+          }
+          continue;
+        }
+        // hash: the row's points from the first cell at or after l0
+        const int2 rp = gv.row((uint64_t)rk);
         if (rp.x == rp.y) continue;
         const int dmax = (int)(rw.l1 - rw.cl);
         for (int q = gv.lower(rp.x, rp.y, gv.hi | ((uint64_t)rk + (uint64_t)rw.l0));
@@ -1718,31 +1786,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
           const int d = (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
           if (d > dmax) break;
           const int qe = cell_end<KEY64>(B, q);
-          const int cB = B.cellcore[q] > 0 ? B.cellcid[q] : INT_MAX;
-          if (cB < best) {
-            int cls = 0;
-            if (prune) {
-              const float smax = rmx + sel5(lmx, d), smin = rmn + sel5(lmn, d);
-              cls = smax <= Q.thr_in ? 1 : (smin >= Q.thr_out ? -1 : 0);
-            }
-            if (cls > 0) {
-              best = cB;  // every point of that cell, a core among them, is in reach
-            } else if (cls == 0) {
-              for (int qq = q; qq < qe; ++qq) {
-                if (!B.core[qq]) continue;
-                if (budget-- == 0) {
-                  over = true;
-                  break;
-                }
-                Cand<D, F32> cd;
-                load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
-                if (pair_test<D, F32>(px, pf, cd, B.X, n, qq, false, Q, t)) {
-                  best = cB;
-                  break;
-                }
-              }
-            }
-          }
+          visitb(q, qe, d);
           q = qe;
         }
       }
@@ -2281,6 +2325,10 @@ void run_scatter(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) 
 void cell_counts(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) {
   if (key64) k_cell_counts<unsigned long long><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
   else k_cell_counts<uint32_t><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
+}
+
+void start_fill(const Bufs& B, int K, cudaStream_t s) {
+  k_start_fill<<<(K + 127) / 128, 128, 0, s>>>(B, K);
 }
 
 void occ_rank(const Bufs& B, int K, void* scan_temp, cudaStream_t s) {
