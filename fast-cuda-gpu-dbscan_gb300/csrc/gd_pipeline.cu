@@ -1630,6 +1630,16 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
             }
             continue;
           }
+          if (gv.sparse == 2) {
+            // row table: the row's cells with last-axis coordinate in [z0, z1]
+            const int2 rc = gv.row_cells(udiv_by((uint64_t)rk, gv.glm, gv.gls));
+            for (int mq = gv.zlower(rc.x, rc.y, z0); mq < rc.y; ++mq) {
+              const int64_t z = gv.cellz[mq];
+              if (z > z1) break;
+              visit(B.reps[mq], B.reps[mq + 1], (int)(z - rw.cl));
+            }
+            continue;
+          }
           const int2 sp = gv.span_row((uint64_t)rk, z0, z1);
           for (int q = sp.x; q < sp.y;) {
             const int qe = cell_end<KEY64>(B, q);
