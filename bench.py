@@ -55,10 +55,12 @@ METRIC = "points/sec at exact labels"
 # kernels of each timed phase (the library records CUDA events between phases)
 PHASE_KERNELS = {
     "ms_index": "k_bbox_chunk, k_params_inst, k_layout, k_keys, radix sort, k_gather, "
-                "k_run_flags, scan, k_run_scatter, k_cell_counts, scan, k_row_hash",
+                "k_run_flags, scan, k_run_scatter, k_cell_counts, k_start_fill, scan, "
+                "k_occ_popc, scan, k_rank_off, k_row_hash",
     "ms_core": "k_core_point + k_core_heavy",
     "ms_union": "k_parent_init, k_union_scan x2, k_union_heavy x2, k_asym_resolve, k_compress",
-    "ms_label": "k_roots, scan, k_label, k_border_point, k_border_heavy, k_scatter_labels",
+    "ms_label": "k_roots, scan, k_label, k_core_occ, k_border_point, k_border_heavy, "
+                "k_scatter_labels",
 }
 
 
@@ -72,6 +74,25 @@ def phase_bytes_per_point(phase: str, dim: int, f32: bool) -> int:
             "ms_core": c + 1,            # coordinates in, core flag out
             "ms_union": c + 1,           # coordinates + core flag in
             "ms_label": c + 1 + 4 + 4}[phase]  # coordinates, core flag, point id in; label out
+
+
+def max_over_ranks(x: float, dist) -> float:
+    """The largest x over all ranks (one process per GPU); x itself in a
+    single-process run.  Step times are combined this way, so the job's rate is
+    set by its slowest replica."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank: float, seconds: float, world: int) -> float:
+    """Whole-job rate of `world` replicas that each process units_per_rank in
+    `seconds` (the slowest replica's time): the work is fixed per GPU (weak
+    scaling), so the total grows with the replica count."""
+    return world * units_per_rank / seconds
 
 
 def peaks():
@@ -264,7 +285,7 @@ def run_batch(args, rank, world, local, dist):
             b.record(stream)
             torch.cuda.synchronize()
             ms.append(a.elapsed_time(b))
-    t_batch = sum(ms) / len(ms)
+    t_batch = max_over_ranks(sum(ms) / len(ms), dist)
     batch_labels = d_lab.cpu().numpy()
     # the single-instance path once per instance, same device-resident data
     offs = np.cumsum([0] + [inst.n * inst.dim for inst in insts])
@@ -305,12 +326,12 @@ def run_batch(args, rank, world, local, dist):
         a = time.perf_counter()
         step_e2e()
         e2e.append(time.perf_counter() - a)
-    t_e2e = sum(e2e) / len(e2e)
+    t_e2e = max_over_ranks(sum(e2e) / len(e2e), dist)
     same_e2e = bool(np.array_equal(h_lab, batch_labels))
     peak, peak_kind = peaks()
     algo = int(sum(inst.n * (8 * inst.dim + 4) for inst in insts))
     achieved = algo / (t_batch / 1e3) / 1e9
-    value = world * ntot / (t_batch / 1e3)
+    value = job_rate(ntot, t_batch / 1e3, world)
     line = {
         "metric": METRIC + " (batched instances)", "value": value, "unit": "points/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_batch,
@@ -325,7 +346,7 @@ def run_batch(args, rank, world, local, dist):
                    {"sample": "first 256 instances", "seconds": round(tune_s, 2),
                     "sample_device_ms": tune_ms},
                    "l2": "512 MiB flush write between timed steps"},
-        "e2e": {"value": world * ntot / t_e2e, "unit": "points/s",
+        "e2e": {"value": job_rate(ntot, t_e2e, world), "unit": "points/s",
                 "h2d_bytes_per_step": int(flat.nbytes), "d2h_bytes_per_step": ntot * 4,
                 "ms_per_step": t_e2e * 1e3, "labels_equal_device_run": same_e2e},
         "looped_single_instance": {"value": ntot / t_loop, "ms_per_batch": t_loop * 1e3,
@@ -454,7 +475,8 @@ def run_serve(args, rank, world, local, dist):
     same = all(np.array_equal(a, b) for a, b in zip(s_labs, o_labs))
     total = int(npts.sum())
     sat_pts = int(npts[:sat_n].sum())
-    value = world * sat_pts / sat_server
+    sat_server = max_over_ranks(sat_server, dist)
+    value = job_rate(sat_pts, sat_server, world)
     line = {
         "metric": METRIC + " (served request stream)", "value": value, "unit": "points/s",
         "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": sat_server * 1e3,
@@ -589,11 +611,8 @@ def main():
         ms, phases = timed_device(args.steps, args.warmup)
     clocks = clk.summary()
     t_step = sum(ms) / len(ms)
-    if dist:
-        t = torch.tensor([t_step], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_step = float(t.item())
-    value = world * n / (t_step / 1e3)
+    t_step = max_over_ranks(t_step, dist)
+    value = job_rate(n, t_step / 1e3, world)
     st = phases[-1]
     ref_labels = lab_dev.cpu().numpy()
 
@@ -627,10 +646,7 @@ def main():
         step_e2e()
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = sum(e2e_times) / len(e2e_times)
-    if dist:
-        t = torch.tensor([e2e_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, dist)
     e2e_equal = bool(np.array_equal(host_lab, ref_labels))
     ctx2.close()
 
@@ -666,7 +682,7 @@ def main():
                    "minpts": inst.minpts, "precision": args.precision,
                    "parallelism": f"replicas{world}",
                    "l2": "512 MiB flush write between timed steps; inputs 160+ MB > L2"},
-        "e2e": {"value": world * n / e2e_s, "unit": "points/s",
+        "e2e": {"value": job_rate(n, e2e_s, world), "unit": "points/s",
                 "h2d_bytes_per_step": n * dim * 8, "d2h_bytes_per_step": n * 4,
                 "ms_per_step": e2e_s * 1e3, "labels_equal_device_run": e2e_equal},
         "gpu_launches": int(st["launches"]) * args.steps,
@@ -689,7 +705,8 @@ def main():
                                       "n_dense_cells", "tests_fp64", "tests_fp32",
                                       "band_retests", "asym_pairs", "key_bits")},
         "other_precision": {"precision": "fp32band" if other == gdm.GD_PREC_FP32_BAND else "fp64",
-                            "value": world * n / (sum(ms2) / len(ms2) / 1e3),
+                            "value": job_rate(n, max_over_ranks(sum(ms2) / len(ms2), dist) / 1e3,
+                                              world),
                             "ms_per_step": sum(ms2) / len(ms2),
                             "labels_identical": other_labels_equal,
                             "tests_fp32": ph2[-1]["tests_fp32"],
