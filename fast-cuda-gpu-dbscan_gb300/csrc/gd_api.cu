@@ -163,8 +163,10 @@ struct gd_ctx {
     B.bbox = static_cast<long long*>(bbox.p);
     B.keys = skeys;
     B.ids = sids;
-    // the sort's other id buffer is free after the sort
+    // the sort's other id and key buffers are free after the sort
     B.blist = static_cast<uint32_t*>(sids == vals0.p ? vals1.p : vals0.p);
+    B.lflag = static_cast<uint32_t*>(skeys == keys0.p ? keys1.p : keys0.p);
+    B.lcount = reinterpret_cast<uint32_t*>(static_cast<char*>(small.p) + 8);
     B.reps = static_cast<int*>(reps.p);
     B.M = dM();
     B.runfl = static_cast<uint32_t*>(runfl.p);
@@ -351,7 +353,7 @@ cudaError_t launch_expand(gd_ctx* ctx, bool capturing) {
   keep(cudaMemsetAsync(B.Fmark, 0, (n + 1) * 4, s));
   gdl::roots(B, n, ctx->sms, s);
   gdprim::exclusive_scan_u32(B.Fmark, B.Fmark, n + 1, ctx->scantemp.p, ctx->dK(), s);
-  gdl::label(B, ctx->key64, n, ctx->sms, s);
+  gdl::label(B, ctx->key64, n, ctx->sms, ctx->scantemp.p, s);
   gdl::border(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, s);
   keep(cudaGetLastError());
   return e;
@@ -374,8 +376,8 @@ gd_status expand_run(gd_ctx* ctx) {
                      "scan temp"));
   const int cp = gdl::launches_per_cell_phase(ctx->dims);
   // core, parent init, 2 union passes, compress, merge replay, roots, scan,
-  // label, core occupancy (with tables), border
-  ctx->launches += 2 * cp + 1 + 4 * cp + 1 + 1 + 1 + 3 + 1 + (ctx->bi.occ_total ? 1 : 0) + 2 * cp;
+  // label + list scan + scatter, core occupancy (with tables), border
+  ctx->launches += 2 * cp + 1 + 4 * cp + 1 + 1 + 1 + 3 + 5 + (ctx->bi.occ_total ? 1 : 0) + 2 * cp;
   ctx->stage = 2;
   if (ctx->graphs && ctx->xgraph) {
     GD_CUDA(cudaGraphLaunch(ctx->xgraph, s), "expand graph launch");

@@ -186,8 +186,6 @@ enum Counter {
   kCtrHeavyUnion,       // cells queued for warp-cooperative link searches
   kCtrHeavyBorder,      // cells queued for warp-cooperative border search
   kCtrCells2D,          // cells of 2D instances (they sort first)
-  kCtrBorder2,          // non-core points of 2D instances listed for the border search
-  kCtrBorder3,          // non-core points of 3D instances (listed from the back)
   kCtrCount = 16
 };
 

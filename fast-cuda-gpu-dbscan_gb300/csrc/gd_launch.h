@@ -52,8 +52,10 @@ struct Bufs {
   int* cellcid = nullptr;       // per rep: cluster id of the cell's core points
   int* lab = nullptr;           // label per sorted position
   int* asym = nullptr;          // kAsymCap (from, to) sorted-position pairs
-  uint32_t* blist = nullptr;    // non-core sorted positions for the border search (n):
-                                // 2D instances' from the front, 3D instances' from the back
+  uint32_t* blist = nullptr;    // non-core sorted positions for the border search (n), in
+                                // sorted order (2D instances' first)
+  uint32_t* lflag = nullptr;    // n: list positions (exclusive scan of the non-core flags)
+  uint32_t* lcount = nullptr;   // device scalar: list length
   int* hv_cell = nullptr;       // heavy-work list: cell index m (capacity n)
   unsigned long long* hv_mask = nullptr;  // heavy-work list: stencil offsets still open
   unsigned long long* ctr = nullptr;      // gd::Counter
@@ -89,7 +91,7 @@ void hash_insert(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
 void core(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s);
 void unite(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s);
 void roots(const Bufs& B, int64_t n, int sms, cudaStream_t s);
-void label(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
+void label(const Bufs& B, bool key64, int64_t n, int sms, void* scan_temp, cudaStream_t s);
 void border(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s);
 void scatter_labels(const Bufs& B, int64_t n, int* out, uint8_t* core_out, int sms,
                     cudaStream_t s);

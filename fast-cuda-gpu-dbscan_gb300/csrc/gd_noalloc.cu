@@ -214,7 +214,9 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   }
   B.keys = skeys;
   B.ids = vb[r];
-  B.blist = vb[1 - r];  // the sort's other id buffer is free after the sort
+  B.blist = vb[1 - r];  // the sort's other id and key buffers are free after the sort
+  B.lflag = reinterpret_cast<uint32_t*>(base + (skeys == base + kOffKeys0 ? kOffKeys1 : kOffKeys0));
+  B.lcount = reinterpret_cast<uint32_t*>(base + kOffSmall + 8);
   B.X = reinterpret_cast<double*>(base + kOffX);
   B.Xf = reinterpret_cast<float*>(base + kOffXf);
   B.runfl = reinterpret_cast<uint32_t*>(base + kOffRunfl);
@@ -263,7 +265,7 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   NA_CUDA(cudaMemsetAsync(B.Fmark, 0, (n + 1) * 4, s), "clear cluster marks");
   gdl::roots(B, n, sms, s);
   gdprim::exclusive_scan_u32(B.Fmark, B.Fmark, n + 1, base + kOffScanTemp, dK, s);
-  gdl::label(B, key64, n, sms, s);
+  gdl::label(B, key64, n, sms, base + kOffScanTemp, s);
   gdl::border(B, n, dims, f32, key64, sms, s);
   gdl::scatter_labels(B, n, labels_dev, nullptr, sms, s);
   NA_CUDA(cudaGetLastError(), "launch");

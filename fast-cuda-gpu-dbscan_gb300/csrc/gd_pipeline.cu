@@ -1668,15 +1668,20 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
   const OffTab& T = kRows[D - 2];
   const int lane = threadIdx.x & 31;
   const int LB = B.Bi->LB;
-  const int64_t L = (int64_t)B.ctr[D == 2 ? kCtrBorder2 : kCtrBorder3];
+  // this dimension's part of the list: 2D instances' points come first
+  const int64_t p3 = B.reps[(int64_t)B.ctr[kCtrCells2D]];
+  const int64_t L = (int64_t)*B.lcount;
+  const int64_t L2 = p3 < n ? (int64_t)B.lflag[p3] : L;
+  const int64_t jlo = D == 2 ? 0 : L2, jhi = D == 2 ? L2 : L;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   Tally t;
-  for (int64_t j0 = (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); j0 < L; j0 += stride) {
+  for (int64_t j0 = jlo + (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); j0 < jhi;
+       j0 += stride) {
     const int64_t j = j0 + lane;
     int m = -1;
     bool over = false;
-    if (j < L) {
-      const int64_t i = D == 2 ? (int64_t)B.blist[j] : (int64_t)B.blist[n - 1 - j];
+    if (j < jhi) {
+      const int64_t i = (int64_t)B.blist[j];
       m = (int)(B.runpos[i] + B.runfl[i]) - 1;
       const int b = B.reps[m];
       const CellCtx cx = cell_ctx<KEY64>(B, b, LB);
@@ -2084,6 +2089,15 @@ __global__ void k_roots(const gdl::Bufs B) {
 // and the provisional label of every point: its cluster if core, NOISE otherwise.
 // Cluster numbers restart at 0 in every instance: the scan value at the
 // instance's first point counts the clusters of the instances before it.
+// The border-search list: every non-core point at its scanned position, so
+// the list keeps the sorted order (neighbouring list entries are neighbouring
+// points, 2D instances' first).
+__global__ void k_list_scatter(const gdl::Bufs B, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    if (!B.core[i]) B.blist[B.lflag[i]] = (uint32_t)i;
+}
+
 // Core occupancy: one bit per cell-table (row-table) entry whose cell (row)
 // holds a core point, so the border search skips the rest without lookups.
 template <bool KEY64>
@@ -2107,40 +2121,18 @@ __global__ void k_core_occ(const gdl::Bufs B) {
 template <bool KEY64>
 __global__ void k_label(const gdl::Bufs B, int64_t n) {
   const int LB = B.Bi->LB;
-  const int lane = threadIdx.x & 31;
-  // first sorted position of a 3D instance (n when there is none)
-  const int64_t p3 = B.reps[(int64_t)B.ctr[kCtrCells2D]];
-  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); i0 < n;
-       i0 += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = i0 + lane;
-    bool nc = false;
-    if (i < n) {
-      const int b = rep_of(B, i);
-      int cl = INT_MAX;
-      if (B.cellcore[b] > 0) {
-        const int64_t pt_off = B.Pv[(int)(key_at<KEY64>(B, i) >> LB)].pt_off;
-        cl = (int)(B.Fmark[B.cellmin[uf_find(B.parent, b)]] - B.Fmark[pt_off]);
-      }
-      if (i == b) B.cellcid[b] = cl;
-      nc = !B.core[i];
-      B.lab[i] = nc ? kNoise : cl;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int b = rep_of(B, i);
+    int cl = INT_MAX;
+    if (B.cellcore[b] > 0) {
+      const int64_t pt_off = B.Pv[(int)(key_at<KEY64>(B, i) >> LB)].pt_off;
+      cl = (int)(B.Fmark[B.cellmin[uf_find(B.parent, b)]] - B.Fmark[pt_off]);
     }
-    // list the non-core points for the border search: 2D instances' from the
-    // front, 3D instances' from the back
-    const bool is3 = i >= p3;
-    const unsigned b2 = __ballot_sync(kFull, nc && !is3), b3 = __ballot_sync(kFull, nc && is3);
-    unsigned long long at2 = 0, at3 = 0;
-    if (lane == 0) {
-      if (b2) at2 = atomicAdd(B.ctr + kCtrBorder2, (unsigned long long)__popc(b2));
-      if (b3) at3 = atomicAdd(B.ctr + kCtrBorder3, (unsigned long long)__popc(b3));
-    }
-    at2 = __shfl_sync(kFull, at2, 0);
-    at3 = __shfl_sync(kFull, at3, 0);
-    if (nc) {
-      const unsigned below = (1u << lane) - 1u;
-      if (!is3) B.blist[at2 + __popc(b2 & below)] = (uint32_t)i;
-      else B.blist[n - 1 - (int64_t)(at3 + __popc(b3 & below))] = (uint32_t)i;
-    }
+    if (i == b) B.cellcid[b] = cl;
+    const bool nc = !B.core[i];
+    B.lab[i] = nc ? kNoise : cl;
+    B.lflag[i] = nc ? 1u : 0u;  // the non-core points go to the border-search list
   }
 }
 
@@ -2398,10 +2390,11 @@ void roots(const Bufs& B, int64_t n, int sms, cudaStream_t s) {
   k_roots<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
 }
 
-void label(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) {
-  cudaMemsetAsync(B.ctr + kCtrBorder2, 0, 16, s);
+void label(const Bufs& B, bool key64, int64_t n, int sms, void* scan_temp, cudaStream_t s) {
   if (key64) k_label<true><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
   else k_label<false><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
+  gdprim::exclusive_scan_u32(B.lflag, B.lflag, n, scan_temp, B.lcount, s);
+  k_list_scatter<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
 }
 
 void border(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s) {
