@@ -346,7 +346,7 @@ cudaError_t launch_expand(gd_ctx* ctx, bool capturing) {
                        (gd::kCtrHeavyBorder - gd::kCtrTests64 + 1) * 8, s));
   gdl::Bufs B = ctx->bufs();
   keep(cudaEventRecordWithFlags(ctx->ev[3], s, evf));
-  gdl::core(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, s);
+  gdl::core(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, ctx->scantemp.p, s);
   keep(cudaEventRecordWithFlags(ctx->ev[4], s, evf));
   gdl::unite(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, s);
   keep(cudaEventRecordWithFlags(ctx->ev[5], s, evf));
@@ -375,9 +375,10 @@ gd_status expand_run(gd_ctx* ctx) {
   GD_TRY(ctx->ensure(ctx->scantemp, std::max(gdprim::scan_temp_bytes(n + 1), ctx->scantemp.bytes),
                      "scan temp"));
   const int cp = gdl::launches_per_cell_phase(ctx->dims);
-  // core, parent init, 2 union passes, compress, merge replay, roots, scan,
-  // label + list scan + scatter, core occupancy (with tables), border
-  ctx->launches += 2 * cp + 1 + 4 * cp + 1 + 1 + 1 + 3 + 5 + (ctx->bi.occ_total ? 1 : 0) + 2 * cp;
+  // core split + list scan + scatter, core, parent init, 2 union passes,
+  // compress, merge replay, roots, scan, label + list scan + scatter, core
+  // occupancy (with tables), border
+  ctx->launches += 5 + 2 * cp + 1 + 4 * cp + 1 + 1 + 1 + 3 + 5 + (ctx->bi.occ_total ? 1 : 0) + 2 * cp;
   ctx->stage = 2;
   if (ctx->graphs && ctx->xgraph) {
     GD_CUDA(cudaGraphLaunch(ctx->xgraph, s), "expand graph launch");

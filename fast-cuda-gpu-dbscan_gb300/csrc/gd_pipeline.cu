@@ -1234,6 +1234,57 @@ struct CoreFlushStage {
   int nq[32];
 };
 
+// Core flags of points in dense cells (at least minpts points: all core, no
+// test), with their cells' core counts and smallest core indices.  Every other
+// point is flagged for the walk list (scanned and scattered in sorted order
+// afterwards), so that k_core_point's warps hold only neighbouring points that
+// walk.
+template <bool KEY64>
+__global__ void k_core_split(const gdl::Bufs B, int64_t n) {
+  const int LB = B.Bi->LB;
+  const int lane = threadIdx.x & 31;
+  unsigned long long dense = 0;
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); i0 < n;
+       i0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = i0 + lane;
+    bool dn = false;
+    int b = 0;
+    if (i < n) {
+      const int m = (int)(B.runpos[i] + B.runfl[i]) - 1;
+      b = B.reps[m];
+      const int sz = B.reps[m + 1] - b;
+      dn = sz >= B.Pv[(int)(key_at<KEY64>(B, b) >> LB)].minpts;
+      if (dn) {
+        B.core[i] = 1;
+        if (i == b) ++dense;
+      }
+      B.lflag[i] = dn ? 0u : 1u;
+    }
+    const unsigned cm = __ballot_sync(kFull, dn);
+    if (dn) {
+      const unsigned grp = __match_any_sync(cm, b);
+      const unsigned mn = __reduce_min_sync(grp, (unsigned)B.ids[i]);
+      if (lane == __ffs(grp) - 1) {
+        atomicAdd(B.cellcore + b, __popc(grp));
+        atomicMin(reinterpret_cast<unsigned*>(B.cellmin) + b, mn);
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) dense += __shfl_xor_sync(kFull, dense, o);
+  if (lane == 0 && dense) atomicAdd(B.ctr + kCtrDenseCells, dense);
+}
+
+// The walk list: every flagged point at its scanned position (sorted order).
+__global__ void k_walk_scatter(const gdl::Bufs B, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t a = B.lflag[i];
+    const uint32_t e = i + 1 < n ? B.lflag[i + 1] : *B.lcount;
+    if (e != a) B.blist[a] = (uint32_t)i;
+  }
+}
+
 // Core flags, one thread per point.  Neighbouring lanes hold neighbouring
 // sorted points, mostly of one cell, so they walk the same stencil rows in
 // step: their loads coincide and their branches agree.  A point of a cell with
@@ -1260,30 +1311,28 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
   const int wbase = threadIdx.x & ~31;
   CoreFlushStage<D, F32>& S = stage[threadIdx.x >> 5];
   const int LB = B.Bi->LB;
-  int64_t mlo, mhi;
-  dim_range<D>(B, mlo, mhi);
-  const int64_t plo = B.reps[mlo], phi = B.reps[mhi];
+  // this dimension's part of the walk list: 2D instances' points come first
+  const int64_t p3 = B.reps[(int64_t)B.ctr[kCtrCells2D]];
+  const int64_t L = (int64_t)*B.lcount;
+  const int64_t L2 = p3 < n ? (int64_t)B.lflag[p3] : L;
+  const int64_t jlo = D == 2 ? 0 : L2, jhi = D == 2 ? L2 : L;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   Tally t;
-  unsigned long long dense = 0;
-  for (int64_t i0 = plo + (int64_t)blockIdx.x * blockDim.x + wbase; i0 < phi; i0 += stride) {
-    const int64_t i = i0 + lane;
-    const bool valid = i < phi;
+  for (int64_t j0 = jlo + (int64_t)blockIdx.x * blockDim.x + wbase; j0 < jhi; j0 += stride) {
+    const int64_t j = j0 + lane;
+    const bool valid = j < jhi;
+    const int64_t i = valid ? (int64_t)B.blist[j] : 0;
     int m = -1, b = 0;
     bool isc = false, over = false, pend = false;
     int cnt = 0, nq = 0, minpts = 0;
     if (valid) {
       m = (int)(B.runpos[i] + B.runfl[i]) - 1;
       b = B.reps[m];
-      const int e = B.reps[m + 1], sz = e - b;
       const CellCtx cx = cell_ctx<KEY64>(B, b, LB);
       const DevParams& P = *cx.P;
       const PredParams Q = pred_params(P);
       minpts = Q.minpts;
-      if (sz >= Q.minpts) {
-        isc = true;
-        if (i == b) ++dense;
-      } else {
+      {
         const GridView gv = view_of(B, P);
         const bool prune = Q.prune != 0;
         RowWalk<D> rw;
@@ -1481,9 +1530,6 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
     heavy_push(B, kCtrHeavyCore, lead, m, 0);
   }
   flush_tally(t, B.ctr);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) dense += __shfl_xor_sync(kFull, dense, o);
-  if (lane == 0 && dense) atomicAdd(B.ctr + kCtrDenseCells, dense);
 }
 
 // Bounded link search between the core points of cells A and B by one thread:
@@ -2366,11 +2412,17 @@ void hash_insert(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) 
 
 int launches_per_cell_phase(int dims) { return ((dims & 1) ? 1 : 0) + ((dims & 2) ? 1 : 0); }
 
-void core(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s) {
+void core(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, void* scan_temp,
+          cudaStream_t s) {
   cudaMemsetAsync(B.ctr + kCtrHeavyCore, 0, 8, s);
   // per-cell core counts (0) and smallest core indices (0xffffffff as unsigned)
   cudaMemsetAsync(B.cellcore, 0, (size_t)n * 4, s);
   cudaMemsetAsync(B.cellmin, 0xff, (size_t)n * 4, s);
+  // dense cells at once; the other points listed in sorted order for the walk
+  if (key64) k_core_split<true><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
+  else k_core_split<false><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
+  gdprim::exclusive_scan_u32(B.lflag, B.lflag, n, scan_temp, B.lcount, s);
+  k_walk_scatter<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
   GD_LAUNCH_DIMS(dims, f32, key64, k_core_point, sms * 8, kScanThreadsPerBlock, B, n);
   GD_LAUNCH_DIMS(dims, f32, key64, k_core_heavy, sms * 8, kCellThreads, B, n);
 }
