@@ -348,7 +348,7 @@ cudaError_t launch_expand(gd_ctx* ctx, bool capturing) {
   keep(cudaEventRecordWithFlags(ctx->ev[3], s, evf));
   gdl::core(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, ctx->scantemp.p, s);
   keep(cudaEventRecordWithFlags(ctx->ev[4], s, evf));
-  gdl::unite(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, s);
+  gdl::unite(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, ctx->scantemp.p, s);
   keep(cudaEventRecordWithFlags(ctx->ev[5], s, evf));
   keep(cudaMemsetAsync(B.Fmark, 0, (n + 1) * 4, s));
   gdl::roots(B, n, ctx->sms, s);
@@ -375,10 +375,11 @@ gd_status expand_run(gd_ctx* ctx) {
   GD_TRY(ctx->ensure(ctx->scantemp, std::max(gdprim::scan_temp_bytes(n + 1), ctx->scantemp.bytes),
                      "scan temp"));
   const int cp = gdl::launches_per_cell_phase(ctx->dims);
-  // core split + list scan + scatter, core, parent init, 2 union passes,
+  // core split + list scan + scatter, core, parent init + list scan + scatter,
+  // 2 union passes,
   // compress, merge replay, roots, scan, label + list scan + scatter, core
   // occupancy (with tables), border
-  ctx->launches += 5 + 2 * cp + 1 + 4 * cp + 1 + 1 + 1 + 3 + 5 + (ctx->bi.occ_total ? 1 : 0) + 2 * cp;
+  ctx->launches += 5 + 2 * cp + 5 + 4 * cp + 1 + 1 + 1 + 3 + 5 + (ctx->bi.occ_total ? 1 : 0) + 2 * cp;
   ctx->stage = 2;
   if (ctx->graphs && ctx->xgraph) {
     GD_CUDA(cudaGraphLaunch(ctx->xgraph, s), "expand graph launch");

@@ -90,7 +90,8 @@ void hash_insert(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
 // cell phases; dims: bit 0 = 2D instances present, bit 1 = 3D
 void core(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, void* scan_temp,
           cudaStream_t s);
-void unite(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s);
+void unite(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, void* scan_temp,
+           cudaStream_t s);
 void roots(const Bufs& B, int64_t n, int sms, cudaStream_t s);
 void label(const Bufs& B, bool key64, int64_t n, int sms, void* scan_temp, cudaStream_t s);
 void border(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s);

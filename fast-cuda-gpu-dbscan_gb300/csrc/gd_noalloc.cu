@@ -261,7 +261,7 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   B.hv_cell = reinterpret_cast<int*>(base + kOffHvCell);
   B.hv_mask = reinterpret_cast<unsigned long long*>(base + kOffHvMask);
   gdl::core(B, n, dims, f32, key64, sms, base + kOffScanTemp, s);
-  gdl::unite(B, n, dims, f32, key64, sms, s);
+  gdl::unite(B, n, dims, f32, key64, sms, base + kOffScanTemp, s);
   NA_CUDA(cudaMemsetAsync(B.Fmark, 0, (n + 1) * 4, s), "clear cluster marks");
   gdl::roots(B, n, sms, s);
   gdprim::exclusive_scan_u32(B.Fmark, B.Fmark, n + 1, base + kOffScanTemp, dK, s);

@@ -1597,17 +1597,21 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
   const OffTab& T = kRows[D - 2];
   const int lane = threadIdx.x & 31;
   const int LB = B.Bi->LB;
-  int64_t mlo, mhi;
-  dim_range<D>(B, mlo, mhi);
+  // this dimension's part of the core-cell list: 2D instances' cells come first
+  const int64_t M2 = (int64_t)B.ctr[kCtrCells2D];
+  const int64_t L = (int64_t)*B.lcount;
+  const int64_t L2 = M2 < n ? (int64_t)B.lflag[M2] : L;
+  const int64_t jlo = D == 2 ? 0 : L2, jhi = D == 2 ? L2 : L;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   Tally t;
-  for (int64_t m0 = mlo + (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); m0 < mhi;
-       m0 += stride) {
-    const int64_t m = m0 + lane;
+  for (int64_t j0 = jlo + (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); j0 < jhi;
+       j0 += stride) {
+    const int64_t j = j0 + lane;
+    const int64_t m = j < jhi ? (int64_t)B.blist[j] : 0;
     unsigned long long open = 0;
-    if (m < mhi) {
+    if (j < jhi) {
       const int b = B.reps[m];
-      if (B.cellcore[b] > 0) {
+      {
         const int e = B.reps[m + 1];
         const CellCtx cx = cell_ctx<KEY64>(B, b, LB);
         const DevParams& P = *cx.P;
@@ -1949,12 +1953,29 @@ __global__ void __launch_bounds__(kCellThreads) k_core_heavy(const gdl::Bufs B, 
 }
 
 // ------------------------------------------------------------- union-find
-__global__ void k_parent_init(const gdl::Bufs B) {
+// Union-find roots, and the flags of the core-cell list (cells with a core
+// point; scanned and scattered in sorted order for k_union_scan).
+__global__ void k_parent_init(const gdl::Bufs B, int64_t n) {
   const int64_t M = *B.M;
-  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
+  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < n;
        m += (int64_t)gridDim.x * blockDim.x) {
-    int b = B.reps[m];
-    B.parent[b] = b;
+    uint32_t f = 0;
+    if (m < M) {
+      const int b = B.reps[m];
+      B.parent[b] = b;
+      f = B.cellcore[b] > 0 ? 1u : 0u;
+    }
+    B.lflag[m] = f;
+  }
+}
+
+// The core-cell list: every flagged cell at its scanned position.
+__global__ void k_cell_list_scatter(const gdl::Bufs B, int64_t n) {
+  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < n;
+       m += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t a = B.lflag[m];
+    const uint32_t e = m + 1 < n ? B.lflag[m + 1] : *B.lcount;
+    if (e != a) B.blist[a] = (uint32_t)m;
   }
 }
 
@@ -2427,8 +2448,11 @@ void core(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, voi
   GD_LAUNCH_DIMS(dims, f32, key64, k_core_heavy, sms * 8, kCellThreads, B, n);
 }
 
-void unite(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s) {
-  k_parent_init<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
+void unite(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, void* scan_temp,
+           cudaStream_t s) {
+  k_parent_init<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
+  gdprim::exclusive_scan_u32(B.lflag, B.lflag, n, scan_temp, B.lcount, s);
+  k_cell_list_scatter<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
   for (int pass = 0; pass < 2; ++pass) {
     cudaMemsetAsync(B.ctr + kCtrHeavyUnion, 0, 8, s);
     GD_LAUNCH_DIMS(dims, f32, key64, k_union_scan, sms * 8, kScanThreadsPerBlock, B, n, pass);
