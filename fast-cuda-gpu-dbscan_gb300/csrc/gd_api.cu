@@ -417,7 +417,12 @@ gd_status expand_run(gd_ctx* ctx) {
 
 // Scatter labels (and core flags) to the caller's point order, copy them out,
 // read the counters into ctx->st.
-gd_status finish_run(gd_ctx* ctx, int32_t* labels, uint8_t* is_core, int32_t on_device) {
+// Scatter labels (and core flags) to the caller's order, copy them out, read the
+// counters, all behind one stream synchronisation.  A batch also passes its
+// per-instance cluster-count array (kc, kc_count entries in sorted-instance
+// order), filled before that same synchronisation.
+gd_status finish_run(gd_ctx* ctx, int32_t* labels, uint8_t* is_core, int32_t on_device,
+                     int64_t* kc = nullptr, int kc_count = 0) {
   cudaStream_t s = ctx->stream;
   const int64_t n = ctx->n;
   gd_stats& S = ctx->st;
@@ -440,6 +445,13 @@ gd_status finish_run(gd_ctx* ctx, int32_t* labels, uint8_t* is_core, int32_t on_
     GD_CUDA(cudaMemcpyAsync(labels, out, n * 4, cudaMemcpyDeviceToHost, s), "copy labels");
     if (is_core)
       GD_CUDA(cudaMemcpyAsync(is_core, cout, n, cudaMemcpyDeviceToHost, s), "copy core flags");
+  }
+  if (kc && kc_count > 0) {
+    GD_TRY(ctx->ensure(ctx->kcount, (int64_t)kc_count * 8, "cluster counts"));
+    gdl::cluster_counts(ctx->bufs(), kc_count, static_cast<int64_t*>(ctx->kcount.p), s);
+    ++ctx->launches;
+    GD_CUDA(cudaMemcpyAsync(kc, ctx->kcount.p, (size_t)kc_count * 8, cudaMemcpyDeviceToHost, s),
+            "copy cluster counts");
   }
   cudaEventRecord(ctx->ev[7], s);
   unsigned long long ctr[gd::kCtrCount];
@@ -824,17 +836,10 @@ gd_status gd_batch_dbscan(gd_ctx* ctx, int32_t count, const gd_instance* inst,
   GD_TRY(build_run(ctx, 4096, kCellsPerPoint));
   cudaEventRecord(ctx->ev[2], ctx->stream);
   GD_TRY(expand_run(ctx));
-  GD_TRY(finish_run(ctx, labels, nullptr, on_device));
-  if (cluster_counts) {
-    GD_TRY(ctx->ensure(ctx->kcount, count * 8, "cluster counts"));
-    gdl::Bufs B = ctx->bufs();
-    gdl::cluster_counts(B, count, static_cast<int64_t*>(ctx->kcount.p), ctx->stream);
-    std::vector<int64_t> kc(count);
-    GD_CUDA(cudaMemcpyAsync(kc.data(), ctx->kcount.p, count * 8, cudaMemcpyDeviceToHost,
-                            ctx->stream), "copy cluster counts");
-    GD_CUDA(cudaStreamSynchronize(ctx->stream), "cluster counts");
+  std::vector<int64_t> kc(cluster_counts ? count : 0);
+  GD_TRY(finish_run(ctx, labels, nullptr, on_device, kc.data(), (int)kc.size()));
+  if (cluster_counts)
     for (int j = 0; j < count; ++j) cluster_counts[order[j]] = kc[j];
-  }
   if (stats) *stats = ctx->st;
   return GD_OK;
 }
