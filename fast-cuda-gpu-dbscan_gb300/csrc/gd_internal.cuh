@@ -186,6 +186,8 @@ enum Counter {
   kCtrHeavyUnion,       // cells queued for warp-cooperative link searches
   kCtrHeavyBorder,      // cells queued for warp-cooperative border search
   kCtrCells2D,          // cells of 2D instances (they sort first)
+  kCtrWalkCursor2,      // walk-list entries handed out (2D, 3D); cleared before each walk launch
+  kCtrWalkCursor3,
   kCtrCount = 16
 };
 

@@ -1116,13 +1116,40 @@ __device__ __forceinline__ int classify(const float* u, int ox, int oy, int oz, 
 // sorted points, and its non-empty cells are visited through the run structure,
 // so empty cells cost nothing.
 constexpr int kScanThreadsPerBlock = 256;
+// The walk kernels (core count, union scan, border search) take their list
+// entries from a global cursor in batches of kWalkBatch, 32 per pass of a
+// warp: work is handed out as it is done, so no warp is left with a tail of
+// costly entries after the others finish (a static grid-stride split left
+// whole SMs idle behind a few slow warps).
+constexpr int kWalkBatch = 64;
+struct WalkCursor {
+  unsigned long long* c;  // kCtrWalkCursor2/3, zero at launch
+  int span;               // list entries of this dimension (< 2^31)
+  int next, end;          // the warp's batch, relative to its first entry (warp-uniform)
+  // the warp's next 32 entries are [next, min(next + 32, end)); false when the
+  // list is used up (all lanes call it)
+  __device__ __forceinline__ bool advance(int lane) {
+    if (next < end) return true;
+    unsigned long long got = 0;
+    if (lane == 0) got = atomicAdd(c, (unsigned long long)kWalkBatch);
+    got = __shfl_sync(kFull, got, 0);
+    if (got >= (unsigned long long)span) return false;
+    next = (int)got;
+    end = span - next > kWalkBatch ? next + kWalkBatch : span;
+    return true;
+  }
+};
+template <int D>
+__device__ __forceinline__ WalkCursor walk_cursor(const gdl::Bufs& B, int64_t jlo, int64_t jhi) {
+  return WalkCursor{B.ctr + (D == 2 ? kCtrWalkCursor2 : kCtrWalkCursor3), (int)(jhi - jlo), 0, 0};
+}
 // Resident 256-thread blocks per SM the front-end kernels are compiled for
 // (register budget 65536 / (256 * blocks) per thread).  These kernels are
 // bound by memory latency, so occupancy beats registers; the counts were
 // measured on GB300 (a few spilled bytes cost less than a lost block).
-constexpr int core_min_blocks(int D) { return D == 2 ? 2 : 3; }
+constexpr int kCoreMinBlocks = 4;
 constexpr int kUnionMinBlocks = 4;
-constexpr int kBorderMinBlocks = 3;
+constexpr int kBorderMinBlocks = 4;
 // The pair-test budgets of one thread (core count per point, link search per
 // cell pair, border search per point) come with the buffers (Bufs::tn_*): the
 // context sets them, the autotuner varies them.
@@ -1303,24 +1330,25 @@ __global__ void k_walk_scatter(const gdl::Bufs B, int64_t n) {
 // recomputes the whole cell.  Per-cell core counts and smallest core indices
 // are warp-aggregated atomics (cleared before the launch).
 template <int D, bool F32, bool KEY64>
-__global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_core_point(const gdl::Bufs B, int64_t n) {
+__global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_point(const gdl::Bufs B, int64_t n) {
   __shared__ int2 sq[core_queue(F32)][kScanThreadsPerBlock];
-  __shared__ CoreFlushStage<D, F32> stage[kCoreWarps];
+  __shared__ CoreFlushStage<D, F32> stage[F32 ? 1 : kCoreWarps];
   const OffTab& T = kRows[D - 2];
   const int lane = threadIdx.x & 31;
   const int wbase = threadIdx.x & ~31;
-  CoreFlushStage<D, F32>& S = stage[threadIdx.x >> 5];
+  CoreFlushStage<D, F32>& S = stage[F32 ? 0 : threadIdx.x >> 5];
   const int LB = B.Bi->LB;
   // this dimension's part of the walk list: 2D instances' points come first
   const int64_t p3 = B.reps[(int64_t)B.ctr[kCtrCells2D]];
   const int64_t L = (int64_t)*B.lcount;
   const int64_t L2 = p3 < n ? (int64_t)B.lflag[p3] : L;
   const int64_t jlo = D == 2 ? 0 : L2, jhi = D == 2 ? L2 : L;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  WalkCursor wc = walk_cursor<D>(B, jlo, jhi);
   Tally t;
-  for (int64_t j0 = jlo + (int64_t)blockIdx.x * blockDim.x + wbase; j0 < jhi; j0 += stride) {
-    const int64_t j = j0 + lane;
-    const bool valid = j < jhi;
+  while (wc.advance(lane)) {
+    const int64_t j = jlo + wc.next + lane;
+    const bool valid = wc.next + lane < wc.end;
+    wc.next += 32;
     const int64_t i = valid ? (int64_t)B.blist[j] : 0;
     int m = -1, b = 0;
     bool isc = false, over = false, pend = false;
@@ -1435,6 +1463,11 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
         }
         // what is still queued decides only if it can lift the count to minpts
         pend = !over && cnt < Q.minpts && nq > 0 && cnt + ptot >= Q.minpts;
+        if (F32 && pend) {
+          // float32 tests are cheap enough to finish by the point's own lane
+          flush();
+          pend = false;
+        }
         if (pend) {
 #pragma unroll
           for (int k = 0; k < D; ++k) {
@@ -1447,9 +1480,9 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, core_min_blocks(D)) k_co
         isc = !over && cnt >= Q.minpts;
       }
     }
-    // ---- warp-cooperative final flush
-    const unsigned pm = __ballot_sync(kFull, pend);
-    if (pm) {
+    // ---- warp-cooperative final flush (float64 mode)
+    const unsigned pm = F32 ? 0u : __ballot_sync(kFull, pend);
+    if (!F32 && pm) {
       int tot = 0;
       if (pend)
         for (int j = 0; j < nq; ++j) tot += sq[j][threadIdx.x].y - sq[j][threadIdx.x].x;
@@ -1602,14 +1635,15 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
   const int64_t L = (int64_t)*B.lcount;
   const int64_t L2 = M2 < n ? (int64_t)B.lflag[M2] : L;
   const int64_t jlo = D == 2 ? 0 : L2, jhi = D == 2 ? L2 : L;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  WalkCursor wc = walk_cursor<D>(B, jlo, jhi);
   Tally t;
-  for (int64_t j0 = jlo + (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); j0 < jhi;
-       j0 += stride) {
-    const int64_t j = j0 + lane;
-    const int64_t m = j < jhi ? (int64_t)B.blist[j] : 0;
+  while (wc.advance(lane)) {
+    const int64_t j = jlo + wc.next + lane;
+    const bool valid = wc.next + lane < wc.end;
+    wc.next += 32;
+    const int64_t m = valid ? (int64_t)B.blist[j] : 0;
     unsigned long long open = 0;
-    if (j < jhi) {
+    if (valid) {
       const int b = B.reps[m];
       {
         const int e = B.reps[m + 1];
@@ -1723,14 +1757,15 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
   const int64_t L = (int64_t)*B.lcount;
   const int64_t L2 = p3 < n ? (int64_t)B.lflag[p3] : L;
   const int64_t jlo = D == 2 ? 0 : L2, jhi = D == 2 ? L2 : L;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  WalkCursor wc = walk_cursor<D>(B, jlo, jhi);
   Tally t;
-  for (int64_t j0 = jlo + (int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31); j0 < jhi;
-       j0 += stride) {
-    const int64_t j = j0 + lane;
+  while (wc.advance(lane)) {
+    const int64_t j = jlo + wc.next + lane;
+    const bool valid = wc.next + lane < wc.end;
+    wc.next += 32;
     int m = -1;
     bool over = false;
-    if (j < jhi) {
+    if (valid) {
       const int64_t i = (int64_t)B.blist[j];
       m = (int)(B.runpos[i] + B.runfl[i]) - 1;
       const int b = B.reps[m];
@@ -2444,6 +2479,7 @@ void core(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, voi
   else k_core_split<false><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
   gdprim::exclusive_scan_u32(B.lflag, B.lflag, n, scan_temp, B.lcount, s);
   k_walk_scatter<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
+  cudaMemsetAsync(B.ctr + kCtrWalkCursor2, 0, 16, s);
   GD_LAUNCH_DIMS(dims, f32, key64, k_core_point, sms * 8, kScanThreadsPerBlock, B, n);
   GD_LAUNCH_DIMS(dims, f32, key64, k_core_heavy, sms * 8, kCellThreads, B, n);
 }
@@ -2455,6 +2491,7 @@ void unite(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, vo
   k_cell_list_scatter<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
   for (int pass = 0; pass < 2; ++pass) {
     cudaMemsetAsync(B.ctr + kCtrHeavyUnion, 0, 8, s);
+    cudaMemsetAsync(B.ctr + kCtrWalkCursor2, 0, 16, s);
     GD_LAUNCH_DIMS(dims, f32, key64, k_union_scan, sms * 8, kScanThreadsPerBlock, B, n, pass);
     GD_LAUNCH_DIMS(dims, f32, key64, k_union_heavy, sms * 8, kCellThreads, B, n, pass);
   }
@@ -2480,6 +2517,7 @@ void border(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, c
     if (key64) k_core_occ<true><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
     else k_core_occ<false><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
   }
+  cudaMemsetAsync(B.ctr + kCtrWalkCursor2, 0, 16, s);
   GD_LAUNCH_DIMS(dims, f32, key64, k_border_point, sms * 8, kScanThreadsPerBlock, B, n);
   GD_LAUNCH_DIMS(dims, f32, key64, k_border_heavy, sms * 8, kCellThreads, B, n);
 }
