@@ -323,7 +323,8 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
     table_launches += 1;
   }
   GD_CUDA(cudaGetLastError(), "index build launch");
-  const int passes = (key_bits + 7) / 8;
+  const int rb = gdprim::sort_digit_bits(key_bits);
+  const int passes = (key_bits + rb - 1) / rb;
   // bbox init+chunks, params, layout, keys, sort, gather, run flags, scan,
   // run scatter + split, tables
   ctx->launches = 4 + 1 + (passes ? passes * 5 : 1) + 1 + 1 + 3 + 2 + table_launches;

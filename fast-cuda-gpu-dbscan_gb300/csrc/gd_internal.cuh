@@ -290,4 +290,6 @@ size_t sort_temp_bytes(int64_t n);
 template <class K>
 int radix_sort_pairs(K* keys[2], uint32_t* vals[2], int64_t n, int bits, bool vals_in_is_iota,
                      void* temp, cudaStream_t s);
+// digit width radix_sort_pairs uses for a `bits`-bit key (8 or 9)
+int sort_digit_bits(int bits);
 }  // namespace gdprim

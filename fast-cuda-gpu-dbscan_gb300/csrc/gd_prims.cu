@@ -7,7 +7,7 @@
 //   k_scan_reduce    tile sums                       reads 4 B/elem
 //   k_scan_partials  one block scans the tile sums
 //   k_scan_down      tile-local scan + tile offset   reads 4 B, writes 4 B/elem
-// Radix sort (u32 key, u32 value), 8-bit digits, tiles of 4096 pairs
+// Radix sort (u32 or u64 key, u32 value), 8- or 9-bit digits, tiles of 4096 pairs
 // (256 threads x 16 items; each warp owns a contiguous 512-element segment so
 // warp-local ranking in item order is stable):
 //   k_rs_upsweep     per-tile digit histograms       reads 4 B/pair
@@ -138,52 +138,59 @@ k_scan_down(const uint32_t* in, uint32_t* out, int64_t n, const uint32_t* __rest
 // ---------------------------------------------------------------- radix sort
 constexpr int kRsThreads = 256;
 constexpr int kRsWarps = kRsThreads / 32;
-constexpr int kRsBins = 256;
+constexpr int kRsMaxBins = 512;  // digits of 8 or 9 bits
 // items per thread: 16 for 32-bit keys (4096-pair tiles), 8 for 64-bit keys
 template <class K>
 constexpr int rs_items() { return sizeof(K) == 4 ? 16 : 8; }
 constexpr int kRsMinTile = kRsThreads * 8;
 
-template <class K, int ITEMS>
+template <class K, int ITEMS, int RB>
 __global__ void __launch_bounds__(kRsThreads)
 k_rs_upsweep(const K* __restrict__ keys, int64_t n, int shift, uint32_t* __restrict__ hist,
              int64_t T) {
-  constexpr int SEG = 32 * ITEMS, TILE = kRsThreads * ITEMS;
+  constexpr int SEG = 32 * ITEMS, TILE = kRsThreads * ITEMS, BINS = 1 << RB;
+  constexpr uint32_t MASK = BINS - 1;
   // warp-private digit counts (shared-memory atomics), summed at the end
-  __shared__ uint32_t h[kRsWarps][kRsBins];
+  __shared__ uint32_t h[kRsWarps][BINS];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-  for (int ww = 0; ww < kRsWarps; ++ww) h[ww][threadIdx.x] = 0;
+  for (int ww = 0; ww < kRsWarps; ++ww)
+    for (int d = threadIdx.x; d < BINS; d += kRsThreads) h[ww][d] = 0;
   __syncthreads();
   const int64_t seg = (int64_t)blockIdx.x * TILE + w * SEG;
 #pragma unroll 4
   for (int i = 0; i < ITEMS; ++i) {
     const int64_t e = seg + i * 32 + lane;
-    if (e < n) atomicAdd(&h[w][(uint32_t)(__ldg(keys + e) >> shift) & 0xffu], 1u);
+    if (e < n) atomicAdd(&h[w][(uint32_t)(__ldg(keys + e) >> shift) & MASK], 1u);
   }
   __syncthreads();
-  uint32_t tot = 0;
+  for (int d = threadIdx.x; d < BINS; d += kRsThreads) {
+    uint32_t tot = 0;
 #pragma unroll
-  for (int ww = 0; ww < kRsWarps; ++ww) tot += h[ww][threadIdx.x];
-  hist[(int64_t)threadIdx.x * T + blockIdx.x] = tot;
+    for (int ww = 0; ww < kRsWarps; ++ww) tot += h[ww][d];
+    hist[(int64_t)d * T + blockIdx.x] = tot;
+  }
 }
 
-template <class K, int ITEMS>
+template <class K, int ITEMS, int RB>
 __global__ void __launch_bounds__(kRsThreads)
 k_rs_downsweep(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
                K* __restrict__ kout, uint32_t* __restrict__ vout, int64_t n,
                int shift, const uint32_t* __restrict__ goff, int64_t T) {
-  constexpr int SEG = 32 * ITEMS, TILE = kRsThreads * ITEMS;
+  constexpr int SEG = 32 * ITEMS, TILE = kRsThreads * ITEMS, BINS = 1 << RB;
+  constexpr int BPT = BINS / kRsThreads;  // digits per thread in the tile scan
+  constexpr uint32_t MASK = BINS - 1;
+  static_assert(TILE <= 65535, "per-warp digit offsets are 16-bit");
   __shared__ K s_keys[TILE];
   __shared__ uint32_t s_vals[TILE];
-  __shared__ uint32_t s_cnt[kRsWarps][kRsBins];
-  __shared__ uint32_t s_dstart[kRsBins];
-  __shared__ int32_t s_gbase[kRsBins];
+  __shared__ uint16_t s_cnt[kRsWarps][BINS];  // per-warp digit counts, then offsets
+  __shared__ uint32_t s_dstart[BINS];
+  __shared__ int32_t s_gbase[BINS];
   __shared__ uint32_t s_warp[32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t base = (int64_t)blockIdx.x * TILE;
   const int valid_count = (int)min((int64_t)TILE, n - base);
-  for (int i = lane; i < kRsBins; i += 32) s_cnt[w][i] = 0;
+  for (int i = lane; i < BINS; i += 32) s_cnt[w][i] = 0;
   __syncwarp();
   const unsigned lt_mask = (1u << lane) - 1u;
   K k[ITEMS];
@@ -202,38 +209,51 @@ k_rs_downsweep(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
   }
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
-    uint32_t d = (uint32_t)(k[i] >> shift) & 0xffu;
+    uint32_t d = (uint32_t)(k[i] >> shift) & MASK;
     // lanes holding the same digit: one ballot per digit bit
     unsigned peers = gd::kFull;
 #pragma unroll
-    for (int bit = 0; bit < 8; ++bit) {
+    for (int bit = 0; bit < RB; ++bit) {
       const unsigned bb = __ballot_sync(gd::kFull, (d >> bit) & 1u);
       peers &= ((d >> bit) & 1u) ? bb : ~bb;
     }
     uint32_t b = s_cnt[w][d];
     __syncwarp();
-    if (lane == __ffs(peers) - 1) s_cnt[w][d] = b + (uint32_t)__popc(peers);
+    if (lane == __ffs(peers) - 1) s_cnt[w][d] = (uint16_t)(b + (uint32_t)__popc(peers));
     __syncwarp();
     r[i] = b + (uint32_t)__popc(peers & lt_mask);
   }
   __syncthreads();
   {
-    const int d = threadIdx.x;
-    uint32_t tot = 0;
+    // digits threadIdx.x * BPT .. + BPT - 1: offsets across warps, then the
+    // tile's digit starts
+    uint32_t tots[BPT], sum = 0;
 #pragma unroll
-    for (int ww = 0; ww < kRsWarps; ++ww) {
-      uint32_t c = s_cnt[ww][d];
-      s_cnt[ww][d] = tot;
-      tot += c;
+    for (int q = 0; q < BPT; ++q) {
+      const int d = threadIdx.x * BPT + q;
+      uint32_t tot = 0;
+#pragma unroll
+      for (int ww = 0; ww < kRsWarps; ++ww) {
+        const uint32_t c = s_cnt[ww][d];
+        s_cnt[ww][d] = (uint16_t)tot;
+        tot += c;
+      }
+      tots[q] = tot;
+      sum += tot;
     }
-    uint32_t ex = block_excl_scan<kRsThreads>(tot, s_warp, nullptr);
-    s_dstart[d] = ex;
-    s_gbase[d] = (int32_t)goff[(int64_t)d * T + blockIdx.x] - (int32_t)ex;
+    uint32_t ex = block_excl_scan<kRsThreads>(sum, s_warp, nullptr);
+#pragma unroll
+    for (int q = 0; q < BPT; ++q) {
+      const int d = threadIdx.x * BPT + q;
+      s_dstart[d] = ex;
+      s_gbase[d] = (int32_t)goff[(int64_t)d * T + blockIdx.x] - (int32_t)ex;
+      ex += tots[q];
+    }
   }
   __syncthreads();
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
-    uint32_t d = (uint32_t)(k[i] >> shift) & 0xffu;
+    uint32_t d = (uint32_t)(k[i] >> shift) & MASK;
     uint32_t pos = s_dstart[d] + s_cnt[w][d] + r[i];
     s_keys[pos] = k[i];
     s_vals[pos] = v[i];
@@ -241,7 +261,7 @@ k_rs_downsweep(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
   __syncthreads();
   for (int j = threadIdx.x; j < valid_count; j += kRsThreads) {
     K key = s_keys[j];
-    uint32_t d = (uint32_t)(key >> shift) & 0xffu;
+    uint32_t d = (uint32_t)(key >> shift) & MASK;
     int64_t g = (int64_t)s_gbase[d] + j;
     kout[g] = key;
     vout[g] = s_vals[j];
@@ -278,36 +298,48 @@ void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, void* temp
 
 size_t sort_temp_bytes(int64_t n) {
   int64_t T = (n + kRsMinTile - 1) / kRsMinTile;
-  int64_t h = T * kRsBins;
+  int64_t h = T * kRsMaxBins;
   return align_up((size_t)h * sizeof(uint32_t)) + scan_temp_bytes(h);
 }
 
-template <class K>
-int radix_sort_pairs(K* keys[2], uint32_t* vals[2], int64_t n, int bits, bool vals_in_is_iota,
-                     void* temp, cudaStream_t s) {
-  if (n <= 0) return 0;
-  int passes = (bits + 7) / 8;
-  if (passes == 0) {
-    if (vals_in_is_iota) k_iota<<<1024, 256, 0, s>>>(vals[0], n);
-    return 0;
-  }
+template <class K, int RB>
+int sort_passes(K* keys[2], uint32_t* vals[2], int64_t n, int passes, bool vals_in_is_iota,
+                void* temp, cudaStream_t s) {
   constexpr int ITEMS = rs_items<K>();
   constexpr int TILE = kRsThreads * ITEMS;
   int64_t T = (n + TILE - 1) / TILE;
-  int64_t h = T * kRsBins;
+  int64_t h = T << RB;
   uint32_t* hist = static_cast<uint32_t*>(temp);
   void* scan_temp = static_cast<char*>(temp) + align_up((size_t)h * sizeof(uint32_t));
   int cur = 0;
   for (int p = 0; p < passes; ++p) {
-    int shift = 8 * p;
-    k_rs_upsweep<K, ITEMS><<<(unsigned)T, kRsThreads, 0, s>>>(keys[cur], n, shift, hist, T);
+    int shift = RB * p;
+    k_rs_upsweep<K, ITEMS, RB><<<(unsigned)T, kRsThreads, 0, s>>>(keys[cur], n, shift, hist, T);
     exclusive_scan_u32(hist, hist, h, scan_temp, nullptr, s);
     const uint32_t* vin = (p == 0 && vals_in_is_iota) ? nullptr : vals[cur];
-    k_rs_downsweep<K, ITEMS><<<(unsigned)T, kRsThreads, 0, s>>>(keys[cur], vin, keys[cur ^ 1],
-                                                                vals[cur ^ 1], n, shift, hist, T);
+    k_rs_downsweep<K, ITEMS, RB><<<(unsigned)T, kRsThreads, 0, s>>>(
+        keys[cur], vin, keys[cur ^ 1], vals[cur ^ 1], n, shift, hist, T);
     cur ^= 1;
   }
   return cur;
+}
+
+int sort_digit_bits(int bits) { return (bits + 8) / 9 < (bits + 7) / 8 ? 9 : 8; }
+
+// Digits of 9 bits where they save a pass (a 26-bit key: 3 passes, not 4),
+// else of 8 bits.
+template <class K>
+int radix_sort_pairs(K* keys[2], uint32_t* vals[2], int64_t n, int bits, bool vals_in_is_iota,
+                     void* temp, cudaStream_t s) {
+  if (n <= 0) return 0;
+  const int rb = sort_digit_bits(bits);
+  const int passes = (bits + rb - 1) / rb;
+  if (passes == 0) {
+    if (vals_in_is_iota) k_iota<<<1024, 256, 0, s>>>(vals[0], n);
+    return 0;
+  }
+  return rb == 9 ? sort_passes<K, 9>(keys, vals, n, passes, vals_in_is_iota, temp, s)
+                 : sort_passes<K, 8>(keys, vals, n, passes, vals_in_is_iota, temp, s);
 }
 
 template int radix_sort_pairs<uint32_t>(uint32_t* [2], uint32_t* [2], int64_t, int, bool, void*,
