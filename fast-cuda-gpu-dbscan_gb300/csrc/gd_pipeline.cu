@@ -1239,10 +1239,14 @@ __device__ __forceinline__ float sel5(const float (&a)[5], int d) {
   return r;
 }
 
-// undecided cells a point queues before testing them: float64 tests are
-// costly off the warp-cooperative final flush, float32 ones are cheap enough
-// that an early exit matters more
-__host__ __device__ constexpr int core_queue(bool f32) { return f32 ? 8 : 16; }
+// undecided cells a point queues before testing them (float64 mode): float64
+// tests are costly off the warp-cooperative final flush, and the 3D walks meet
+// more undecided cells.  Float32 tests are cheap enough that testing each
+// undecided cell at once, with the early exit it allows, wins: that mode keeps
+// no queue (lengths measured on GB300).
+__host__ __device__ constexpr int core_queue(int d, bool f32) {
+  return f32 ? 1 : (d == 2 ? 16 : 24);
+}
 constexpr int kCoreWarps = kScanThreadsPerBlock / 32;
 
 // Per-warp staging of the final flush: the points whose core decision waits on
@@ -1331,7 +1335,7 @@ __global__ void k_walk_scatter(const gdl::Bufs B, int64_t n) {
 // are warp-aggregated atomics (cleared before the launch).
 template <int D, bool F32, bool KEY64>
 __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_point(const gdl::Bufs B, int64_t n) {
-  __shared__ int2 sq[core_queue(F32)][kScanThreadsPerBlock];
+  __shared__ int2 sq[core_queue(D, F32)][kScanThreadsPerBlock];
   __shared__ CoreFlushStage<D, F32> stage[F32 ? 1 : kCoreWarps];
   const OffTab& T = kRows[D - 2];
   const int lane = threadIdx.x & 31;
@@ -1377,18 +1381,22 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
           for (int j = 0; j < 5; ++j) axis_terms(u[D - 1], j - 2, Q, lmx[j], lmn[j]);
         }
         int ptot = 0, budget = B.tn_core;
+        // test the points [q, qe) of one cell until the count reaches minpts
+        auto test_cell = [&](int q, int qe) {
+          for (int qq = q; qq < qe && cnt < Q.minpts; ++qq) {
+            if (budget-- == 0) {
+              over = true;
+              break;
+            }
+            Cand<D, F32> cd;
+            load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
+            cnt += pair_test<D, F32>(px, pf, cd, B.X, n, qq, true, Q, t) ? 1 : 0;
+          }
+        };
         auto flush = [&](void) {
           for (int j = 0; j < nq && cnt < Q.minpts && !over; ++j) {
             const int2 c = sq[j][threadIdx.x];
-            for (int qq = c.x; qq < c.y && cnt < Q.minpts; ++qq) {
-              if (budget-- == 0) {
-                over = true;
-                break;
-              }
-              Cand<D, F32> cd;
-              load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
-              cnt += pair_test<D, F32>(px, pf, cd, B.X, n, qq, true, Q, t) ? 1 : 0;
-            }
+            test_cell(c.x, c.y);
           }
           nq = 0;
           ptot = 0;
@@ -1418,10 +1426,14 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
             if (cls > 0) {
               cnt += qe - q;
             } else if (cls == 0) {
-              if (nq == core_queue(F32)) flush();
-              sq[nq][threadIdx.x] = make_int2(q, qe);
-              ++nq;
-              ptot += qe - q;
+              if constexpr (F32) {
+                test_cell(q, qe);
+              } else {
+                if (nq == core_queue(D, F32)) flush();
+                sq[nq][threadIdx.x] = make_int2(q, qe);
+                ++nq;
+                ptot += qe - q;
+              }
             }
           };
           if (gv.sparse == 0) {
@@ -1463,11 +1475,6 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
         }
         // what is still queued decides only if it can lift the count to minpts
         pend = !over && cnt < Q.minpts && nq > 0 && cnt + ptot >= Q.minpts;
-        if (F32 && pend) {
-          // float32 tests are cheap enough to finish by the point's own lane
-          flush();
-          pend = false;
-        }
         if (pend) {
 #pragma unroll
           for (int k = 0; k < D; ++k) {
