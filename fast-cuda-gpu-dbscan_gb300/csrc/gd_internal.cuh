@@ -111,6 +111,12 @@ struct DevParams {
   float f_hi, f_lo;
   float b_hi[3], b_lo[3];
   int32_t fast_origin;
+  // float32 cell keys (k_keys): lo and 1/f in float, and the bound on
+  // |t32 - t64| in cell units; a coordinate whose float32 cell position is
+  // farther than key_band from a cell boundary takes its cell from it, the
+  // others from the float64 formula.  Valid when key_fast.
+  float key_lo32[3], key_inv32, key_band;
+  int32_t key_fast;
 };
 
 // Division by an invariant integer d >= 1 through a multiply-high (Granlund &

@@ -223,6 +223,32 @@ __global__ void k_params_inst(const gdl::Bufs B, int K, double mult2, double mul
     }
     p.fast_origin = fast ? 1 : 0;
   }
+  {
+    // Float32 cell keys.  k_keys computes t64 = fl64(fl64(x - lo) * inv_f) and
+    // floor(t64).  Its float32 path takes x32 = x rounded toward zero (from the
+    // bits, |x32 - x| <= |x| 2^-23), lo32 = fl32(lo), i32 = fl32(inv_f) and
+    // t32 = fl32(fl32(x32 - lo32) * i32).  With T = (x - lo) inv_f exact,
+    //   |t32 - T| <= (|x| 2^-23 + |lo| 2^-24) inv_f (1 + 2^-22) + T (3 2^-24 + 2^-47)
+    //   |t64 - T| <= T 2^-52,
+    // and 0 <= T <= (hi - lo) inv_f < G + 1.  key_band is 1.25 times the sum
+    // (rounded up to float): a t32 farther than that from every integer has
+    // floor(t32) = floor(t64).
+    double maxabs_k = 0.0, loabs = 0.0;
+    for (int k = 0; k < D; ++k) {
+      maxabs_k = fmax(maxabs_k, fmax(fabs(p.lo[k]), fabs(p.hi[k])));
+      loabs = fmax(loabs, fabs(p.lo[k]));
+    }
+    double gmax = 1.0;
+    for (int k = 0; k < D; ++k) gmax = fmax(gmax, (double)p.G[k]);
+    const double band = 1.25 * ((maxabs_k * 0x1p-23 + loabs * 0x1p-24) * p.inv_f * (1.0 + 0x1p-22) +
+                                (gmax + 1.0) * (3.0 * 0x1p-24 + 0x1p-47));
+    bool kf = I.n > 0 && band < 0.125 && gmax < 0x1p21 && maxabs_k < 0x1p100 && p.inv_f < 0x1p100 &&
+              maxabs_k * p.inv_f < 0x1p100;
+    for (int k = 0; k < 3; ++k) p.key_lo32[k] = k < D ? __double2float_rn(p.lo[k]) : 0.0f;
+    p.key_inv32 = __double2float_rn(p.inv_f);
+    p.key_band = __double2float_ru(band);
+    p.key_fast = kf ? 1 : 0;
+  }
   p.flags = fl;
   p.occ_off = 0;
   p.start_off = 0;
@@ -371,6 +397,10 @@ __global__ void __launch_bounds__(256) k_keys(const gdl::Bufs B, Key* __restrict
   int64_t G[3];
   for (int k = 0; k < 3; ++k) { lo[k] = P.lo[k]; G[k] = P.G[k]; }
   const uint64_t hi = (uint64_t)P.inst << P.LB;
+  const bool kfast = P.key_fast != 0;
+  const float band = P.key_band, inv32 = P.key_inv32;
+  float lo32[3];
+  for (int k = 0; k < 3; ++k) lo32[k] = P.key_lo32[k];
   const double* __restrict__ pts = B.coords + P.co_off;
   for (int64_t g = c.begin + threadIdx.x; g < c.end; g += blockDim.x) {
     const int64_t l = g - P.pt_off;
@@ -378,8 +408,33 @@ __global__ void __launch_bounds__(256) k_keys(const gdl::Bufs B, Key* __restrict
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       if (k >= D) break;
-      const double t = __dmul_rn(__dsub_rn(pts[l * D + k], lo[k]), inv_f);
-      int64_t q = __double2ll_rd(t);  // floor and convert in one step (t is finite)
+      const double x = pts[l * D + k];
+      int64_t q;
+      bool fast = false;
+      if (kfast) {
+        // float32 cell position (no float64 instruction), used when it is
+        // farther than key_band from a cell boundary
+        const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+        const int fe = (int)((bits >> 52) & 0x7ff) - 1023 + 127;
+        const bool zero = (bits << 1) == 0;
+        if (zero || (fe > 0 && fe < 255)) {
+          const unsigned sgn = (unsigned)(bits >> 63) << 31;
+          const float x32 = zero ? 0.0f
+                                 : __uint_as_float(sgn | ((unsigned)fe << 23) |
+                                                   (unsigned)((bits >> 29) & 0x7fffffu));
+          const float t = __fmul_rn(__fsub_rn(x32, lo32[k]), inv32);
+          const float fl = floorf(t);
+          const float fr = __fsub_rn(t, fl);
+          if (fabsf(t) < 4194304.0f && fr > band && fr < 1.0f - band) {
+            q = (int64_t)fl;
+            fast = true;
+          }
+        }
+      }
+      if (!fast) {
+        const double t = __dmul_rn(__dsub_rn(x, lo[k]), inv_f);
+        q = __double2ll_rd(t);  // floor and convert in one step (t is finite)
+      }
       q = q < 0 ? 0 : (q >= G[k] ? G[k] - 1 : q);
       key = key * (uint64_t)G[k] + (uint64_t)q;
     }
