@@ -1203,7 +1203,7 @@ __device__ __forceinline__ WalkCursor walk_cursor(const gdl::Bufs& B, int64_t jl
 // bound by memory latency, so occupancy beats registers; the counts were
 // measured on GB300 (a few spilled bytes cost less than a lost block).
 constexpr int kCoreMinBlocks = 4;
-constexpr int kUnionMinBlocks = 4;
+constexpr int kUnionMinBlocks = 5;
 constexpr int kBorderMinBlocks = 4;
 // The pair-test budgets of one thread (core count per point, link search per
 // cell pair, border search per point) come with the buffers (Bufs::tn_*): the
