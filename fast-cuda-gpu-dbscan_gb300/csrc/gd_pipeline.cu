@@ -1391,6 +1391,9 @@ __global__ void k_walk_scatter(const gdl::Bufs B, int64_t n) {
 template <int D, bool F32, bool KEY64>
 __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_point(const gdl::Bufs B, int64_t n) {
   __shared__ int2 sq[core_queue(D, F32)][kScanThreadsPerBlock];
+  // per thread: squared largest / smallest distance terms to the five cell
+  // slabs along the last axis (offsets -2..2), kept out of registers
+  __shared__ float2 slt[5][kScanThreadsPerBlock];
   __shared__ CoreFlushStage<D, F32> stage[F32 ? 1 : kCoreWarps];
   const OffTab& T = kRows[D - 2];
   const int lane = threadIdx.x & 31;
@@ -1427,13 +1430,17 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
         double px[D];
         float pf[D];
         load_point<D, F32>(px, pf, B, n, i, prune);
-        float u[D], lmx[5], lmn[5];
+        float u[D];
         if (prune) {
           float o[D];
           cell_origin32<D>(rw.cc, P, o);
           frac_pos<D>(pf, o, Q, u);
 #pragma unroll
-          for (int j = 0; j < 5; ++j) axis_terms(u[D - 1], j - 2, Q, lmx[j], lmn[j]);
+          for (int j = 0; j < 5; ++j) {
+            float a2, b2;
+            axis_terms(u[D - 1], j - 2, Q, a2, b2);
+            slt[j][threadIdx.x] = make_float2(a2, b2);
+          }
         }
         int ptot = 0, budget = B.tn_core;
         // test the points [q, qe) of one cell until the count reaches minpts
@@ -1475,7 +1482,8 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
           auto visit = [&](int q, int qe, int d) {
             int cls = 0;
             if (prune) {
-              const float smax = rmx + sel5(lmx, d), smin = rmn + sel5(lmn, d);
+              const float2 lt = slt[d + 2][threadIdx.x];
+              const float smax = rmx + lt.x, smin = rmn + lt.y;
               cls = smax <= Q.thr_in ? 1 : (smin >= Q.thr_out ? -1 : 0);
             }
             if (cls > 0) {
