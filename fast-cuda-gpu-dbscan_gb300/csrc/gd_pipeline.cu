@@ -1284,16 +1284,6 @@ __device__ __forceinline__ void axis_terms(float a, int o, const PP& P, float& m
   mn2 = mn * mn;
 }
 
-// a[d + 2] for d in [-2, 2], by selects (the array stays in registers)
-__device__ __forceinline__ float sel5(const float (&a)[5], int d) {
-  float r = a[0];
-  r = d == -1 ? a[1] : r;
-  r = d == 0 ? a[2] : r;
-  r = d == 1 ? a[3] : r;
-  r = d == 2 ? a[4] : r;
-  return r;
-}
-
 // undecided cells a point queues before testing them (float64 mode): float64
 // tests are costly off the warp-cooperative final flush, and the 3D walks meet
 // more undecided cells.  Float32 tests are cheap enough that testing each
@@ -1819,6 +1809,9 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
 // tests pass the budget sends its cell to the warp kernel.
 template <int D, bool F32, bool KEY64>
 __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_border_point(const gdl::Bufs B, int64_t n) {
+  // per thread: squared largest / smallest distance terms to the five cell
+  // slabs along the last axis (offsets -2..2), kept out of registers
+  __shared__ float2 slt[5][kScanThreadsPerBlock];
   const OffTab& T = kRows[D - 2];
   const int lane = threadIdx.x & 31;
   const int LB = B.Bi->LB;
@@ -1849,13 +1842,17 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
       double px[D];
       float pf[D];
       load_point<D, F32>(px, pf, B, n, i, prune);
-      float u[D], lmx[5], lmn[5];
+      float u[D];
       if (prune) {
         float o[D];
         cell_origin32<D>(rw.cc, P, o);
         frac_pos<D>(pf, o, Q, u);
 #pragma unroll
-        for (int k = 0; k < 5; ++k) axis_terms(u[D - 1], k - 2, Q, lmx[k], lmn[k]);
+        for (int k = 0; k < 5; ++k) {
+          float a2, b2;
+          axis_terms(u[D - 1], k - 2, Q, a2, b2);
+          slt[k][threadIdx.x] = make_float2(a2, b2);
+        }
       }
       int best = INT_MAX, budget = B.tn_border;
       for (int r = 0; r < T.n && !over; ++r) {
@@ -1886,7 +1883,8 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
             int cls = 0;
             if (prune) {
               const int d = (int)(rw.l0 + z - rw.cl);
-              const float smax = rmx + sel5(lmx, d), smin = rmn + sel5(lmn, d);
+              const float2 lt = slt[d + 2][threadIdx.x];
+              const float smax = rmx + lt.x, smin = rmn + lt.y;
               cls = smax <= Q.thr_in ? 1 : (smin >= Q.thr_out ? -1 : 0);
             }
             if (cls > 0) {
@@ -1916,7 +1914,8 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
           if (cB >= best) return;
           int cls = 0;
           if (prune) {
-            const float smax = rmx + sel5(lmx, d), smin = rmn + sel5(lmn, d);
+            const float2 lt = slt[d + 2][threadIdx.x];
+            const float smax = rmx + lt.x, smin = rmn + lt.y;
             cls = smax <= Q.thr_in ? 1 : (smin >= Q.thr_out ? -1 : 0);
           }
           if (cls > 0) {
