@@ -1294,15 +1294,15 @@ __host__ __device__ constexpr int core_queue(int d, bool f32) {
 }
 constexpr int kCoreWarps = kScanThreadsPerBlock / 32;
 
-// Per-warp staging of the final flush: the points whose core decision waits on
-// their queued cells, with their instances (lanes of one warp may belong to
-// different instances; the predicate constants are read from Pv).
+// Per-warp staging of the final flush (float64 mode): the points whose core
+// decision waits on their queued cells, with their instances (lanes of one
+// warp may belong to different instances; the predicate constants are read
+// from Pv).
 template <int D, bool F32>
 struct CoreFlushStage {
   double x[32][D];
   float f[32][D];
-  // float32 mode (short queue): the predicate constants themselves; float64
-  // mode (long queue, less shared memory left): the instance, constants from Pv
+  // the predicate constants (unused: float32 mode has no final flush)
   PredParams q[F32 ? 32 : 1];
   int inst[32];
   int cnt[32];    // neighbours counted so far
@@ -1361,23 +1361,25 @@ __global__ void k_walk_scatter(const gdl::Bufs B, int64_t n) {
   }
 }
 
-// Core flags, one thread per point.  Neighbouring lanes hold neighbouring
-// sorted points, mostly of one cell, so they walk the same stencil rows in
-// step: their loads coincide and their branches agree.  A point of a cell with
-// at least minpts points is core at once.  Otherwise the walk goes row by row,
-// own row first: with cell classification, rows and cells wholly inside eps
-// count without tests, those wholly outside are skipped, and undecided cells
-// are queued (shared memory).  The classification's per-axis terms are formed
-// per row for the fixed axes and per point for the last axis (five values in
-// registers).  A full queue is tested by its own thread; what is queued when
-// the walk ends is tested by the whole warp together: the lanes whose decision
-// depends on their queue pool its candidates and every lane tests one
-// candidate per round (one owner's point against one queued point), so the
-// float64 tests run on full warps, and owners stop consuming once they reach
-// minpts.  A point whose tests pass the budget (or a warp whose pooled
-// candidates pass 32 budgets) sends its cell to the warp kernel, which
-// recomputes the whole cell.  Per-cell core counts and smallest core indices
-// are warp-aggregated atomics (cleared before the launch).
+// Core flags of the listed points (those outside dense cells, in sorted
+// order), one thread per point; warps take the list from the walk cursor.
+// Neighbouring lanes hold neighbouring sorted points, mostly of one cell, so
+// they walk the same stencil rows in step: their loads coincide and their
+// branches agree.  The walk goes row by row, own row first: with cell
+// classification, rows and cells wholly inside eps count without tests, those
+// wholly outside are skipped.  The classification's per-axis terms are formed
+// per row for the fixed axes and per point for the last axis (five pairs in
+// per-thread shared memory).  An undecided cell is tested at once in float32
+// mode.  In float64 mode undecided cells are queued (shared memory); a full
+// queue is tested by its own thread, and what is queued when the walk ends is
+// tested by the whole warp together: the lanes whose decision depends on their
+// queue pool its candidates and every lane tests one candidate per round (one
+// owner's point against one queued point), so the float64 tests run on full
+// warps, and owners stop consuming once they reach minpts.  A point whose
+// tests pass the budget (or a warp whose pooled candidates pass 32 budgets)
+// sends its cell to the warp kernel, which recomputes the whole cell.
+// Per-cell core counts and smallest core indices are warp-aggregated atomics
+// (cleared before the launch).
 template <int D, bool F32, bool KEY64>
 __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_point(const gdl::Bufs B, int64_t n) {
   __shared__ int2 sq[core_queue(D, F32)][kScanThreadsPerBlock];
