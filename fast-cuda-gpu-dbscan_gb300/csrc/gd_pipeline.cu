@@ -1302,8 +1302,6 @@ template <int D, bool F32>
 struct CoreFlushStage {
   double x[32][D];
   float f[32][D];
-  // the predicate constants (unused: float32 mode has no final flush)
-  PredParams q[F32 ? 32 : 1];
   int inst[32];
   int cnt[32];    // neighbours counted so far
   int incl[32];   // inclusive prefix of the queued candidate counts
@@ -1536,8 +1534,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
             S.x[lane][k] = px[k];
             S.f[lane][k] = pf[k];
           }
-          if constexpr (F32) S.q[lane] = Q;
-          else S.inst[lane] = P.inst;
+          S.inst[lane] = P.inst;
         }
         isc = !over && cnt >= Q.minpts;
       }
@@ -1573,9 +1570,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
               else lo = mid + 1;
             }
             const int ow = lo;
-            PredParams Qo;
-            if constexpr (F32) Qo = S.q[ow];
-            else Qo = pred_params(B.Pv[S.inst[ow]]);
+            const PredParams Qo = pred_params(B.Pv[S.inst[ow]]);
             if (S.cnt[ow] < Qo.minpts) {
               int k = c - (ow > 0 ? S.incl[ow - 1] : 0);  // candidate index within the owner's queue
               int qq = -1;
