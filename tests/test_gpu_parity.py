@@ -203,3 +203,27 @@ def test_far_from_origin_disables_shortcuts(gpu_ctx, oracle, prec):
     olab, ocore, _ = oracle.oracle_dbscan(pts, 0.25, 5)
     assert np.array_equal(core, ocore)
     assert np.array_equal(lab, olab)
+
+
+@pytest.mark.parametrize("prec", PRECISIONS)
+def test_points_on_cell_boundaries_vs_oracle(gpu_ctx, oracle, prec):
+    """Coordinates on, and a few ulps either side of, the grid's cell boundaries
+    lo + c f (lo = 0, f the default cell side eps * 0.5 (1 + 2^-16)): the cell
+    keys' float32 path must hand these to the float64 formula.  The lattice
+    also puts many pairs at 2f = eps (1 + 2^-16), just beyond eps, and the ulp
+    offsets move some of them across.  Labels and core flags must stay the
+    oracle's."""
+    rng = np.random.default_rng(77)
+    for d, cells, n, mp in ((2, 200, 60000, 12), (3, 40, 60000, 26)):
+        eps = 0.3 if d == 2 else 0.05
+        f = eps * (0.5 * (1 + 2.0 ** -16))
+        c = rng.integers(0, cells, (n, d)).astype(np.float64)
+        base = c * f
+        ulps = rng.integers(-3, 4, (n, d)).astype(np.float64)
+        pts = np.maximum(base + ulps * np.spacing(np.maximum(base, f)), 0.0)
+        pts[0] = 0.0
+        lab, core = run(gpu_ctx, pts, eps, mp, prec)
+        olab, ocore, _ = oracle.oracle_dbscan(pts, eps, mp)
+        assert np.array_equal(core, ocore), d
+        assert np.array_equal(lab, olab), d
+        assert 0 < int(ocore.sum()) < n and olab.max() >= 1, d   # a real mix of outcomes
