@@ -7,6 +7,7 @@ to the CUDA library, and loading fails loudly when the library is missing.
 
 Stages mirror the reference program (main.cu):
   import_dataset   ImportDataset            main.cu:469-498
+  label_quality    cluster check            test-results/cluster-check.cpp:41-199
   Context.index_build   index construction  main.cu:166-338, indexing.cu
   Context.expand        expansion + merge   main.cu:369-403, dbscan.cu:25-387
   Context.get_result    GetDbscanResult     dbscan.cu:225-251
@@ -94,6 +95,15 @@ class GdServerStats(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class GdLabelQuality(ctypes.Structure):
+    _fields_ = [("score", ctypes.c_double), ("mismatch_loss", ctypes.c_double)] + [
+        (name, ctypes.c_int64) for name in (
+            "noise_mismatch", "noise_agree", "clusters_a", "clusters_b", "n")]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 _lib = None
 
 # (name, restype, argtypes) of every entry point declared in include/gbdbscan.h
@@ -137,6 +147,8 @@ SIGNATURES = [
                                          ctypes.POINTER(ctypes.POINTER(ctypes.c_double)),
                                          ctypes.POINTER(ctypes.c_int64)]),
     ("gd_write_labels", ctypes.c_int, [ctypes.c_char_p, _P, ctypes.c_int64]),
+    ("gd_label_quality_compare", ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.c_int32,
+                                                ctypes.POINTER(GdLabelQuality)]),
     ("gd_free", None, [_P]),
 ]
 
@@ -192,6 +204,21 @@ def import_dataset(path: str, dim: int, max_points: int = 0) -> np.ndarray:
     finally:
         lib.gd_free(ctypes.cast(out, ctypes.c_void_p))
     return arr.reshape(n.value, dim)
+
+
+def label_quality(a, b, noise: int = NOISE) -> dict:
+    """How far labelling ``b`` is from labelling ``a`` (the reference's cluster
+    check): per point 0 when noise in exactly one, 1 when noise in both, else
+    the Jaccard index of its two clusters; ``score`` is the mean.  Host code:
+    needs no GPU."""
+    la = np.ascontiguousarray(a, dtype=np.int32)
+    lb = np.ascontiguousarray(b, dtype=np.int32)
+    if la.shape != lb.shape or la.ndim != 1:
+        raise ValueError("label_quality: a and b must be 1-D arrays of one length")
+    q = GdLabelQuality()
+    _check(load_library().gd_label_quality_compare(la.ctypes.data, lb.ctypes.data, la.shape[0],
+                                                   int(noise), ctypes.byref(q)))
+    return q.as_dict()
 
 
 def write_labels(path: str, labels: np.ndarray) -> None:

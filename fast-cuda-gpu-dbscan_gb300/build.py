@@ -1,10 +1,11 @@
-"""Build recipe for libgbdbscan.so and the gbdbscan_main CLI (sm_103a only).
+"""Build recipe for libgbdbscan.so and its command-line tools (sm_103a only).
 
 Every translation unit under csrc/ is compiled by nvcc in parallel with
   -gencode arch=compute_103a,code=sm_103a -O3 -lineinfo -std=c++17
 and linked in-tree:
   <package>/libgbdbscan.so      the C-ABI library (include/gbdbscan.h)
   <package>/gbdbscan_main       the command-line driver (links the library)
+  <package>/gbdbscan_check      the label-quality report (links the library)
 Objects go to <package>/_build/.  No cmake, no torch extension machinery.
 """
 from __future__ import annotations
@@ -22,13 +23,14 @@ INCLUDE = os.path.join(ROOT, "include")
 OBJ = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libgbdbscan.so")
 CLI = os.path.join(PKG, "gbdbscan_main")
+CHECK = os.path.join(PKG, "gbdbscan_check")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
            "-I", INCLUDE, "-I", CSRC]
 LIB_SOURCES = ["gd_prims.cu", "gd_pipeline.cu", "gd_api.cu", "gd_noalloc.cu", "gd_io.cpp",
-               "gd_server.cpp"]
-CLI_SOURCES = ["gd_main.cpp"]
+               "gd_server.cpp", "gd_quality.cpp"]
+CLI_SOURCES = ["gd_main.cpp", "gd_check_main.cpp"]
 
 
 def nvcc() -> str:
@@ -66,7 +68,7 @@ def _compile(src: str, verbose: bool) -> str:
 
 def build(force: bool = False, verbose: bool = False) -> str:
     deps = _deps()
-    if not force and not _stale(LIB, deps) and not _stale(CLI, deps):
+    if not force and not any(_stale(t, deps) for t in (LIB, CLI, CHECK)):
         return LIB
     os.makedirs(OBJ, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(LIB_SOURCES) + len(CLI_SOURCES)) as ex:
@@ -76,10 +78,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
     tmp = LIB + f".tmp{os.getpid()}"
     subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *lib_objs], check=True)
     os.replace(tmp, LIB)
-    tmp = CLI + f".tmp{os.getpid()}"
-    subprocess.run([nvcc(), *ARCH, "-o", tmp, *cli_objs, "-L", PKG, "-lgbdbscan",
-                    "-Xlinker", "-rpath,$ORIGIN"], check=True)
-    os.replace(tmp, CLI)
+    for exe, obj in zip((CLI, CHECK), cli_objs):
+        tmp = exe + f".tmp{os.getpid()}"
+        subprocess.run([nvcc(), *ARCH, "-o", tmp, obj, "-L", PKG, "-lgbdbscan",
+                        "-Xlinker", "-rpath,$ORIGIN"], check=True)
+        os.replace(tmp, exe)
     return LIB
 
 

@@ -276,6 +276,26 @@ gd_status gd_import_dataset(const char* path, int32_t dim, int64_t max_points, d
 gd_status gd_write_labels(const char* path, const int32_t* labels, int64_t n);
 void gd_free(void* p);
 
+/* ---- label-quality report ---------------------------------------------- */
+/* Replaces the reference's cluster check (test-results/cluster-check.cpp,
+   DetermineErrorTwoClusterResults, lines 41-199): how far labelling b of n
+   points is from labelling a.  Labels equal to `noise` are noise (the
+   reference's files use 0; this library's labels use GD_NOISE); any other
+   value is a cluster id.  Per point: 0 when noise in exactly one labelling,
+   1 when noise in both, else the Jaccard index of its two clusters.  Host code
+   only (no GPU needed).  n == 0 gives score 1. */
+typedef struct gd_label_quality {
+  double score;          /* mean per-point score ("Final Error metric") */
+  double mismatch_loss;  /* sum of (1 - score) over points clustered in both, / n */
+  int64_t noise_mismatch;  /* noise in exactly one labelling */
+  int64_t noise_agree;     /* noise in both */
+  int64_t clusters_a;      /* distinct non-noise labels in a */
+  int64_t clusters_b;      /* distinct non-noise labels in b */
+  int64_t n;
+} gd_label_quality;
+gd_status gd_label_quality_compare(const int32_t* a, const int32_t* b, int64_t n, int32_t noise,
+                                   gd_label_quality* out);
+
 /* ---- errors -------------------------------------------------------------- */
 const char* gd_status_string(gd_status s);
 /* Message of the last failure on the calling thread ("" if none). */

@@ -8,6 +8,10 @@
                   checkout (REF_ROOT, default /root/reference) into
                   oracle/_ref/libref_rtree.so through ref_rtree_harness.cpp.
                   Skipped (returns None) when the checkout is absent.
+  build_ref_check() compiles the reference's cluster check
+                  (test-results/cluster-check.cpp) into the executable
+                  oracle/_ref/ref_cluster_check through ref_check_harness.cpp.
+                  Skipped (returns None) when the checkout is absent.
 """
 from __future__ import annotations
 
@@ -20,6 +24,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD_DIR, "libgd_oracle.so")
 REF_RTREE_SO = os.path.join(REF_DIR, "libref_rtree.so")
+REF_CHECK_EXE = os.path.join(REF_DIR, "ref_cluster_check")
 REF_ROOT = os.environ.get("GD_REFERENCE_ROOT", "/root/reference")
 
 _COMMON = ["-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off"]
@@ -60,6 +65,23 @@ def build_ref(force: bool = False) -> str | None:
     return REF_RTREE_SO
 
 
+def build_ref_check(force: bool = False) -> str | None:
+    src_dir = os.path.join(REF_ROOT, "test-results")
+    src = os.path.join(src_dir, "cluster-check.cpp")
+    if not os.path.exists(src):
+        return None
+    harness = os.path.join(HERE, "ref_check_harness.cpp")
+    if not force and _newer(REF_CHECK_EXE, [harness, src]):
+        return REF_CHECK_EXE
+    os.makedirs(REF_DIR, exist_ok=True)
+    tmp = REF_CHECK_EXE + f".tmp{os.getpid()}"
+    cmd = ["g++", "-O2", "-std=c++17", "-w", "-I", src_dir, harness, "-o", tmp]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, REF_CHECK_EXE)
+    return REF_CHECK_EXE
+
+
 if __name__ == "__main__":
     print(build_oracle(force="-f" in sys.argv))
     print(build_ref(force="-f" in sys.argv))
+    print(build_ref_check(force="-f" in sys.argv))
