@@ -872,11 +872,6 @@ struct GridView {
     if (sh + len > 32) bits |= (uint64_t)cocc[w + 1] << (32 - sh);
     return (uint32_t)bits & ((1u << len) - 1u);
   }
-  // row table: whether the row whose first cell is rowkey holds a core point
-  __device__ __forceinline__ bool core_row(uint64_t rowkey) const {
-    const uint64_t idx = occ_off + udiv_by(rowkey, glm, gls);
-    return (cocc[idx >> 5] >> (idx & 31)) & 1u;
-  }
   // first sorted position in [b, e) whose key is >= g
   __device__ __forceinline__ int lower(int b, int e, uint64_t g) const {
     while (b < e) {
@@ -966,7 +961,7 @@ __device__ __forceinline__ void dim_range(const gdl::Bufs& B, int64_t& mlo, int6
 // Offsets within +-2 cells, built at compile time.  kRows: the (ox, oy) rows a
 // core count scans, own row first.  kHalf[d][pass]: the half stencil (o > 0
 // lexicographically) split into near offsets (all |o_k| <= 1, pass 0) and the
-// rest (pass 1).  kFull[d]: all offsets (border search).
+// rest (pass 1).  kFullSt[d]: all offsets (the warp border search).
 struct OffTab {
   signed char o[128][3];
   int n;
@@ -1019,36 +1014,7 @@ constexpr OffTab make_full(int D) {
 __constant__ OffTab kRows[2] = {make_rows(2), make_rows(3)};
 __constant__ OffTab kHalf[2][2] = {{make_half(2, 0), make_half(2, 1)},
                                    {make_half(3, 0), make_half(3, 1)}};
-// All offsets ordered near to far (smallest box-to-box distance first, then
-// largest), so a core count that stops at minpts usually stops early.
-constexpr OffTab make_near_first(int D) {
-  OffTab t = make_full(D);
-  int key[128] = {};
-  for (int i = 0; i < t.n; ++i) {
-    int mn = 0, mx = 0;
-    for (int k = 0; k < 3; ++k) {
-      int a = t.o[i][k] < 0 ? -t.o[i][k] : t.o[i][k];
-      int lo = a > 0 ? a - 1 : 0;
-      mn += lo * lo;
-      mx += (a + 1) * (a + 1);
-    }
-    key[i] = mn * 64 + mx;
-  }
-  for (int i = 1; i < t.n; ++i) {
-    int j = i;
-    while (j > 0 && key[j - 1] > key[j]) {
-      int tk = key[j]; key[j] = key[j - 1]; key[j - 1] = tk;
-      for (int k = 0; k < 3; ++k) {
-        signed char tc = t.o[j][k]; t.o[j][k] = t.o[j - 1][k]; t.o[j - 1][k] = tc;
-      }
-      --j;
-    }
-  }
-  return t;
-}
-
 __constant__ OffTab kFullSt[2] = {make_full(2), make_full(3)};
-__constant__ OffTab kNearSt[2] = {make_near_first(2), make_near_first(3)};
 
 // Per-warp list of candidate rows: row r holds the points lo[r] .. lo[r]+len,
 // and pre[r] is the exclusive prefix of the lengths (rows concatenated in
