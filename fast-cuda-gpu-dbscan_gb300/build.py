@@ -46,6 +46,20 @@ def _deps() -> list[str]:
     return out
 
 
+def source_digest() -> str:
+    """Digest of every source the library is built from (csrc/ and the public
+    header): profiles record it with their numbers, so a number captured on
+    other sources can be told apart from one of this build."""
+    import hashlib
+    h = hashlib.sha256()
+    for path in sorted(_deps()):
+        if os.path.isfile(path) and path.endswith((".cu", ".cuh", ".h", ".cpp")):
+            h.update(os.path.basename(path).encode())
+            with open(path, "rb") as f:
+                h.update(f.read())
+    return h.hexdigest()[:16]
+
+
 def _stale(target: str, deps: list[str]) -> bool:
     if not os.path.exists(target):
         return True

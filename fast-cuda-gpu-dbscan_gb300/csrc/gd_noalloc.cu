@@ -1,32 +1,39 @@
 // gd_noalloc.cu -- gd_dbscan_noalloc: exact DBSCAN for small point sets that
 // allocates no memory at all.
 //
-// Who needs it: callers that may not call cudaMalloc/cudaFree -- code that runs
-// while a CUDA graph is being captured into, real-time loops whose memory was
-// fixed at start-up, or hosts whose allocator policy forbids device
-// allocations after initialisation.  They pass device pointers for the points
-// and the labels; every other buffer of the pipeline lives in one file-scope
-// __device__ array (kScratchBytes, about 5 MiB) that the module holds on every
-// GPU that loads this library until the process exits.
+// Who needs it: callers that cannot call cudaMalloc/cudaFree.  Control and
+// real-time loops reserve all their device memory at start-up, because an
+// allocation can block for milliseconds and cudaFree waits for the whole
+// device; plug-ins that run inside a host process whose memory manager owns
+// the GPU's memory may not allocate behind its back.  They pass device
+// pointers for the points and the labels; every other buffer of the pipeline
+// lives in one file-scope __device__ array (kScratchBytes, about 5 MiB) that
+// the module holds on every GPU that loads this library until the process
+// exits.
 //
 // Limits and rules:
 //   * n <= GD_NOALLOC_MAX_POINTS (32768); larger inputs are rejected with
 //     GD_ERANGE.  Grids of more than 8*32768 cells use the hash of occupied
 //     cells instead of the dense table, so any extent fits.
-//   * The first call on a device looks the array's device address up
-//     (cudaGetSymbolAddress, with that device current) and caches it; make that
-//     first call before any stream capture begins.
+//   * The first call in a CUDA context of a device looks the array's device
+//     address up (cudaGetSymbolAddress, with that device current) and caches it
+//     with the context's id; a new context on that device (after
+//     cudaDeviceReset, say) repeats the look-up.  Make that first call before
+//     any stream capture begins.
 //   * All calls share the one array and it keeps the previous call's contents:
 //     everything that must start at zero (counters, flags, cluster marks, the
 //     cell table or hash) is cleared inside each call.  Calls whose work
 //     overlaps on the GPU (two host threads, or two streams) race on the array
 //     and must be serialised by the caller.
-//   * The call synchronises the stream once (to read the grid size) and at the
-//     end; it uses the same kernels as gd_dbscan, so the labels are identical.
+//   * The call synchronises its stream twice: once in the middle, to read the
+//     grid layout back to the host, and once at the end.  It uses the same
+//     kernels as gd_dbscan, so the labels are identical.
 #include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <string>
+
+#include <cuda.h>
 
 #include "gbdbscan.h"
 #include "gd_launch.h"
@@ -88,7 +95,16 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
+// per device: the scratch address and the id of the CUDA context it belongs to
 unsigned char* g_scratch_ptr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx[kMaxDevices] = {};
+
+// Driver functions that identify the current context, reached through the
+// runtime (the library does not link the driver library itself).
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
 
 gd_status fail(gd_status s, const std::string& m) {
   gdio::set_error(m);
@@ -105,15 +121,50 @@ gd_status cuda_fail(cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return cuda_fail(e_, what); \
   } while (0)
 
-// Device address of the scratch array on the current device (set up once per
-// device, with that device current).
+// Id of the CUDA context current on the calling thread (0 when none is).
+gd_status current_ctx_id(unsigned long long* id) {
+  *id = 0;
+  if (!g_ctx_get_current || !g_ctx_get_id) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    void *f1 = nullptr, *f2 = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) !=
+            cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) !=
+            cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2) {
+      cudaGetLastError();
+      return fail(GD_ECUDA, "gd_dbscan_noalloc: driver context functions unavailable");
+    }
+    g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f2);
+  }
+  CUcontext c = nullptr;
+  if (g_ctx_get_current(&c) != CUDA_SUCCESS)
+    return fail(GD_ECUDA, "gd_dbscan_noalloc: cuCtxGetCurrent failed");
+  if (c && g_ctx_get_id(c, id) != CUDA_SUCCESS)
+    return fail(GD_ECUDA, "gd_dbscan_noalloc: cuCtxGetId failed");
+  return GD_OK;
+}
+
+// Device address of the scratch array on the current device.  Set up once per
+// CUDA context of a device, with that device current: the address is looked up
+// and cached with the context's id, and looked up again only when another
+// context has become current on the device (the module, and with it the array,
+// is loaded anew in every context).
 gd_status scratch_of(int dev, unsigned char** out) {
   std::lock_guard<std::mutex> lock(g_setup_mu);
-  if (!g_scratch_ptr[dev]) {
+  unsigned long long id = 0;
+  gd_status st = current_ctx_id(&id);
+  if (st != GD_OK) return st;
+  if (!g_scratch_ptr[dev] || id == 0 || id != g_scratch_ctx[dev]) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress");
+    // the look-up made the device's primary context current if none was
+    st = current_ctx_id(&id);
+    if (st != GD_OK) return st;
     g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
+    g_scratch_ctx[dev] = id;
   }
   *out = g_scratch_ptr[dev];
   return GD_OK;

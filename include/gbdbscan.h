@@ -248,18 +248,23 @@ gd_status gd_server_wait(gd_server* srv, int64_t request_id, double timeout_ms,
 gd_status gd_server_get_stats(gd_server* srv, gd_server_stats* stats);
 
 /* ---- exact DBSCAN without any memory allocation ------------------------ */
-/* No counterpart in the reference.  For callers that may not allocate device
-   memory -- code running while a CUDA graph is captured, real-time loops whose
-   memory was fixed at start-up, hosts whose allocator policy forbids device
-   allocations after initialisation.  Same labels as gd_dbscan, for up to
-   GD_NOALLOC_MAX_POINTS points; larger n is rejected with GD_ERANGE.
-   coords_dev (n x dim float64) and labels_dev (n int32) are device pointers
-   on the current device; stream may be NULL (default stream).  All scratch is
-   one fixed static device array of about 5 MiB that every GPU which loads the
-   library keeps until the process exits; nothing is allocated or freed.
-   The first call on a device looks up that array's address; make it before
-   any stream capture.  Calls share the array: calls that overlap on the GPU
-   race and must be serialised by the caller.  n_clusters may be NULL. */
+/* No counterpart in the reference.  For callers that cannot call cudaMalloc
+   or cudaFree: control and real-time loops that reserve all their device
+   memory at start-up (an allocation can block for milliseconds, and cudaFree
+   waits for the whole device), and plug-ins hosted by a process whose memory
+   manager owns the GPU's memory and forbids allocations behind its back.
+   Same labels as gd_dbscan, for up to GD_NOALLOC_MAX_POINTS points; larger n
+   is rejected with GD_ERANGE.  coords_dev (n x dim float64) and labels_dev
+   (n int32) are device pointers on the current device; stream may be NULL
+   (default stream).  All scratch is one fixed static device array of about
+   5 MiB that every GPU which loads the library keeps until the process exits;
+   nothing is allocated or freed.  The first call in a CUDA context of a device
+   does a one-time set-up (it looks up that array's device address); make that
+   first call before any stream capture begins.  The call synchronises its
+   stream twice: in the middle, to read the grid layout back to the host, and
+   at the end.  Calls share the array and it keeps the last call's contents;
+   calls that overlap on the GPU race and must be serialised by the caller.
+   labels_dev is undefined when the call fails.  n_clusters may be NULL. */
 #define GD_NOALLOC_MAX_POINTS 32768
 gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int32_t dim, double eps,
                             int32_t minpts, int32_t precision, int32_t* labels_dev,

@@ -1,6 +1,7 @@
-"""gd_dbscan_noalloc: the entry point for callers that must not allocate device
-memory (graph-capture regions, real-time loops with memory fixed at start-up,
-hosts that forbid device allocation after initialisation).
+"""gd_dbscan_noalloc: the entry point for callers that cannot allocate device
+memory -- loops that reserve all their device memory at start-up (an allocation
+can block, and cudaFree waits for the whole device) and plug-ins whose host
+process owns the GPU's memory.
 
 It runs the same kernels as gd_dbscan out of one fixed static device array, so
 its labels must equal gd_dbscan's bit for bit (integer labels: no tolerance).
