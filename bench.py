@@ -406,7 +406,9 @@ def run_single(args, world, local, dist, workload, precision, scale, steps, warm
                    "l2": "512 MiB flush write between timed steps; inputs 160+ MB > L2"},
         "e2e": {"value": job_rate(n, e2e_s, world), "unit": "points/s",
                 "h2d_bytes_per_step": n * dim * 8, "d2h_bytes_per_step": n * 4,
-                "ms_per_step": e2e_s * 1e3, "labels_equal_device_run": e2e_equal},
+                "ms_per_step": e2e_s * 1e3, "labels_equal_device_run": e2e_equal,
+                "last_step_ms": {"h2d": gst.ms_h2d, "pipeline": gst.ms_total,
+                                 "d2h": gst.ms_d2h}},
         "gpu_launches": int(st["launches"]) * steps,
         "roofline": {"bound": "hbm", "achieved": dom_achieved, "peak": peak, "unit": "GB/s",
                      "frac": dom_achieved / peak, "traffic": dom_traffic,

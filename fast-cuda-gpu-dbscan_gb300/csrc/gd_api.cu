@@ -86,8 +86,7 @@ struct gd_ctx {
   int tn_core = kDefaultCoreTests, tn_link = kDefaultLinkTests, tn_border = kDefaultBorderTests;
 
   DevBuf coords, inst, chunks, Pv, Bi, bbox, keys0, keys1, vals0, vals1, X, Xf, table, occ, cellz,
-      hkeys,
-      hvals, reps, runfl, runpos, core, cellcore, cellmin, parent, Fmark, cellcid, lab, asym,
+      hkeys, hvals, reps, bits, core, cellcore, cellmin, parent, cellcid, lab, asym,
       hvcell, hvmask, out, coreout, sorttemp, scantemp, small, kcount;
 
   // the current run
@@ -115,7 +114,8 @@ struct gd_ctx {
     expands_on_index = 0;
   }
   gd_stats st{};
-  int launches = 0;
+  int launches = 0;         // kernels of the last index build
+  int expand_launches = 0;  // kernels of the expand stage (the captured graph holds as many)
 
   gd_status ensure(DevBuf& b, size_t bytes, const char* what) {
     bytes = up256(bytes ? bytes : 1);
@@ -135,8 +135,8 @@ struct gd_ctx {
   void free_all(bool keep_small) {
     DevBuf* a[] = {&coords, &inst,   &chunks,   &Pv,      &Bi,     &bbox,     &keys0,
                    &keys1,  &vals0,  &vals1,    &X,       &Xf,     &table,    &occ, &cellz, &hkeys,
-                   &hvals,  &reps,   &runfl,    &runpos,  &core,   &cellcore, &cellmin,
-                   &parent, &Fmark,  &cellcid,  &lab,     &asym,   &hvcell,   &hvmask,
+                   &hvals,  &reps,   &bits,     &core,    &cellcore, &cellmin,
+                   &parent, &cellcid,  &lab,     &asym,   &hvcell,   &hvmask,
                    &out,    &coreout, &sorttemp, &scantemp, &small, &kcount};
     for (DevBuf* b : a) {
       if (keep_small && b == &small) continue;
@@ -165,12 +165,10 @@ struct gd_ctx {
     B.ids = sids;
     // the sort's other id and key buffers are free after the sort
     B.blist = static_cast<uint32_t*>(sids == vals0.p ? vals1.p : vals0.p);
-    B.lflag = static_cast<uint32_t*>(skeys == keys0.p ? keys1.p : keys0.p);
-    B.lcount = reinterpret_cast<uint32_t*>(static_cast<char*>(small.p) + 8);
+    B.cidm = static_cast<int*>(skeys == keys0.p ? keys1.p : keys0.p);
     B.reps = static_cast<int*>(reps.p);
-    B.M = dM();
-    B.runfl = static_cast<uint32_t*>(runfl.p);
-    B.runpos = static_cast<uint32_t*>(runpos.p);
+    if (bits.p) gdl::set_bits(B, static_cast<uint32_t*>(bits.p), n);
+    B.K = dK();
     B.start = static_cast<uint32_t*>(table.p);
     B.occ = static_cast<uint32_t*>(occ.p);
     B.cellz = static_cast<uint32_t*>(cellz.p);
@@ -189,7 +187,6 @@ struct gd_ctx {
     B.cellcore = static_cast<int*>(cellcore.p);
     B.cellmin = static_cast<int*>(cellmin.p);
     B.parent = static_cast<int*>(parent.p);
-    B.Fmark = static_cast<uint32_t*>(Fmark.p);
     B.cellcid = static_cast<int*>(cellcid.p);
     B.lab = static_cast<int*>(lab.p);
     B.asym = static_cast<int*>(asym.p);
@@ -244,7 +241,8 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
   GD_CUDA(cudaMemsetAsync(ctx->small.p, 0, ctx->small.bytes, s), "clear counters");
   GD_CUDA(cudaMemsetAsync(ctx->Bi.p, 0, sizeof(gd::BatchInfo), s), "clear layout");
   gdl::Bufs B = ctx->bufs();
-  gdl::grids(B, K, nch, ctx->mult2, ctx->mult3, dense_floor, dense_per_point, s);
+  const int grid_launches =
+      gdl::grids(B, K, nch, ctx->mult2, ctx->mult3, dense_floor, dense_per_point, s);
   GD_CUDA(cudaMemcpyAsync(&ctx->bi, ctx->Bi.p, sizeof(gd::BatchInfo), cudaMemcpyDeviceToHost, s),
           "read run layout");
   GD_CUDA(cudaStreamSynchronize(s), "grid parameters");
@@ -280,8 +278,7 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
   ctx->hmask = (uint32_t)(hcap - 1);
   GD_TRY(ctx->ensure(ctx->reps, (n + 1) * 4, "cell reps"));
   GD_TRY(ctx->ensure(ctx->cellz, n * 4, "cell coordinates"));
-  GD_TRY(ctx->ensure(ctx->runfl, n * 4, "run flags"));
-  GD_TRY(ctx->ensure(ctx->runpos, n * 4, "run positions"));
+  GD_TRY(ctx->ensure(ctx->bits, gdl::bit_layout(n).words * 4, "bit masks"));
   GD_TRY(ctx->ensure(ctx->sorttemp, gdprim::sort_temp_bytes(n), "sort temp"));
   size_t sc = std::max({gdprim::scan_temp_bytes(n + 1),
                         gdprim::scan_temp_bytes((int64_t)bi.start_total),
@@ -291,7 +288,7 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
   int r;
   uint32_t* vb[2] = {static_cast<uint32_t*>(ctx->vals0.p), static_cast<uint32_t*>(ctx->vals1.p)};
   B = ctx->bufs();
-  gdl::keys(B, ctx->key64, nch, ctx->keys0.p, s);
+  int L = grid_launches + gdl::keys(B, ctx->key64, nch, ctx->keys0.p, s);
   if (ctx->key64) {
     using U64 = unsigned long long;
     U64* kb[2] = {static_cast<U64*>(ctx->keys0.p), static_cast<U64*>(ctx->keys1.p)};
@@ -302,32 +299,30 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
     r = gdprim::radix_sort_pairs<uint32_t>(kb, vb, n, key_bits, true, ctx->sorttemp.p, s);
     ctx->skeys = kb[r];
   }
+  {
+    const int rb = gdprim::sort_digit_bits(key_bits);
+    const int passes = (key_bits + rb - 1) / rb;
+    L += n > 0 ? (passes ? passes * 5 : 1) : 0;  // upsweep, 3 scan kernels, downsweep per pass
+  }
   ctx->sids = vb[r];
   B = ctx->bufs();
-  gdl::gather(B, ctx->key64, n, ctx->xf, ctx->sms, s);
-  gdl::run_flags(ctx->skeys, ctx->key64, n, B.runfl, ctx->sms, s);
-  gdprim::exclusive_scan_u32(B.runfl, B.runpos, n, ctx->scantemp.p, ctx->dM(), s);
-  gdl::run_scatter(B, ctx->key64, n, ctx->sms, s);
+  L += gdl::gather(B, ctx->key64, n, ctx->xf, K == 1, ctx->sms, s);
+  L += gdl::runs(B, ctx->key64, n, ctx->dims == 3, ctx->sms, ctx->scantemp.p, s);
   // occupancy bits, row-table starts, occupancy ranks
   GD_CUDA(cudaMemsetAsync(ctx->table.p, 0, bi.start_total * 4, s), "clear row tables");
   if (W) GD_CUDA(cudaMemsetAsync(ctx->occ.p, 0, W * 4, s), "clear occupancy");
-  gdl::cell_counts(B, ctx->key64, n, ctx->sms, s);
-  gdl::start_fill(B, ctx->K, s);
+  L += gdl::cell_counts(B, ctx->key64, n, ctx->sms, s);
+  L += gdl::start_fill(B, ctx->K, s);
   gdprim::exclusive_scan_u32(B.start, B.start, (int64_t)bi.start_total, ctx->scantemp.p, nullptr,
                              s);
-  gdl::occ_rank(B, ctx->K, ctx->scantemp.p, s);
-  int table_launches = 5 + (W ? 5 : 0);
+  L += bi.start_total ? 3 : 0;
+  L += gdl::occ_rank(B, ctx->K, ctx->scantemp.p, s);
   if (bi.any_sparse) {
     GD_CUDA(cudaMemsetAsync(ctx->hkeys.p, 0xff, hcap * 8, s), "clear row hash");
-    gdl::hash_insert(B, ctx->key64, n, ctx->sms, s);
-    table_launches += 1;
+    L += gdl::hash_insert(B, ctx->key64, n, ctx->sms, s);
   }
   GD_CUDA(cudaGetLastError(), "index build launch");
-  const int rb = gdprim::sort_digit_bits(key_bits);
-  const int passes = (key_bits + rb - 1) / rb;
-  // bbox init+chunks, params, layout, keys, sort, gather, run flags, scan,
-  // run scatter + split, tables
-  ctx->launches = 4 + 1 + (passes ? passes * 5 : 1) + 1 + 1 + 3 + 2 + table_launches;
+  ctx->launches = L;
   ctx->st.grid_cells = (int64_t)bi.occ_total;
   ctx->st.key_bits = key_bits;
   ctx->stage = 1;
@@ -347,16 +342,16 @@ cudaError_t launch_expand(gd_ctx* ctx, bool capturing) {
                        (gd::kCtrHeavyBorder - gd::kCtrTests64 + 1) * 8, s));
   gdl::Bufs B = ctx->bufs();
   keep(cudaEventRecordWithFlags(ctx->ev[3], s, evf));
-  gdl::core(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, ctx->scantemp.p, s);
+  int L = gdl::core(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->K == 1, ctx->sms,
+                    ctx->scantemp.p, s);
   keep(cudaEventRecordWithFlags(ctx->ev[4], s, evf));
-  gdl::unite(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, ctx->scantemp.p, s);
+  L += gdl::unite(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, ctx->scantemp.p, s);
   keep(cudaEventRecordWithFlags(ctx->ev[5], s, evf));
-  keep(cudaMemsetAsync(B.Fmark, 0, (n + 1) * 4, s));
-  gdl::roots(B, n, ctx->sms, s);
-  gdprim::exclusive_scan_u32(B.Fmark, B.Fmark, n + 1, ctx->scantemp.p, ctx->dK(), s);
-  gdl::label(B, ctx->key64, n, ctx->sms, ctx->scantemp.p, s);
-  gdl::border(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, s);
+  L += gdl::roots(B, ctx->key64, n, ctx->sms, ctx->scantemp.p, s);
+  L += gdl::label(B, n, ctx->sms, ctx->scantemp.p, s);
+  L += gdl::border(B, n, ctx->dims, ctx->f32, ctx->key64, ctx->sms, s);
   keep(cudaGetLastError());
+  ctx->expand_launches = L;
   return e;
 }
 
@@ -367,7 +362,6 @@ gd_status expand_run(gd_ctx* ctx) {
   GD_TRY(ctx->ensure(ctx->cellcore, n * 4, "cell core counts"));
   GD_TRY(ctx->ensure(ctx->cellmin, n * 4, "cell min index"));
   GD_TRY(ctx->ensure(ctx->parent, n * 4, "union-find parents"));
-  GD_TRY(ctx->ensure(ctx->Fmark, (n + 1) * 4, "cluster marks"));
   GD_TRY(ctx->ensure(ctx->cellcid, n * 4, "cell cluster ids"));
   GD_TRY(ctx->ensure(ctx->lab, n * 4, "labels"));
   GD_TRY(ctx->ensure(ctx->asym, gd::kAsymCap * 8, "one-directional links"));
@@ -375,12 +369,6 @@ gd_status expand_run(gd_ctx* ctx) {
   GD_TRY(ctx->ensure(ctx->hvmask, n * 8, "heavy-work masks"));
   GD_TRY(ctx->ensure(ctx->scantemp, std::max(gdprim::scan_temp_bytes(n + 1), ctx->scantemp.bytes),
                      "scan temp"));
-  const int cp = gdl::launches_per_cell_phase(ctx->dims);
-  // core split + list scan + scatter, core, parent init + list scan + scatter,
-  // 2 union passes,
-  // compress, merge replay, roots, scan, label + list scan + scatter, core
-  // occupancy (with tables), border
-  ctx->launches += 5 + 2 * cp + 5 + 4 * cp + 1 + 1 + 1 + 3 + 5 + (ctx->bi.occ_total ? 1 : 0) + 2 * cp;
   ctx->stage = 2;
   if (ctx->graphs && ctx->xgraph) {
     GD_CUDA(cudaGraphLaunch(ctx->xgraph, s), "expand graph launch");
@@ -439,8 +427,7 @@ gd_status finish_run(gd_ctx* ctx, int32_t* labels, uint8_t* is_core, int32_t on_
   }
   GD_CUDA(cudaMemsetAsync(ctx->dCtr() + gd::kCtrCore, 0, 2 * 8, s), "clear counters");
   gdl::Bufs B = ctx->bufs();
-  gdl::scatter_labels(B, n, out, cout, ctx->sms, s);
-  ++ctx->launches;
+  int fin = gdl::scatter_labels(B, n, out, cout, ctx->sms, s);
   cudaEventRecord(ctx->ev[6], s);
   if (!on_device) {
     GD_CUDA(cudaMemcpyAsync(labels, out, n * 4, cudaMemcpyDeviceToHost, s), "copy labels");
@@ -449,8 +436,7 @@ gd_status finish_run(gd_ctx* ctx, int32_t* labels, uint8_t* is_core, int32_t on_
   }
   if (kc && kc_count > 0) {
     GD_TRY(ctx->ensure(ctx->kcount, (int64_t)kc_count * 8, "cluster counts"));
-    gdl::cluster_counts(ctx->bufs(), kc_count, static_cast<int64_t*>(ctx->kcount.p), s);
-    ++ctx->launches;
+    fin += gdl::cluster_counts(ctx->bufs(), kc_count, static_cast<int64_t*>(ctx->kcount.p), s);
     GD_CUDA(cudaMemcpyAsync(kc, ctx->kcount.p, (size_t)kc_count * 8, cudaMemcpyDeviceToHost, s),
             "copy cluster counts");
   }
@@ -473,7 +459,7 @@ gd_status finish_run(gd_ctx* ctx, int32_t* labels, uint8_t* is_core, int32_t on_
   S.band_retests = (int64_t)ctr[gd::kCtrBand];
   S.asym_pairs = (int64_t)ctr[gd::kCtrAsym];
   S.precision_used = ctx->f32 ? GD_PREC_FP32_BAND : GD_PREC_FP64;
-  S.launches = ctx->launches;
+  S.launches = ctx->launches + ctx->expand_launches + fin;
   if (ctr[gd::kCtrAsymEdges] > (unsigned long long)gd::kAsymCap) {
     ctx->stage = 1;
     return fail(GD_ERANGE, "more one-directional core neighbour pairs than the merge replay "

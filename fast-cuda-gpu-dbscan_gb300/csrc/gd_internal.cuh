@@ -286,6 +286,14 @@ size_t scan_temp_bytes(int64_t n);
 // (device pointer, may be null).
 void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, void* temp,
                         uint32_t* total_dev, cudaStream_t s);
+// pre[w] = number of set bits in words[0, w) (exclusive scan of popcounts),
+// total in *total_dev (may be null); words and pre 16-byte aligned, distinct.
+void exclusive_scan_popc(const uint32_t* words, uint32_t* pre, int64_t nw, void* temp,
+                         uint32_t* total_dev, cudaStream_t s);
+// the positions of the set bits of words[0, nw) in ascending order:
+// out[pre[w] + r] = 32 w + (position of the r-th set bit of word w)
+void compact_bits(const uint32_t* words, const uint32_t* pre, int64_t nw, uint32_t* out, int sms,
+                  cudaStream_t s);
 // temp bytes needed by radix_sort_pairs for n elements (either key width)
 size_t sort_temp_bytes(int64_t n);
 // Stable LSD radix sort of (key, value) pairs on the low `bits` key bits,

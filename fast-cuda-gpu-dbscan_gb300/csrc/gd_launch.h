@@ -27,9 +27,19 @@ struct Bufs {
   const void* keys = nullptr;   // sorted cell keys: u32 or u64 (BatchInfo::key64)
   uint32_t* ids = nullptr;      // global point index per sorted position
   int* reps = nullptr;          // M+1 first positions of the non-empty cells
-  uint32_t* M = nullptr;        // number of non-empty cells (device scalar)
-  uint32_t* runfl = nullptr;    // 1 where a cell starts (per sorted position)
-  uint32_t* runpos = nullptr;   // exclusive scan of runfl: cell index = runpos+runfl-1
+  uint32_t* M = nullptr;        // number of non-empty cells (device scalar, runpre[nw])
+  // Bit masks over sorted positions (or cells), nw = ceil(n / 32) words each,
+  // with per-word exclusive prefix counts (nw + 1 entries; the last one is the
+  // total): a position's rank among the set bits is pre[i / 32] + the set bits
+  // below it in its word (bit_rank).
+  uint32_t* runbits = nullptr;  // 1 where a cell starts: cell index of i = rank(i + 1) - 1
+  uint32_t* runpre = nullptr;
+  uint32_t* lbits = nullptr;    // membership of the current walk list (points or cells)
+  uint32_t* lpre = nullptr;
+  uint32_t* fbits = nullptr;    // n+1 bits over global point indices: 1 at the smallest
+  uint32_t* fpre = nullptr;     // core index of each cluster (cluster number = rank)
+  int64_t nw = 0;               // words of runbits / lbits
+  int64_t nwf = 0;              // words of fbits
   uint32_t* start = nullptr;    // row tables: first cell (index into reps) per row, after
                                 // the scan; other instances: one entry holding their cells
   uint32_t* cellz = nullptr;    // per non-empty cell: its last-axis coordinate
@@ -47,15 +57,14 @@ struct Bufs {
   int* cellcore = nullptr;      // per rep: number of core points
   int* cellmin = nullptr;       // per rep: smallest global index of a core point
   int* parent = nullptr;        // per rep: union-find parent
-  uint32_t* Fmark = nullptr;    // n+1: 1 at the smallest core index of each cluster,
-                                // then its exclusive scan (global cluster numbers)
   int* cellcid = nullptr;       // per rep: cluster id of the cell's core points
+  int* cidm = nullptr;          // the same per cell index m (the sort's spare key buffer)
   int* lab = nullptr;           // label per sorted position
   int* asym = nullptr;          // kAsymCap (from, to) sorted-position pairs
-  uint32_t* blist = nullptr;    // non-core sorted positions for the border search (n), in
-                                // sorted order (2D instances' first)
-  uint32_t* lflag = nullptr;    // n: list positions (exclusive scan of the non-core flags)
-  uint32_t* lcount = nullptr;   // device scalar: list length
+  uint32_t* blist = nullptr;    // the current walk list (set bits of lbits in order: sorted
+                                // positions or cells, 2D instances' first), capacity n
+  uint32_t* lcount = nullptr;   // device scalar: list length (lpre[nw])
+  uint32_t* K = nullptr;        // device scalar: clusters of the run
   int* hv_cell = nullptr;       // heavy-work list: cell index m (capacity n)
   unsigned long long* hv_mask = nullptr;  // heavy-work list: stencil offsets still open
   unsigned long long* ctr = nullptr;      // gd::Counter
@@ -69,37 +78,76 @@ struct Bufs {
 inline uint64_t occ_wpre_offset(uint64_t W) { return (2 * W + 63) & ~uint64_t(63); }
 inline uint64_t occ_buffer_words(uint64_t W) { return occ_wpre_offset(W) + W; }
 
+// The bit masks of a run of n points (runbits, runpre, lbits, lpre, fbits,
+// fpre) in one buffer: each array nw + 1 (fbits, fpre: nwf + 1) words, at
+// 256-byte aligned offsets.
+struct BitLayout {
+  int64_t nw = 0, nwf = 0;
+  uint64_t off[6] = {};
+  uint64_t words = 0;
+};
+constexpr BitLayout bit_layout(int64_t n) {
+  BitLayout L;
+  L.nw = (n + 31) / 32;
+  L.nwf = (n + 1 + 31) / 32;
+  uint64_t at = 0;
+  for (int a = 0; a < 6; ++a) {
+    L.off[a] = at;
+    at += ((uint64_t)(a < 4 ? L.nw : L.nwf) + 1 + 63) & ~uint64_t(63);
+  }
+  L.words = at;
+  return L;
+}
+// points the Bufs at the bit masks in `words` (bit_layout(n).words words)
+inline void set_bits(Bufs& B, uint32_t* words, int64_t n) {
+  const BitLayout L = bit_layout(n);
+  B.nw = L.nw;
+  B.nwf = L.nwf;
+  B.runbits = words + L.off[0];
+  B.runpre = words + L.off[1];
+  B.lbits = words + L.off[2];
+  B.lpre = words + L.off[3];
+  B.fbits = words + L.off[4];
+  B.fpre = words + L.off[5];
+  B.M = B.runpre + L.nw;
+  B.lcount = B.lpre + L.nw;
+}
+
+// Host launchers.  Each returns the number of kernels it launched.
 // per-instance bounding boxes, grids and the run layout
-void grids(const Bufs& B, int K, int nchunks, double mult2, double mult3, uint64_t dense_floor,
-           uint64_t dense_per_point, cudaStream_t s);
+int grids(const Bufs& B, int K, int nchunks, double mult2, double mult3, uint64_t dense_floor,
+          uint64_t dense_per_point, cudaStream_t s);
 // cell keys in global point order (width from the run layout)
-void keys(const Bufs& B, bool key64, int nchunks, void* keys_out, cudaStream_t s);
-void gather(const Bufs& B, bool key64, int64_t n, bool xf, int sms, cudaStream_t s);
-void run_flags(const void* keys, bool key64, int64_t n, uint32_t* fl, int sms, cudaStream_t s);
-// cell starts (reps), cell count, and the split between 2D and 3D cells
-void run_scatter(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
+int keys(const Bufs& B, bool key64, int nchunks, void* keys_out, cudaStream_t s);
+// sorted float64 (and centred float32) coordinates; one: a single instance
+int gather(const Bufs& B, bool key64, int64_t n, bool xf, bool one, int sms, cudaStream_t s);
+// cell starts: run bits and their ranks, reps, the cell count M, and the split
+// between 2D and 3D cells (mixed: a run holding both)
+int runs(const Bufs& B, bool key64, int64_t n, bool mixed, int sms, void* scan_temp,
+         cudaStream_t s);
 // occupancy bits, row-table cell counts, cellz, each instance's first and last cells
-void cell_counts(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
+int cell_counts(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
 // one-entry start slices (cell counts of instances without a row table); then scan
-void start_fill(const Bufs& B, int K, cudaStream_t s);
+int start_fill(const Bufs& B, int K, cudaStream_t s);
 // occupancy ranks: word prefix counts (scan temp: scan_temp_bytes(occ_words)) and each
 // cell table's rank offset
-void occ_rank(const Bufs& B, int K, void* scan_temp, cudaStream_t s);
+int occ_rank(const Bufs& B, int K, void* scan_temp, cudaStream_t s);
 // sparse instances: hash of occupied rows (clear the slots first)
-void hash_insert(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
-// cell phases; dims: bit 0 = 2D instances present, bit 1 = 3D
-void core(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, void* scan_temp,
+int hash_insert(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s);
+// cell phases; dims: bit 0 = 2D instances present, bit 1 = 3D; one: a single instance
+int core(const Bufs& B, int64_t n, int dims, bool f32, bool key64, bool one, int sms,
+         void* scan_temp, cudaStream_t s);
+int unite(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, void* scan_temp,
           cudaStream_t s);
-void unite(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, void* scan_temp,
-           cudaStream_t s);
-void roots(const Bufs& B, int64_t n, int sms, cudaStream_t s);
-void label(const Bufs& B, bool key64, int64_t n, int sms, void* scan_temp, cudaStream_t s);
-void border(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s);
-void scatter_labels(const Bufs& B, int64_t n, int* out, uint8_t* core_out, int sms,
-                    cudaStream_t s);
-// per-instance cluster counts (K entries) from the cluster-number scan
-void cluster_counts(const Bufs& B, int K, int64_t* out, cudaStream_t s);
-// kernel launches of one cell phase (per dimension present)
-int launches_per_cell_phase(int dims);
+// root marks, cluster numbers (total into *B.K), per-cell cluster ids and core
+// occupancy bits
+int roots(const Bufs& B, bool key64, int64_t n, int sms, void* scan_temp, cudaStream_t s);
+// the border-search list (non-core points)
+int label(const Bufs& B, int64_t n, int sms, void* scan_temp, cudaStream_t s);
+int border(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s);
+int scatter_labels(const Bufs& B, int64_t n, int* out, uint8_t* core_out, int sms,
+                   cudaStream_t s);
+// per-instance cluster counts (K entries) from the cluster marks
+int cluster_counts(const Bufs& B, int K, int64_t* out, cudaStream_t s);
 
 }  // namespace gdl

@@ -71,14 +71,12 @@ constexpr size_t kOffHkeys = kOffOcc + up((3 * (kTableCells / 32 + 1) + 64) * 4)
 constexpr size_t kOffHvals = kOffHkeys + up(kHashSlots * 8);
 constexpr size_t kOffReps = kOffHvals + up(kHashSlots * 8);
 constexpr size_t kOffCellz = kOffReps + up((kMaxPoints + 1) * 4);
-constexpr size_t kOffRunfl = kOffCellz + up(kMaxPoints * 4);
-constexpr size_t kOffRunpos = kOffRunfl + up(kMaxPoints * 4);
-constexpr size_t kOffCore = kOffRunpos + up(kMaxPoints * 4);
+constexpr size_t kOffBits = kOffCellz + up(kMaxPoints * 4);    // cell starts, lists, marks
+constexpr size_t kOffCore = kOffBits + up(gdl::bit_layout(kMaxPoints).words * 4);
 constexpr size_t kOffCellcore = kOffCore + up(kMaxPoints);
 constexpr size_t kOffCellmin = kOffCellcore + up(kMaxPoints * 4);
 constexpr size_t kOffParent = kOffCellmin + up(kMaxPoints * 4);
-constexpr size_t kOffFmark = kOffParent + up(kMaxPoints * 4);
-constexpr size_t kOffCellcid = kOffFmark + up((kMaxPoints + 1) * 4);
+constexpr size_t kOffCellcid = kOffParent + up(kMaxPoints * 4);
 constexpr size_t kOffLab = kOffCellcid + up(kMaxPoints * 4);
 constexpr size_t kOffAsym = kOffLab + up(kMaxPoints * 4);
 constexpr size_t kOffHvCell = kOffAsym + up(gd::kAsymCap * 8);
@@ -266,12 +264,11 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   B.keys = skeys;
   B.ids = vb[r];
   B.blist = vb[1 - r];  // the sort's other id and key buffers are free after the sort
-  B.lflag = reinterpret_cast<uint32_t*>(base + (skeys == base + kOffKeys0 ? kOffKeys1 : kOffKeys0));
-  B.lcount = reinterpret_cast<uint32_t*>(base + kOffSmall + 8);
+  B.cidm = reinterpret_cast<int*>(base + (skeys == base + kOffKeys0 ? kOffKeys1 : kOffKeys0));
+  gdl::set_bits(B, reinterpret_cast<uint32_t*>(base + kOffBits), n);
+  B.K = dK;
   B.X = reinterpret_cast<double*>(base + kOffX);
   B.Xf = reinterpret_cast<float*>(base + kOffXf);
-  B.runfl = reinterpret_cast<uint32_t*>(base + kOffRunfl);
-  B.runpos = reinterpret_cast<uint32_t*>(base + kOffRunpos);
   B.reps = reinterpret_cast<int*>(base + kOffReps);
   B.cellz = reinterpret_cast<uint32_t*>(base + kOffCellz);
   B.start = reinterpret_cast<uint32_t*>(base + kOffTable);
@@ -284,10 +281,8 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   B.hkeys = reinterpret_cast<unsigned long long*>(base + kOffHkeys);
   B.hvals = reinterpret_cast<uint32_t*>(base + kOffHvals);
   B.hmask = (uint32_t)(kHashSlots - 1);
-  gdl::gather(B, key64, n, xf, sms, s);
-  gdl::run_flags(skeys, key64, n, B.runfl, sms, s);
-  gdprim::exclusive_scan_u32(B.runfl, B.runpos, n, base + kOffScanTemp, dM, s);
-  gdl::run_scatter(B, key64, n, sms, s);
+  gdl::gather(B, key64, n, xf, true, sms, s);
+  gdl::runs(B, key64, n, false, sms, base + kOffScanTemp, s);
   NA_CUDA(cudaMemsetAsync(B.start, 0, bi.start_total * 4, s), "clear row table");
   if (B.occ_words) NA_CUDA(cudaMemsetAsync(B.occ, 0, B.occ_words * 4, s), "clear occupancy");
   gdl::cell_counts(B, key64, n, sms, s);
@@ -305,18 +300,15 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   B.cellcore = reinterpret_cast<int*>(base + kOffCellcore);
   B.cellmin = reinterpret_cast<int*>(base + kOffCellmin);
   B.parent = reinterpret_cast<int*>(base + kOffParent);
-  B.Fmark = reinterpret_cast<uint32_t*>(base + kOffFmark);
   B.cellcid = reinterpret_cast<int*>(base + kOffCellcid);
   B.lab = reinterpret_cast<int*>(base + kOffLab);
   B.asym = reinterpret_cast<int*>(base + kOffAsym);
   B.hv_cell = reinterpret_cast<int*>(base + kOffHvCell);
   B.hv_mask = reinterpret_cast<unsigned long long*>(base + kOffHvMask);
-  gdl::core(B, n, dims, f32, key64, sms, base + kOffScanTemp, s);
+  gdl::core(B, n, dims, f32, key64, true, sms, base + kOffScanTemp, s);
   gdl::unite(B, n, dims, f32, key64, sms, base + kOffScanTemp, s);
-  NA_CUDA(cudaMemsetAsync(B.Fmark, 0, (n + 1) * 4, s), "clear cluster marks");
-  gdl::roots(B, n, sms, s);
-  gdprim::exclusive_scan_u32(B.Fmark, B.Fmark, n + 1, base + kOffScanTemp, dK, s);
-  gdl::label(B, key64, n, sms, base + kOffScanTemp, s);
+  gdl::roots(B, key64, n, sms, base + kOffScanTemp, s);
+  gdl::label(B, n, sms, base + kOffScanTemp, s);
   gdl::border(B, n, dims, f32, key64, sms, s);
   gdl::scatter_labels(B, n, labels_dev, nullptr, sms, s);
   NA_CUDA(cudaGetLastError(), "launch");

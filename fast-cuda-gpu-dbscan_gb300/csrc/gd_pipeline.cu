@@ -52,6 +52,80 @@ __global__ void k_bbox_init(const gdl::Bufs B, int K) {
 
 constexpr int kBboxThreads = 256;
 
+// Calls f(l, x) for every point l in [l0, l1) of an instance whose coordinates
+// start at pts (row-major, D doubles per point), x holding its coordinates;
+// the block's threads share the range.  With pts 16-byte aligned the points
+// come in 16-byte vector loads (2D: one per point, four points in flight per
+// thread; 3D: three per pair of points, l0 even), otherwise in scalar loads.
+template <int D, class F>
+__device__ __forceinline__ void for_points(const double* __restrict__ pts, int64_t l0, int64_t l1,
+                                           F&& f) {
+  const int t = threadIdx.x, NT = blockDim.x;
+  if ((reinterpret_cast<uintptr_t>(pts) & 15) == 0 && (D == 2 || (l0 & 1) == 0)) {
+    const double2* __restrict__ p2 = reinterpret_cast<const double2*>(pts);
+    if constexpr (D == 2) {
+      for (int64_t base = l0; base < l1; base += 4 * NT) {
+        double2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int64_t l = base + u * NT + t;
+          if (l < l1) v[u] = __ldg(p2 + l);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int64_t l = base + u * NT + t;
+          if (l < l1) {
+            const double x[3] = {v[u].x, v[u].y, 0.0};
+            f(l, x);
+          }
+        }
+      }
+    } else {
+      const int64_t q0 = l0 >> 1, q1 = l1 >> 1;  // whole pairs: points [2 q0, 2 q1)
+      for (int64_t base = q0; base < q1; base += 2 * NT) {
+        double2 v[2][3];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int64_t q = base + u * NT + t;
+          if (q < q1) {
+            v[u][0] = __ldg(p2 + 3 * q);
+            v[u][1] = __ldg(p2 + 3 * q + 1);
+            v[u][2] = __ldg(p2 + 3 * q + 2);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int64_t q = base + u * NT + t;
+          if (q < q1) {
+            const double a[3] = {v[u][0].x, v[u][0].y, v[u][1].x};
+            f(2 * q, a);
+            const double b[3] = {v[u][1].y, v[u][2].x, v[u][2].y};
+            f(2 * q + 1, b);
+          }
+        }
+      }
+      if ((l1 & 1) && t == 0 && l1 - 1 >= l0) {  // odd last point
+        const int64_t l = l1 - 1;
+        const double x[3] = {pts[3 * l], pts[3 * l + 1], pts[3 * l + 2]};
+        f(l, x);
+      }
+    }
+    return;
+  }
+  for (int64_t l = l0 + t; l < l1; l += NT) {
+    double x[3] = {0.0, 0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < D; ++k) x[k] = pts[l * D + k];
+    f(l, x);
+  }
+}
+
+// Order-preserving int64 image of a double's bits (monotone for non-NaN values).
+__device__ __forceinline__ long long ord_of(double v) {
+  const long long bv = __double_as_longlong(v);
+  return bv >= 0 ? bv : bv ^ 0x7fffffffffffffffLL;
+}
+
 // one block per chunk of one instance; one atomic per block and bound
 __global__ void __launch_bounds__(kBboxThreads) k_bbox_chunk(const gdl::Bufs B) {
   const Chunk c = B.chunks[blockIdx.x];
@@ -59,19 +133,19 @@ __global__ void __launch_bounds__(kBboxThreads) k_bbox_chunk(const gdl::Bufs B) 
   const int dim = I.dim;
   long long lo[3] = {LLONG_MAX, LLONG_MAX, LLONG_MAX}, hi[3] = {LLONG_MIN, LLONG_MIN, LLONG_MIN};
   bool bad = false;
-  const long long* __restrict__ bits = reinterpret_cast<const long long*>(B.coords + I.co_off);
-  for (int64_t g = c.begin + threadIdx.x; g < c.end; g += blockDim.x) {
-    const int64_t l = g - I.pt_off;
-#pragma unroll
+  const double* __restrict__ pts = B.coords + I.co_off;
+  auto take = [&](int64_t, const double* x) {
     for (int k = 0; k < 3; ++k) {
       if (k >= dim) break;
-      const long long bv = bits[l * dim + k];
+      const long long bv = __double_as_longlong(x[k]);
       bad |= (bv & 0x7ff0000000000000LL) == 0x7ff0000000000000LL;
-      const long long o = bv >= 0 ? bv : bv ^ 0x7fffffffffffffffLL;
+      const long long o = ord_of(x[k]);
       lo[k] = min(lo[k], o);
       hi[k] = max(hi[k], o);
     }
-  }
+  };
+  if (dim == 2) for_points<2>(pts, c.begin - I.pt_off, c.end - I.pt_off, take);
+  else for_points<3>(pts, c.begin - I.pt_off, c.end - I.pt_off, take);
   __shared__ long long s[6][kBboxThreads / 32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
@@ -387,6 +461,12 @@ __global__ void __launch_bounds__(1024) k_layout(const gdl::Bufs B, int K) {
 }
 
 // ------------------------------------------------------------------ keys
+// floor(fl64(fl64(x - lo) * inv_f)) as an int: t is finite; out-of-range
+// values saturate, and the caller's clamp takes them to the grid's edge.
+__device__ __forceinline__ int cell_index_f64(double x, double lo, double inv_f) {
+  return __double2int_rd(__dmul_rn(__dsub_rn(x, lo), inv_f));
+}
+
 // One block per chunk: cell key of every point, instance id above the local key.
 template <class Key>
 __global__ void __launch_bounds__(256) k_keys(const gdl::Bufs B, Key* __restrict__ keys) {
@@ -402,14 +482,16 @@ __global__ void __launch_bounds__(256) k_keys(const gdl::Bufs B, Key* __restrict
   float lo32[3];
   for (int k = 0; k < 3; ++k) lo32[k] = P.key_lo32[k];
   const double* __restrict__ pts = B.coords + P.co_off;
-  for (int64_t g = c.begin + threadIdx.x; g < c.end; g += blockDim.x) {
-    const int64_t l = g - P.pt_off;
+  Key* __restrict__ out = keys + P.pt_off;
+  auto key_of = [&](int64_t l, const double* xs) {
     uint64_t key = 0;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       if (k >= D) break;
-      const double x = pts[l * D + k];
-      int64_t q;
+      const double x = xs[k];
+      // 32-bit cell index: conversions to 64-bit integers run on this GPU's
+      // narrow float64 pipe; every cell index is below 2^31 (grids are checked)
+      int q;
       bool fast = false;
       if (kfast) {
         // float32 cell position (no float64 instruction), used when it is
@@ -423,23 +505,30 @@ __global__ void __launch_bounds__(256) k_keys(const gdl::Bufs B, Key* __restrict
                                  : __uint_as_float(sgn | ((unsigned)fe << 23) |
                                                    (unsigned)((bits >> 29) & 0x7fffffu));
           const float t = __fmul_rn(__fsub_rn(x32, lo32[k]), inv32);
-          const float fl = floorf(t);
-          const float fr = __fsub_rn(t, fl);
-          if (fabsf(t) < 4194304.0f && fr > band && fr < 1.0f - band) {
-            q = (int64_t)fl;
-            fast = true;
+          if (fabsf(t) < 4194304.0f) {
+            // floor without a conversion instruction: for |t| < 2^22,
+            // t + 1.5 * 2^23 rounded down lies in [2^23, 2^24), where floats are
+            // the integers, so it is floor(t) + 1.5 * 2^23 exactly and its
+            // mantissa bits hold floor(t) + 2^22
+            const float s = __fadd_rd(t, 12582912.0f);
+            const float fl = __fsub_rn(s, 12582912.0f);
+            const float fr = __fsub_rn(t, fl);
+            if (fr > band && fr < 1.0f - band) {
+              q = (int)(__float_as_uint(s) - 0x4b400000u);
+              fast = true;
+            }
           }
         }
       }
-      if (!fast) {
-        const double t = __dmul_rn(__dsub_rn(x, lo[k]), inv_f);
-        q = __double2ll_rd(t);  // floor and convert in one step (t is finite)
-      }
-      q = q < 0 ? 0 : (q >= G[k] ? G[k] - 1 : q);
+      // the float64 formula for the few coordinates near a cell boundary
+      if (!fast) q = cell_index_f64(x, lo[k], inv_f);
+      q = q < 0 ? 0 : ((int64_t)q >= G[k] ? (int)(G[k] - 1) : q);
       key = key * (uint64_t)G[k] + (uint64_t)q;
     }
-    keys[g] = (Key)(hi | key);
-  }
+    out[l] = (Key)(hi | key);
+  };
+  if (D == 2) for_points<2>(pts, c.begin - P.pt_off, c.end - P.pt_off, key_of);
+  else for_points<3>(pts, c.begin - P.pt_off, c.end - P.pt_off, key_of);
 }
 
 template <class Key>
@@ -447,55 +536,129 @@ __device__ __forceinline__ int inst_of(Key key, int LB) {
   return (int)((uint64_t)key >> LB);
 }
 
-// sorted structure-of-arrays copy (+ centred float32 copy)
-template <class Key, bool XF>
-__global__ void k_gather(const gdl::Bufs B, int64_t n) {
-  const int LB = B.Bi->LB;
-  const Key* __restrict__ keys = static_cast<const Key*>(B.keys);
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t g = B.ids[i];
-    const DevParams& P = B.Pv[inst_of(keys[i], LB)];
-    const int D = P.dim;
-    const double* __restrict__ src = B.coords + P.co_off + (g - P.pt_off) * D;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      if (k >= D) break;
-      const double v = src[k];
-      B.X[k * n + i] = v;
-      if (XF) B.Xf[k * n + i] = __double2float_rn(__dsub_rn(v, P.centre[k]));
+// Coordinates of one point in 16-byte loads where the address allows (a 2D
+// point at a 16-byte boundary is one load; a 3D point is a 16-byte and an
+// 8-byte load, in the order its alignment allows).
+template <int D>
+__device__ __forceinline__ void load_coords(const double* __restrict__ src, double* v) {
+  const bool a16 = (reinterpret_cast<uintptr_t>(src) & 15) == 0;
+  if (D == 2) {
+    if (a16) {
+      const double2 t = __ldg(reinterpret_cast<const double2*>(src));
+      v[0] = t.x;
+      v[1] = t.y;
+    } else {
+      v[0] = __ldg(src);
+      v[1] = __ldg(src + 1);
+    }
+  } else {
+    if (a16) {
+      const double2 t = __ldg(reinterpret_cast<const double2*>(src));
+      v[0] = t.x;
+      v[1] = t.y;
+      v[2] = __ldg(src + 2);
+    } else {
+      v[0] = __ldg(src);
+      const double2 t = __ldg(reinterpret_cast<const double2*>(src + 1));
+      v[1] = t.x;
+      v[2] = t.y;
     }
   }
 }
 
-template <class Key>
-__global__ void k_run_flags(const Key* __restrict__ keys, int64_t n, uint32_t* __restrict__ fl) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    fl[i] = (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
-}
-
-__global__ void k_run_scatter(const gdl::Bufs B, int64_t n) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    if (B.runfl[i]) B.reps[B.runpos[i]] = (int)i;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    B.reps[*B.M] = (int)n;
-    B.ctr[kCtrCells] = *B.M;
+// Sorted structure-of-arrays copy (+ centred float32 copy).  ONE: a single
+// instance (its parameters are Pv[0], no key is read).  Two points per thread
+// and pass, so that two random loads are in flight.
+template <class Key, bool XF, bool ONE>
+__global__ void k_gather(const gdl::Bufs B, int64_t n) {
+  const int LB = B.Bi->LB;
+  const Key* __restrict__ keys = static_cast<const Key*>(B.keys);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < n; i0 += 2 * stride) {
+    double v[2][3];
+    const DevParams* Pp[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int64_t i = i0 + u * stride;
+      Pp[u] = nullptr;
+      if (i < n) {
+        const int64_t g = B.ids[i];
+        const DevParams& P = B.Pv[ONE ? 0 : inst_of(keys[i], LB)];
+        Pp[u] = &P;
+        const double* src = B.coords + P.co_off + (g - P.pt_off) * P.dim;
+        if (P.dim == 2) load_coords<2>(src, v[u]);
+        else load_coords<3>(src, v[u]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int64_t i = i0 + u * stride;
+      if (i >= n) continue;
+      const DevParams& P = *Pp[u];
+      const int D = P.dim;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        if (k >= D) break;
+        B.X[k * n + i] = v[u][k];
+        if (XF) B.Xf[k * n + i] = __double2float_rn(__dsub_rn(v[u][k], P.centre[k]));
+      }
+    }
   }
 }
 
-// number of cells of 2D instances (2D instances come first): binary search
+// ---------------------------------------------------------------- bit masks
+// Number of set bits of a mask below position i (0 <= i <= its length): the
+// word prefix count plus the set bits of i's word below it.
+__device__ __forceinline__ uint32_t bit_rank(const uint32_t* __restrict__ bits,
+                                             const uint32_t* __restrict__ pre, int64_t i) {
+  const int64_t w = i >> 5;
+  return pre[w] + (uint32_t)__popc(bits[w] & ((1u << (i & 31)) - 1u));
+}
+
+// Cell index m of sorted position i: the cell starts at or before i, less one.
+__device__ __forceinline__ int cell_of(const gdl::Bufs& B, int64_t i) {
+  const int64_t w = i >> 5;
+  return (int)(B.runpre[w] + (uint32_t)__popc(B.runbits[w] & (0xffffffffu >> (31 - (i & 31))))) -
+         1;
+}
+
+// Cell starts: one bit per sorted position (a key differing from the one
+// before it), written a word per warp.
 template <class Key>
-__global__ void k_split(const gdl::Bufs B) {
+__global__ void k_run_bits(const Key* __restrict__ keys, int64_t n, uint32_t* __restrict__ bits) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); i0 < n;
+       i0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = i0 + lane;
+    const Key k = i < n ? keys[i] : (Key)0;
+    Key prev = __shfl_up_sync(kFull, k, 1);
+    if (lane == 0 && i > 0) prev = keys[i - 1];
+    const unsigned b = __ballot_sync(kFull, i < n && (i == 0 || k != prev));
+    if (lane == 0) bits[i0 >> 5] = b;
+  }
+}
+
+// After the cell starts are listed in reps: reps[M] = n, the cell count, and
+// (mixed runs) the number of cells of 2D instances -- 2D instances come first,
+// the first cell of a 3D instance is found by binary search.
+template <class Key>
+__global__ void k_runs_finish(const gdl::Bufs B, int64_t n, int mixed) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const Key* keys = static_cast<const Key*>(B.keys);
-  const int LB = B.Bi->LB, K2 = B.Bi->K2;
-  int64_t lo = 0, hi = *B.M;  // first cell with instance >= K2
-  while (lo < hi) {
-    const int64_t mid = (lo + hi) / 2;
-    if (inst_of(keys[B.reps[mid]], LB) < K2) lo = mid + 1;
-    else hi = mid;
+  const int64_t M = *B.M;
+  B.reps[M] = (int)n;
+  B.ctr[kCtrCells] = (unsigned long long)M;
+  const int K2 = B.Bi->K2;
+  int64_t lo = K2 > 0 ? M : 0;
+  if (mixed) {
+    const Key* keys = static_cast<const Key*>(B.keys);
+    const int LB = B.Bi->LB;
+    int64_t hi = M;  // first cell with instance >= K2
+    lo = 0;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) / 2;
+      if (inst_of(keys[B.reps[mid]], LB) < K2) lo = mid + 1;
+      else hi = mid;
+    }
   }
   B.ctr[kCtrCells2D] = (unsigned long long)lo;
 }
@@ -540,13 +703,6 @@ __global__ void k_start_fill(const gdl::Bufs B, int K) {
     const DevParams& P = B.Pv[i];
     if (P.sparse != 2) B.start[P.start_off] = P.n > 0 ? (uint32_t)(P.m1 - P.m0 + 1) : 0u;
   }
-}
-
-// Occupancy ranks: set bits per word, scanned afterwards into wpre.
-__global__ void k_occ_popc(const gdl::Bufs B) {
-  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < (int64_t)B.occ_words;
-       w += (int64_t)gridDim.x * blockDim.x)
-    B.wpre[w] = (uint32_t)__popc(B.occ[w]);
 }
 
 // A cell table's cells appear in reps in table order from the instance's first
@@ -774,6 +930,28 @@ __device__ __forceinline__ int warp_min_i32(int v) {
   return v;
 }
 
+// The lanes sharing this lane's value v, for values that sit in runs of
+// consecutive lanes (lanes holding sorted points: a cell's points are
+// neighbours).  act: the lanes taking part; the result is the run of
+// consecutive active lanes with v that holds this lane (0 for an inactive
+// lane).  Equal values split by an inactive lane give two runs.  All 32 lanes
+// call it.  (__match_any_sync gives the same sets for such values, at a
+// higher cost.)
+__device__ __forceinline__ unsigned run_peers(unsigned act, int v) {
+  const int lane = threadIdx.x & 31;
+  const int prev = __shfl_up_sync(kFull, v, 1);
+  const bool on = (act >> lane) & 1u;
+  const bool prev_on = ((act << 1) >> lane) & 1u;             // lane - 1 active (0 for lane 0)
+  const bool head = on && (!prev_on || prev != v);
+  const unsigned heads = __ballot_sync(kFull, head);
+  if (!on) return 0u;
+  const unsigned upto = (unsigned)((2ull << lane) - 1ull);   // lanes 0..lane
+  const int s = 31 - __clz(heads & upto);                     // this run's head
+  const unsigned stop = (heads | ~act) & ~upto;               // next head or gap
+  const int e = stop ? __ffs(stop) - 1 : 32;
+  return (unsigned)(((1ull << e) - 1ull) & ~((1ull << s) - 1ull));
+}
+
 // Cell lookup inside one instance.  Dense grids: the instance's slice of the
 // cell tables gives every cell's point range (an occupancy bit per entry skips
 // empty cells without touching the table).  Sparse grids: a hash of the
@@ -931,7 +1109,7 @@ __device__ __forceinline__ uint64_t key_at(const gdl::Bufs& B, int64_t i) {
 
 // first sorted position (rep) of the cell holding sorted position i
 __device__ __forceinline__ int rep_of(const gdl::Bufs& B, int64_t i) {
-  return B.reps[B.runpos[i] + B.runfl[i] - 1];
+  return B.reps[cell_of(B, i)];
 }
 
 // The cell a kernel thread/warp works on: instance parameters and local key.
@@ -1235,7 +1413,7 @@ struct RowWalk {
 // next cell of a row walk: [q, end), its last-axis offset from the cell in work
 template <bool KEY64>
 __device__ __forceinline__ int cell_end(const gdl::Bufs& B, int q) {
-  return B.reps[B.runpos[q] + 1];
+  return B.reps[cell_of(B, q) + 1];
 }
 
 // Squared largest / smallest distance (plus / minus the position error) along
@@ -1276,10 +1454,10 @@ struct CoreFlushStage {
 
 // Core flags of points in dense cells (at least minpts points: all core, no
 // test), with their cells' core counts and smallest core indices.  Every other
-// point is flagged for the walk list (scanned and scattered in sorted order
+// point gets its bit in the walk list's mask (listed in sorted order
 // afterwards), so that k_core_point's warps hold only neighbouring points that
-// walk.
-template <bool KEY64>
+// walk.  ONE: a single instance (its parameters are Pv[0]).
+template <bool KEY64, bool ONE>
 __global__ void k_core_split(const gdl::Bufs B, int64_t n) {
   const int LB = B.Bi->LB;
   const int lane = threadIdx.x & 31;
@@ -1290,19 +1468,21 @@ __global__ void k_core_split(const gdl::Bufs B, int64_t n) {
     bool dn = false;
     int b = 0;
     if (i < n) {
-      const int m = (int)(B.runpos[i] + B.runfl[i]) - 1;
+      const int m = cell_of(B, i);
       b = B.reps[m];
       const int sz = B.reps[m + 1] - b;
-      dn = sz >= B.Pv[(int)(key_at<KEY64>(B, b) >> LB)].minpts;
+      dn = sz >= B.Pv[ONE ? 0 : (int)(key_at<KEY64>(B, i) >> LB)].minpts;
       if (dn) {
         B.core[i] = 1;
         if (i == b) ++dense;
       }
-      B.lflag[i] = dn ? 0u : 1u;
     }
+    // the walk list: every point outside a dense cell
+    const unsigned wl = __ballot_sync(kFull, i < n && !dn);
+    if (lane == 0) B.lbits[i0 >> 5] = wl;
     const unsigned cm = __ballot_sync(kFull, dn);
+    const unsigned grp = run_peers(cm, b);
     if (dn) {
-      const unsigned grp = __match_any_sync(cm, b);
       const unsigned mn = __reduce_min_sync(grp, (unsigned)B.ids[i]);
       if (lane == __ffs(grp) - 1) {
         atomicAdd(B.cellcore + b, __popc(grp));
@@ -1313,16 +1493,6 @@ __global__ void k_core_split(const gdl::Bufs B, int64_t n) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) dense += __shfl_xor_sync(kFull, dense, o);
   if (lane == 0 && dense) atomicAdd(B.ctr + kCtrDenseCells, dense);
-}
-
-// The walk list: every flagged point at its scanned position (sorted order).
-__global__ void k_walk_scatter(const gdl::Bufs B, int64_t n) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t a = B.lflag[i];
-    const uint32_t e = i + 1 < n ? B.lflag[i + 1] : *B.lcount;
-    if (e != a) B.blist[a] = (uint32_t)i;
-  }
 }
 
 // Core flags of the listed points (those outside dense cells, in sorted
@@ -1359,7 +1529,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
   // this dimension's part of the walk list: 2D instances' points come first
   const int64_t p3 = B.reps[(int64_t)B.ctr[kCtrCells2D]];
   const int64_t L = (int64_t)*B.lcount;
-  const int64_t L2 = p3 < n ? (int64_t)B.lflag[p3] : L;
+  const int64_t L2 = p3 < n ? (int64_t)bit_rank(B.lbits, B.lpre, p3) : L;
   const int64_t jlo = D == 2 ? 0 : L2, jhi = D == 2 ? L2 : L;
   WalkCursor wc = walk_cursor<D>(B, jlo, jhi);
   Tally t;
@@ -1372,7 +1542,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
     bool isc = false, over = false, pend = false;
     int cnt = 0, nq = 0, minpts = 0;
     if (valid) {
-      m = (int)(B.runpos[i] + B.runfl[i]) - 1;
+      m = cell_of(B, i);
       b = B.reps[m];
       const CellCtx cx = cell_ctx<KEY64>(B, b, LB);
       const DevParams& P = *cx.P;
@@ -1571,8 +1741,8 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
     // per-cell core count and smallest core index, one atomic pair per cell
     // and warp
     const unsigned cm = __ballot_sync(kFull, isc);
+    const unsigned grp = run_peers(cm, b);
     if (isc) {
-      const unsigned grp = __match_any_sync(cm, b);
       const unsigned mn = __reduce_min_sync(grp, (unsigned)B.ids[i]);
       if (lane == __ffs(grp) - 1) {
         atomicAdd(B.cellcore + b, __popc(grp));
@@ -1656,7 +1826,7 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
   // this dimension's part of the core-cell list: 2D instances' cells come first
   const int64_t M2 = (int64_t)B.ctr[kCtrCells2D];
   const int64_t L = (int64_t)*B.lcount;
-  const int64_t L2 = M2 < n ? (int64_t)B.lflag[M2] : L;
+  const int64_t L2 = M2 < n ? (int64_t)bit_rank(B.lbits, B.lpre, M2) : L;
   const int64_t jlo = D == 2 ? 0 : L2, jhi = D == 2 ? L2 : L;
   WalkCursor wc = walk_cursor<D>(B, jlo, jhi);
   Tally t;
@@ -1707,12 +1877,18 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
           z0 = z0 < rw.l0 ? rw.l0 : z0;
           z1 = z1 > rw.l1 ? rw.l1 : z1;
           if (z0 > z1) continue;
-          // one non-empty cell [q, qe) at last-axis offset d
-          auto visit = [&](int q, int qe, int d) {
+          // one non-empty cell [q, qe) at last-axis offset d; core: the cell is
+          // known to hold a core point (core occupancy bits)
+          auto visit = [&](int q, int qe, int d, bool core) {
             const int bit = D == 3 ? half_bit<D>(pass, ox, oy, d) : half_bit<D>(pass, ox, d, 0);
-            if (bit < 0 || B.cellcore[q] <= 0) return;
-            // ra: a root of A's set, refreshed only when q's root differs
-            const int rq = uf_find(B.parent, q);
+            if (bit < 0 || (!core && B.cellcore[q] <= 0)) return;
+            // ra: a root of A's set, refreshed only when q's root differs.  A
+            // parent equal to ra puts q in A's set from one load (ra stays in
+            // A's set whatever is hooked later; the pass before compressed the
+            // parents to roots).
+            const int pq = reinterpret_cast<volatile int*>(B.parent)[q];
+            if (pq == ra) return;
+            const int rq = pq == q ? q : uf_find(B.parent, pq);
             if (rq == ra) return;
             ra = uf_find(B.parent, ra);
             if (rq == ra) return;
@@ -1726,31 +1902,38 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
             }
           };
           if (gv.sparse == 0) {
-            // cell table: the occupied cells from the occupancy bits
+            // cell table: the cells holding a core point, from the occupancy and
+            // core occupancy bits (a cell's index into reps: the rank of the
+            // first occupied one plus the occupied cells before it)
             int64_t rr = 0;
-            uint32_t mask = gv.occ_cells((uint64_t)rk, z0, z1, rr);
-            while (mask) {
-              const int z = __ffs(mask) - 1;
-              mask &= mask - 1;
-              visit(B.reps[rr], B.reps[rr + 1], (int)(z0 + z - rw.cl));
-              ++rr;
+            const uint32_t mask = gv.occ_cells((uint64_t)rk, z0, z1, rr);
+            uint32_t cm = mask ? mask & gv.core_cells((uint64_t)rk, z0, z1) : 0u;
+            while (cm) {
+              const int z = __ffs(cm) - 1;
+              cm &= cm - 1;
+              const int64_t r = rr + __popc(mask & ((1u << z) - 1u));
+              visit(B.reps[r], B.reps[r + 1], (int)(z0 + z - rw.cl), true);
             }
             continue;
           }
           if (gv.sparse == 2) {
-            // row table: the row's cells with last-axis coordinate in [z0, z1]
-            const int2 rc = gv.row_cells(udiv_by((uint64_t)rk, gv.glm, gv.gls));
+            // row table: the row's cells with last-axis coordinate in [z0, z1],
+            // rows without a core point skipped
+            const uint64_t ri = udiv_by((uint64_t)rk, gv.glm, gv.gls);
+            if (!gv.core_row_at(ri)) continue;
+            const int2 rc = gv.row_cells(ri);
             for (int mq = gv.zlower(rc.x, rc.y, z0); mq < rc.y; ++mq) {
               const int64_t z = gv.cellz[mq];
               if (z > z1) break;
-              visit(B.reps[mq], B.reps[mq + 1], (int)(z - rw.cl));
+              visit(B.reps[mq], B.reps[mq + 1], (int)(z - rw.cl), false);
             }
             continue;
           }
           const int2 sp = gv.span_row((uint64_t)rk, z0, z1);
           for (int q = sp.x; q < sp.y;) {
             const int qe = cell_end<KEY64>(B, q);
-            visit(q, qe, (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl));
+            visit(q, qe, (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl),
+                  false);
             q = qe;
           }
           }
@@ -1781,7 +1964,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
   // this dimension's part of the list: 2D instances' points come first
   const int64_t p3 = B.reps[(int64_t)B.ctr[kCtrCells2D]];
   const int64_t L = (int64_t)*B.lcount;
-  const int64_t L2 = p3 < n ? (int64_t)B.lflag[p3] : L;
+  const int64_t L2 = p3 < n ? (int64_t)bit_rank(B.lbits, B.lpre, p3) : L;
   const int64_t jlo = D == 2 ? 0 : L2, jhi = D == 2 ? L2 : L;
   WalkCursor wc = walk_cursor<D>(B, jlo, jhi);
   Tally t;
@@ -1793,7 +1976,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
     bool over = false;
     if (valid) {
       const int64_t i = (int64_t)B.blist[j];
-      m = (int)(B.runpos[i] + B.runfl[i]) - 1;
+      m = cell_of(B, i);
       const int b = B.reps[m];
       const CellCtx cx = cell_ctx<KEY64>(B, b, LB);
       const DevParams& P = *cx.P;
@@ -1922,7 +2105,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
           q = qe;
         }
       }
-      if (!over && best != INT_MAX) B.lab[i] = best;
+      if (!over) B.lab[i] = best == INT_MAX ? kNoise : best;
     }
     // cells with an undecided point, once per warp
     const unsigned om = __ballot_sync(kFull, over);
@@ -2020,29 +2203,38 @@ __global__ void __launch_bounds__(kCellThreads) k_core_heavy(const gdl::Bufs B, 
 }
 
 // ------------------------------------------------------------- union-find
-// Union-find roots, and the flags of the core-cell list (cells with a core
-// point; scanned and scattered in sorted order for k_union_scan).
+// Union-find roots, the mask of the core-cell list (cells with a core point,
+// listed in order for k_union_scan; a word per warp over [0, n)), and the
+// core occupancy bit of every core cell's cell-table (row-table) entry, so the
+// link and border searches skip cells (rows) without core points without
+// looking them up.
+template <bool KEY64>
 __global__ void k_parent_init(const gdl::Bufs B, int64_t n) {
   const int64_t M = *B.M;
-  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < n;
-       m += (int64_t)gridDim.x * blockDim.x) {
-    uint32_t f = 0;
+  const int lane = threadIdx.x & 31;
+  const int LB = B.Bi->LB;
+  for (int64_t m0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); m0 < n;
+       m0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t m = m0 + lane;
+    bool f = false;
     if (m < M) {
       const int b = B.reps[m];
       B.parent[b] = b;
-      f = B.cellcore[b] > 0 ? 1u : 0u;
+      f = B.cellcore[b] > 0;
+      if (f && B.occ_words) {
+        const uint64_t key = key_at<KEY64>(B, b);
+        const DevParams& P = B.Pv[(int)(key >> LB)];
+        if (P.sparse != 1) {
+          const uint64_t local = key & P.kmask;
+          const int a = P.dim - 2;
+          const uint64_t idx =
+              P.occ_off + (P.sparse == 2 ? udiv_by(local, P.dm[a], P.ds[a]) : local);
+          atomicOr(B.cocc + (idx >> 5), 1u << (idx & 31));
+        }
+      }
     }
-    B.lflag[m] = f;
-  }
-}
-
-// The core-cell list: every flagged cell at its scanned position.
-__global__ void k_cell_list_scatter(const gdl::Bufs B, int64_t n) {
-  for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < n;
-       m += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t a = B.lflag[m];
-    const uint32_t e = m + 1 < n ? B.lflag[m + 1] : *B.lcount;
-    if (e != a) B.blist[a] = (uint32_t)m;
+    const unsigned bl = __ballot_sync(kFull, f);
+    if (lane == 0) B.lbits[m0 >> 5] = bl;
   }
 }
 
@@ -2207,66 +2399,53 @@ __global__ void k_compress(const gdl::Bufs B) {
   }
 }
 
-// every root flags its component's smallest core index
+// every root marks its component's smallest core index (a bit over global
+// point indices; cluster numbers are the ranks of these bits)
 __global__ void k_roots(const gdl::Bufs B) {
   const int64_t M = *B.M;
   for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
        m += (int64_t)gridDim.x * blockDim.x) {
     const int b = B.reps[m];
     if (B.cellcore[b] == 0) continue;
-    if (uf_find(B.parent, b) == b) B.Fmark[B.cellmin[b]] = 1u;
+    if (uf_find(B.parent, b) == b) {
+      const uint32_t cm = (uint32_t)B.cellmin[b];
+      atomicOr(B.fbits + (cm >> 5), 1u << (cm & 31));
+    }
   }
 }
 
-// Cluster id of every cell with core points (ordered by smallest core index:
-// Fmark now holds the exclusive scan of the root marks over global indices),
-// and the provisional label of every point: its cluster if core, NOISE otherwise.
-// Cluster numbers restart at 0 in every instance: the scan value at the
-// instance's first point counts the clusters of the instances before it.
-// The border-search list: every non-core point at its scanned position, so
-// the list keeps the sorted order (neighbouring list entries are neighbouring
-// points, 2D instances' first).
-__global__ void k_list_scatter(const gdl::Bufs B, int64_t n) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    if (!B.core[i]) B.blist[B.lflag[i]] = (uint32_t)i;
-}
-
-// Core occupancy: one bit per cell-table (row-table) entry whose cell (row)
-// holds a core point, so the border search skips the rest without lookups.
+// Per cell: the cluster id of its core points (the rank of its root's mark,
+// less the marks of the instances before it: cluster numbers restart at 0 in
+// every instance), INT_MAX without core points.
 template <bool KEY64>
-__global__ void k_core_occ(const gdl::Bufs B) {
+__global__ void k_cell_ids(const gdl::Bufs B) {
   const int LB = B.Bi->LB;
   const int64_t M = *B.M;
   for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
        m += (int64_t)gridDim.x * blockDim.x) {
     const int b = B.reps[m];
-    if (B.cellcore[b] <= 0) continue;
-    const uint64_t key = key_at<KEY64>(B, b);
-    const DevParams& P = B.Pv[(int)(key >> LB)];
-    if (P.sparse == 1) continue;
-    const uint64_t local = key & P.kmask;
-    const int a = P.dim - 2;
-    const uint64_t idx = P.occ_off + (P.sparse == 2 ? udiv_by(local, P.dm[a], P.ds[a]) : local);
-    atomicOr(B.cocc + (idx >> 5), 1u << (idx & 31));
+    int cid = INT_MAX;
+    if (B.cellcore[b] > 0) {
+      const uint64_t key = key_at<KEY64>(B, b);
+      const DevParams& P = B.Pv[(int)(key >> LB)];
+      const int64_t root_min = B.cellmin[uf_find(B.parent, b)];
+      cid = (int)(bit_rank(B.fbits, B.fpre, root_min) - bit_rank(B.fbits, B.fpre, P.pt_off));
+    }
+    B.cellcid[b] = cid;
+    B.cidm[m] = cid;
   }
 }
 
-template <bool KEY64>
+// The mask of the border-search list: every non-core point (listed in sorted
+// order afterwards, so neighbouring list entries are neighbouring points, 2D
+// instances' first), a word per warp.
 __global__ void k_label(const gdl::Bufs B, int64_t n) {
-  const int LB = B.Bi->LB;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const int b = rep_of(B, i);
-    int cl = INT_MAX;
-    if (B.cellcore[b] > 0) {
-      const int64_t pt_off = B.Pv[(int)(key_at<KEY64>(B, i) >> LB)].pt_off;
-      cl = (int)(B.Fmark[B.cellmin[uf_find(B.parent, b)]] - B.Fmark[pt_off]);
-    }
-    if (i == b) B.cellcid[b] = cl;
-    const bool nc = !B.core[i];
-    B.lab[i] = nc ? kNoise : cl;
-    B.lflag[i] = nc ? 1u : 0u;  // the non-core points go to the border-search list
+  const int lane = threadIdx.x & 31;
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); i0 < n;
+       i0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = i0 + lane;
+    const unsigned nc = __ballot_sync(kFull, i < n && !B.core[i]);
+    if (lane == 0) B.lbits[i0 >> 5] = nc;
   }
 }
 
@@ -2367,19 +2546,45 @@ __global__ void __launch_bounds__(kCellThreads) k_border_heavy(const gdl::Bufs B
   flush_tally(t, B.ctr);
 }
 
-// labels back to the caller's point order; counts
+// labels back to the caller's point order (core points: their cell's cluster;
+// the others: the border search's label or NOISE); counts
 __global__ void k_scatter_labels(const gdl::Bufs B, int64_t n, int* __restrict__ out,
                                  uint8_t* __restrict__ core_out) {
   unsigned long long nn = 0, nc = 0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t j = B.ids[i];
-    const int l = B.lab[i];
-    const uint8_t c = B.core[i];
-    out[j] = l;
-    if (core_out) core_out[j] = c;
-    nn += l == kNoise;
-    nc += c;
+  // four points per thread and pass, in straight-line phases so that each
+  // phase's loads are in flight together: ids, core flags, run words; then
+  // both candidate labels (the border search's, and the cell's cluster for a
+  // core point); then the stores
+  constexpr int U = 4;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < n; i0 += U * stride) {
+    uint32_t j[U], rb[U], rp[U];
+    uint8_t c[U];
+    int l[U], lc[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = i0 + u * stride < n ? i0 + u * stride : n - 1;
+      j[u] = B.ids[i];
+      c[u] = B.core[i];
+      rb[u] = B.runbits[i >> 5];
+      rp[u] = B.runpre[i >> 5];
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = i0 + u * stride < n ? i0 + u * stride : n - 1;
+      const int m = (int)(rp[u] + (uint32_t)__popc(rb[u] & (0xffffffffu >> (31 - (i & 31))))) - 1;
+      l[u] = B.lab[i];
+      lc[u] = B.cidm[m];
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (i0 + u * stride >= n) continue;
+      const int lab = c[u] ? lc[u] : l[u];
+      out[j[u]] = lab;
+      if (core_out) core_out[j[u]] = c[u];
+      nn += lab == kNoise;
+      nc += c[u];
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -2392,12 +2597,12 @@ __global__ void k_scatter_labels(const gdl::Bufs B, int64_t n, int* __restrict__
   }
 }
 
-// clusters of every instance from the global cluster-number scan (Fmark has
-// n+1 entries, the last one the total)
+// clusters of every instance: the root marks in its range of global indices
 __global__ void k_cluster_counts(const gdl::Bufs B, int K, int64_t* out) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < K; i += gridDim.x * blockDim.x) {
     const InstDesc I = B.inst[i];
-    out[i] = (int64_t)B.Fmark[I.pt_off + I.n] - (int64_t)B.Fmark[I.pt_off];
+    out[i] = (int64_t)bit_rank(B.fbits, B.fpre, I.pt_off + I.n) -
+             (int64_t)bit_rank(B.fbits, B.fpre, I.pt_off);
   }
 }
 
@@ -2415,69 +2620,91 @@ static int grid_for(int64_t work, int threads, int sms, int per_sm) {
   return (int)g;
 }
 
-void grids(const Bufs& B, int K, int nchunks, double mult2, double mult3, uint64_t dense_floor,
-           uint64_t dense_per_point, cudaStream_t s) {
+int grids(const Bufs& B, int K, int nchunks, double mult2, double mult3, uint64_t dense_floor,
+          uint64_t dense_per_point, cudaStream_t s) {
   k_bbox_init<<<(K + 255) / 256, 256, 0, s>>>(B, K);
   if (nchunks > 0) k_bbox_chunk<<<nchunks, kBboxThreads, 0, s>>>(B);
   k_params_inst<<<(K + 127) / 128, 128, 0, s>>>(B, K, mult2, mult3, dense_floor, dense_per_point);
   k_layout<<<1, 1024, 0, s>>>(B, K);
+  return 3 + (nchunks > 0 ? 1 : 0);
 }
 
-void keys(const Bufs& B, bool key64, int nchunks, void* keys_out, cudaStream_t s) {
-  if (nchunks <= 0) return;
+int keys(const Bufs& B, bool key64, int nchunks, void* keys_out, cudaStream_t s) {
+  if (nchunks <= 0) return 0;
   if (key64)
     k_keys<unsigned long long><<<nchunks, 256, 0, s>>>(B, static_cast<unsigned long long*>(keys_out));
   else
     k_keys<uint32_t><<<nchunks, 256, 0, s>>>(B, static_cast<uint32_t*>(keys_out));
+  return 1;
 }
 
-void gather(const Bufs& B, bool key64, int64_t n, bool xf, int sms, cudaStream_t s) {
+int gather(const Bufs& B, bool key64, int64_t n, bool xf, bool one, int sms, cudaStream_t s) {
   const int g = grid_for(n, 256, sms, 8);
   using U64 = unsigned long long;
+#define GD_GATHER(KEY, XF)                                                  \
+  do {                                                                      \
+    if (one) k_gather<KEY, XF, true><<<g, 256, 0, s>>>(B, n);               \
+    else k_gather<KEY, XF, false><<<g, 256, 0, s>>>(B, n);                  \
+  } while (0)
   if (key64) {
-    if (xf) k_gather<U64, true><<<g, 256, 0, s>>>(B, n);
-    else k_gather<U64, false><<<g, 256, 0, s>>>(B, n);
+    if (xf) GD_GATHER(U64, true);
+    else GD_GATHER(U64, false);
   } else {
-    if (xf) k_gather<uint32_t, true><<<g, 256, 0, s>>>(B, n);
-    else k_gather<uint32_t, false><<<g, 256, 0, s>>>(B, n);
+    if (xf) GD_GATHER(uint32_t, true);
+    else GD_GATHER(uint32_t, false);
   }
+#undef GD_GATHER
+  return 1;
 }
 
-void run_flags(const void* keys, bool key64, int64_t n, uint32_t* fl, int sms, cudaStream_t s) {
+// kernels of one exclusive scan over nw words
+static int scan_launches(int64_t nw) { return nw > 0 ? 3 : 0; }
+
+// the set bits of B.lbits over [0, n) listed in order into B.blist, their
+// count in *B.lcount
+static int list_bits(const Bufs& B, int64_t n, int sms, void* scan_temp, cudaStream_t s) {
+  const int64_t nw = (n + 31) / 32;
+  gdprim::exclusive_scan_popc(B.lbits, B.lpre, nw, scan_temp, B.lcount, s);
+  gdprim::compact_bits(B.lbits, B.lpre, nw, B.blist, sms, s);
+  return scan_launches(nw) + (nw > 0 ? 1 : 0);
+}
+
+int runs(const Bufs& B, bool key64, int64_t n, bool mixed, int sms, void* scan_temp,
+         cudaStream_t s) {
   const int g = grid_for(n, 256, sms, 8);
-  if (key64)
-    k_run_flags<unsigned long long><<<g, 256, 0, s>>>(static_cast<const unsigned long long*>(keys),
-                                                      n, fl);
-  else
-    k_run_flags<uint32_t><<<g, 256, 0, s>>>(static_cast<const uint32_t*>(keys), n, fl);
+  const int64_t nw = (n + 31) / 32;
+  if (key64) k_run_bits<unsigned long long><<<g, 256, 0, s>>>(
+      static_cast<const unsigned long long*>(B.keys), n, B.runbits);
+  else k_run_bits<uint32_t><<<g, 256, 0, s>>>(static_cast<const uint32_t*>(B.keys), n, B.runbits);
+  gdprim::exclusive_scan_popc(B.runbits, B.runpre, nw, scan_temp, B.M, s);
+  gdprim::compact_bits(B.runbits, B.runpre, nw, reinterpret_cast<uint32_t*>(B.reps), sms, s);
+  if (key64) k_runs_finish<unsigned long long><<<1, 32, 0, s>>>(B, n, mixed ? 1 : 0);
+  else k_runs_finish<uint32_t><<<1, 32, 0, s>>>(B, n, mixed ? 1 : 0);
+  return 3 + scan_launches(nw);
 }
 
-void run_scatter(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) {
-  k_run_scatter<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
-  if (key64) k_split<unsigned long long><<<1, 32, 0, s>>>(B);
-  else k_split<uint32_t><<<1, 32, 0, s>>>(B);
-}
-
-void cell_counts(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) {
+int cell_counts(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) {
   if (key64) k_cell_counts<unsigned long long><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
   else k_cell_counts<uint32_t><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
+  return 1;
 }
 
-void start_fill(const Bufs& B, int K, cudaStream_t s) {
+int start_fill(const Bufs& B, int K, cudaStream_t s) {
   k_start_fill<<<(K + 127) / 128, 128, 0, s>>>(B, K);
+  return 1;
 }
 
-void occ_rank(const Bufs& B, int K, void* scan_temp, cudaStream_t s) {
-  if (!B.occ_words) return;
-  const int g = (int)std::min<int64_t>(((int64_t)B.occ_words + 255) / 256, 4096);
-  k_occ_popc<<<g, 256, 0, s>>>(B);
-  gdprim::exclusive_scan_u32(B.wpre, B.wpre, (int64_t)B.occ_words, scan_temp, nullptr, s);
+int occ_rank(const Bufs& B, int K, void* scan_temp, cudaStream_t s) {
+  if (!B.occ_words) return 0;
+  gdprim::exclusive_scan_popc(B.occ, B.wpre, (int64_t)B.occ_words, scan_temp, nullptr, s);
   k_rank_off<<<(K + 127) / 128, 128, 0, s>>>(B, K);
+  return scan_launches((int64_t)B.occ_words) + 1;
 }
 
-void hash_insert(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) {
+int hash_insert(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) {
   if (key64) k_row_hash<unsigned long long><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
   else k_row_hash<uint32_t><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
+  return 1;
 }
 
 #define GD_L1(D, f32, key64, KERNEL, GRID, THREADS, ...)                          \
@@ -2498,69 +2725,81 @@ void hash_insert(const Bufs& B, bool key64, int64_t n, int sms, cudaStream_t s) 
     if ((dims) & 2) GD_L1(3, f32, key64, KERNEL, GRID, THREADS, __VA_ARGS__);     \
   } while (0)
 
-int launches_per_cell_phase(int dims) { return ((dims & 1) ? 1 : 0) + ((dims & 2) ? 1 : 0); }
+static int per_dim(int dims) { return ((dims & 1) ? 1 : 0) + ((dims & 2) ? 1 : 0); }
 
-void core(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, void* scan_temp,
-          cudaStream_t s) {
+int core(const Bufs& B, int64_t n, int dims, bool f32, bool key64, bool one, int sms,
+         void* scan_temp, cudaStream_t s) {
   cudaMemsetAsync(B.ctr + kCtrHeavyCore, 0, 8, s);
   // per-cell core counts (0) and smallest core indices (0xffffffff as unsigned)
   cudaMemsetAsync(B.cellcore, 0, (size_t)n * 4, s);
   cudaMemsetAsync(B.cellmin, 0xff, (size_t)n * 4, s);
   // dense cells at once; the other points listed in sorted order for the walk
-  if (key64) k_core_split<true><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
-  else k_core_split<false><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
-  gdprim::exclusive_scan_u32(B.lflag, B.lflag, n, scan_temp, B.lcount, s);
-  k_walk_scatter<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
+  const int g = grid_for(n, 256, sms, 8);
+  if (key64) {
+    if (one) k_core_split<true, true><<<g, 256, 0, s>>>(B, n);
+    else k_core_split<true, false><<<g, 256, 0, s>>>(B, n);
+  } else {
+    if (one) k_core_split<false, true><<<g, 256, 0, s>>>(B, n);
+    else k_core_split<false, false><<<g, 256, 0, s>>>(B, n);
+  }
+  int L = 1 + list_bits(B, n, sms, scan_temp, s);
   cudaMemsetAsync(B.ctr + kCtrWalkCursor2, 0, 16, s);
   GD_LAUNCH_DIMS(dims, f32, key64, k_core_point, sms * 8, kScanThreadsPerBlock, B, n);
   GD_LAUNCH_DIMS(dims, f32, key64, k_core_heavy, sms * 8, kCellThreads, B, n);
+  return L + 2 * per_dim(dims);
 }
 
-void unite(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, void* scan_temp,
-           cudaStream_t s) {
-  k_parent_init<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
-  gdprim::exclusive_scan_u32(B.lflag, B.lflag, n, scan_temp, B.lcount, s);
-  k_cell_list_scatter<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
+int unite(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, void* scan_temp,
+          cudaStream_t s) {
+  if (B.occ_words) cudaMemsetAsync(B.cocc, 0, B.occ_words * 4, s);
+  if (key64) k_parent_init<true><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
+  else k_parent_init<false><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
+  int L = 1 + list_bits(B, n, sms, scan_temp, s);
   for (int pass = 0; pass < 2; ++pass) {
     cudaMemsetAsync(B.ctr + kCtrHeavyUnion, 0, 8, s);
     cudaMemsetAsync(B.ctr + kCtrWalkCursor2, 0, 16, s);
     GD_LAUNCH_DIMS(dims, f32, key64, k_union_scan, sms * 8, kScanThreadsPerBlock, B, n, pass);
     GD_LAUNCH_DIMS(dims, f32, key64, k_union_heavy, sms * 8, kCellThreads, B, n, pass);
+    // every parent to its root: the far pass then finds most neighbours in
+    // A's set from one load (parent[q] == A's root)
+    k_compress<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
   }
-  k_compress<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
   k_asym_resolve<<<1, 32, 0, s>>>(B);
+  return L + 4 * per_dim(dims) + 3;
 }
 
-void roots(const Bufs& B, int64_t n, int sms, cudaStream_t s) {
+int roots(const Bufs& B, bool key64, int64_t n, int sms, void* scan_temp, cudaStream_t s) {
+  cudaMemsetAsync(B.fbits, 0, (size_t)(B.nwf + 1) * 4, s);
   k_roots<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
+  // total clusters into the small block (read with the counters)
+  gdprim::exclusive_scan_popc(B.fbits, B.fpre, B.nwf, scan_temp, B.K, s);
+  if (key64) k_cell_ids<true><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
+  else k_cell_ids<false><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
+  return 2 + scan_launches(B.nwf);
 }
 
-void label(const Bufs& B, bool key64, int64_t n, int sms, void* scan_temp, cudaStream_t s) {
-  if (key64) k_label<true><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
-  else k_label<false><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
-  gdprim::exclusive_scan_u32(B.lflag, B.lflag, n, scan_temp, B.lcount, s);
-  k_list_scatter<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
+int label(const Bufs& B, int64_t n, int sms, void* scan_temp, cudaStream_t s) {
+  k_label<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
+  return 1 + list_bits(B, n, sms, scan_temp, s);
 }
 
-void border(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s) {
+int border(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, cudaStream_t s) {
   cudaMemsetAsync(B.ctr + kCtrHeavyBorder, 0, 8, s);
-  if (B.occ_words) {
-    cudaMemsetAsync(B.cocc, 0, B.occ_words * 4, s);
-    if (key64) k_core_occ<true><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
-    else k_core_occ<false><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
-  }
   cudaMemsetAsync(B.ctr + kCtrWalkCursor2, 0, 16, s);
   GD_LAUNCH_DIMS(dims, f32, key64, k_border_point, sms * 8, kScanThreadsPerBlock, B, n);
   GD_LAUNCH_DIMS(dims, f32, key64, k_border_heavy, sms * 8, kCellThreads, B, n);
+  return 2 * per_dim(dims);
 }
 
-void scatter_labels(const Bufs& B, int64_t n, int* out, uint8_t* core_out, int sms,
-                    cudaStream_t s) {
+int scatter_labels(const Bufs& B, int64_t n, int* out, uint8_t* core_out, int sms,
+                   cudaStream_t s) {
   k_scatter_labels<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n, out, core_out);
+  return 1;
 }
 
-void cluster_counts(const Bufs& B, int K, int64_t* out, cudaStream_t s) {
+int cluster_counts(const Bufs& B, int K, int64_t* out, cudaStream_t s) {
   k_cluster_counts<<<(K + 255) / 256, 256, 0, s>>>(B, K, out);
+  return 1;
 }
 
 }  // namespace gdl

@@ -55,6 +55,14 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* s_warp
   return r;
 }
 
+// value of one scanned element: the element itself, or (POPC) the number of
+// set bits of a 32-bit word
+template <bool POPC>
+__device__ __forceinline__ uint32_t scan_val(uint32_t x) {
+  return POPC ? (uint32_t)__popc(x) : x;
+}
+
+template <bool POPC>
 __global__ void __launch_bounds__(kScanThreads)
 k_scan_reduce(const uint32_t* __restrict__ in, int64_t n, uint32_t* __restrict__ partial) {
   __shared__ uint32_t s_warp[32];
@@ -63,10 +71,11 @@ k_scan_reduce(const uint32_t* __restrict__ in, int64_t n, uint32_t* __restrict__
   if (base + kScanItems <= n) {
     const uint4* p = reinterpret_cast<const uint4*>(in + base);
     uint4 a = p[0], b = p[1];
-    sum = a.x + a.y + a.z + a.w + b.x + b.y + b.z + b.w;
+    sum = scan_val<POPC>(a.x) + scan_val<POPC>(a.y) + scan_val<POPC>(a.z) + scan_val<POPC>(a.w) +
+          scan_val<POPC>(b.x) + scan_val<POPC>(b.y) + scan_val<POPC>(b.z) + scan_val<POPC>(b.w);
   } else {
     for (int i = 0; i < kScanItems; ++i)
-      if (base + i < n) sum += in[base + i];
+      if (base + i < n) sum += scan_val<POPC>(in[base + i]);
   }
   // block reduction
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -99,6 +108,7 @@ k_scan_partials(uint32_t* partial, int64_t T, uint32_t* total_dev) {
   if (threadIdx.x == 0 && total_dev) *total_dev = carry;
 }
 
+template <bool POPC>
 __global__ void __launch_bounds__(kScanThreads)
 k_scan_down(const uint32_t* in, uint32_t* out, int64_t n, const uint32_t* __restrict__ partial) {
   __shared__ uint32_t s_warp[32];
@@ -114,6 +124,8 @@ k_scan_down(const uint32_t* in, uint32_t* out, int64_t n, const uint32_t* __rest
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) v[i] = base + i < n ? in[base + i] : 0u;
   }
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) v[i] = scan_val<POPC>(v[i]);
   uint32_t s = 0;
 #pragma unroll
   for (int i = 0; i < kScanItems; ++i) s += v[i];
@@ -158,11 +170,16 @@ k_rs_upsweep(const K* __restrict__ keys, int64_t n, int shift, uint32_t* __restr
     for (int d = threadIdx.x; d < BINS; d += kRsThreads) h[ww][d] = 0;
   __syncthreads();
   const int64_t seg = (int64_t)blockIdx.x * TILE + w * SEG;
-#pragma unroll 4
+  // every item's key in flight at once, then the counts
+  uint32_t d[ITEMS];
+#pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
     const int64_t e = seg + i * 32 + lane;
-    if (e < n) atomicAdd(&h[w][(uint32_t)(__ldg(keys + e) >> shift) & MASK], 1u);
+    d[i] = e < n ? (uint32_t)(__ldg(keys + e) >> shift) & MASK : 0xffffffffu;
   }
+#pragma unroll
+  for (int i = 0; i < ITEMS; ++i)
+    if (d[i] != 0xffffffffu) atomicAdd(&h[w][d[i]], 1u);
   __syncthreads();
   for (int d = threadIdx.x; d < BINS; d += kRsThreads) {
     uint32_t tot = 0;
@@ -210,7 +227,8 @@ k_rs_downsweep(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
 #pragma unroll
   for (int i = 0; i < ITEMS; ++i) {
     uint32_t d = (uint32_t)(k[i] >> shift) & MASK;
-    // lanes holding the same digit: one ballot per digit bit
+    // lanes holding the same digit: one ballot per digit bit (measured faster
+    // than __match_any_sync here)
     unsigned peers = gd::kFull;
 #pragma unroll
     for (int bit = 0; bit < RB; ++bit) {
@@ -268,6 +286,32 @@ k_rs_downsweep(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
   }
 }
 
+// positions of the set bits, in order: out[pre[w] + r] = 32 w + (bit r of word
+// w).  A warp takes 32 words (one per lane), then writes them one word at a
+// time with a lane per bit, so each word's entries go out in one store.
+__global__ void k_compact_bits(const uint32_t* __restrict__ words,
+                               const uint32_t* __restrict__ pre, int64_t nw,
+                               uint32_t* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;  // 32 words per warp
+  for (int64_t w0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); w0 < nw;
+       w0 += step) {
+    const int64_t w = w0 + lane;
+    const uint32_t x = w < nw ? words[w] : 0u;
+    const uint32_t p = w < nw ? pre[w] : 0u;
+    unsigned busy = __ballot_sync(gd::kFull, x != 0u);
+    while (busy) {
+      const int src = __ffs(busy) - 1;
+      busy &= busy - 1;
+      const uint32_t xs = __shfl_sync(gd::kFull, x, src);
+      const uint32_t ps = __shfl_sync(gd::kFull, p, src);
+      if ((xs >> lane) & 1u)
+        out[ps + (uint32_t)__popc(xs & below)] = (uint32_t)((w0 + src) << 5) + (uint32_t)lane;
+    }
+  }
+}
+
 __global__ void k_iota(uint32_t* v, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -283,17 +327,36 @@ size_t scan_temp_bytes(int64_t n) {
   return align_up((size_t)(T + 1) * sizeof(uint32_t));
 }
 
-void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, void* temp,
-                        uint32_t* total_dev, cudaStream_t s) {
+template <bool POPC>
+void scan_impl(const uint32_t* in, uint32_t* out, int64_t n, void* temp, uint32_t* total_dev,
+               cudaStream_t s) {
   if (n <= 0) {
     if (total_dev) cudaMemsetAsync(total_dev, 0, sizeof(uint32_t), s);
     return;
   }
   int64_t T = (n + kScanTile - 1) / kScanTile;
   uint32_t* partial = static_cast<uint32_t*>(temp);
-  k_scan_reduce<<<(unsigned)T, kScanThreads, 0, s>>>(in, n, partial);
+  k_scan_reduce<POPC><<<(unsigned)T, kScanThreads, 0, s>>>(in, n, partial);
   k_scan_partials<<<1, 1024, 0, s>>>(partial, T, total_dev);
-  k_scan_down<<<(unsigned)T, kScanThreads, 0, s>>>(in, out, n, partial);
+  k_scan_down<POPC><<<(unsigned)T, kScanThreads, 0, s>>>(in, out, n, partial);
+}
+
+void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, void* temp,
+                        uint32_t* total_dev, cudaStream_t s) {
+  scan_impl<false>(in, out, n, temp, total_dev, s);
+}
+
+void exclusive_scan_popc(const uint32_t* words, uint32_t* pre, int64_t nw, void* temp,
+                         uint32_t* total_dev, cudaStream_t s) {
+  scan_impl<true>(words, pre, nw, temp, total_dev, s);
+}
+
+void compact_bits(const uint32_t* words, const uint32_t* pre, int64_t nw, uint32_t* out, int sms,
+                  cudaStream_t s) {
+  if (nw <= 0) return;
+  int64_t g = (nw + 255) / 256;
+  if (g > (int64_t)sms * 8) g = (int64_t)sms * 8;
+  k_compact_bits<<<(unsigned)g, 256, 0, s>>>(words, pre, nw, out);
 }
 
 size_t sort_temp_bytes(int64_t n) {
