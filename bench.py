@@ -794,6 +794,35 @@ def _extra_c5(args, world, local, dist, rank):
     return out
 
 
+def _extra_import():
+    """Dataset import on the host (the reference's ImportDataset, main.cu:469-498,
+    parses text): the same points read from the reference's CSV format and from
+    the raw float64 ('.f64') format through gd_import_dataset, on a
+    1,000,000-point sample of the 10M-point 2D workload (time grows linearly)."""
+    import tempfile
+    api = importlib.import_module(PKG + ".api")
+    ds = importlib.import_module(PKG + ".datasets")
+    inst = ds.zipf2d_10m(seed=0, scale=0.1)
+    out = {"points": inst.n, "dim": inst.dim}
+    with tempfile.TemporaryDirectory() as tmp:
+        csv, raw = os.path.join(tmp, "pts.csv"), os.path.join(tmp, "pts.f64")
+        ds.write_csv(csv, inst.points)
+        np.ascontiguousarray(inst.points).tofile(raw)
+        for name, path in (("csv", csv), ("f64", raw)):
+            best = None
+            for _ in range(2):
+                t0 = time.perf_counter()
+                pts = api.import_dataset(path, inst.dim)
+                dt = time.perf_counter() - t0
+                best = dt if best is None else min(best, dt)
+            out[name] = {"seconds": best, "points_per_s": inst.n / best,
+                         "bytes": os.path.getsize(path),
+                         "equal_to_source": bool(np.array_equal(pts, inst.points))}
+    out["f64_speedup"] = out["csv"]["seconds"] / out["f64"]["seconds"]
+    out["full_10m_estimate_s"] = {k: out[k]["seconds"] * 10 for k in ("csv", "f64")}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -869,6 +898,7 @@ def main():
             line["c3"] = _extra_c3(args, world, local, dist, rank)
             line["c4"] = _extra_c4(args, world, local, dist, rank)
             line["c5"] = _extra_c5(args, world, local, dist, rank)
+            line["import_io"] = _extra_import()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

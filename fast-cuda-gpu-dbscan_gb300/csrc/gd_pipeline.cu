@@ -1346,9 +1346,18 @@ __device__ __forceinline__ WalkCursor walk_cursor(const gdl::Bufs& B, int64_t jl
 // (register budget 65536 / (256 * blocks) per thread).  These kernels are
 // bound by memory latency, so occupancy beats registers; the counts were
 // measured on GB300 (a few spilled bytes cost less than a lost block).
-constexpr int kCoreMinBlocks = 4;
-constexpr int kUnionMinBlocks = 5;
-constexpr int kBorderMinBlocks = 4;
+#ifndef GD_CORE_MIN_BLOCKS
+#define GD_CORE_MIN_BLOCKS 4
+#endif
+#ifndef GD_UNION_MIN_BLOCKS
+#define GD_UNION_MIN_BLOCKS 5
+#endif
+#ifndef GD_BORDER_MIN_BLOCKS
+#define GD_BORDER_MIN_BLOCKS 4
+#endif
+constexpr int kCoreMinBlocks = GD_CORE_MIN_BLOCKS;
+constexpr int kUnionMinBlocks = GD_UNION_MIN_BLOCKS;
+constexpr int kBorderMinBlocks = GD_BORDER_MIN_BLOCKS;
 // The pair-test budgets of one thread (core count per point, link search per
 // cell pair, border search per point) come with the buffers (Bufs::tn_*): the
 // context sets them, the autotuner varies them.

@@ -168,6 +168,29 @@ def test_cli_end_to_end(built_lib, tmp_path, ds, oracle):
     assert np.array_equal(np.loadtxt(str(out), dtype=np.int32), olab)
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_cli_binary_f64_input(built_lib, tmp_path, ds, oracle, dim):
+    """The CLI's binary input (raw row-major float64, '.f64'), the fast path
+    that replaces the text parse of ImportDataset (main.cu:469-498): same
+    labels as the oracle and the same report lines as the CSV path."""
+    import os
+    import subprocess
+    inst = ds.blobs2d_100k(seed=8, scale=0.05) if dim == 2 else ds.aniso3d_20m(seed=8,
+                                                                                scale=0.0005)
+    raw = tmp_path / "pts.f64"
+    np.ascontiguousarray(inst.points, dtype=np.float64).tofile(str(raw))
+    out = tmp_path / "labels.txt"
+    exe = os.path.join(os.path.dirname(built_lib), "gbdbscan_main")
+    r = subprocess.run([exe, str(raw), "--eps", str(inst.eps), "--minpts", str(inst.minpts),
+                        "--dim", str(dim), "--out", str(out)], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stderr
+    olab, _, c = oracle.oracle_dbscan(inst.points, inst.eps, inst.minpts)
+    assert f"Final cluster after merging: {c['clusters']}" in r.stdout
+    assert f"Number of noises: {c['noise']}" in r.stdout
+    assert np.array_equal(np.loadtxt(str(out), dtype=np.int32), olab)
+
+
 @pytest.mark.parametrize("prec", PRECISIONS)
 @pytest.mark.parametrize("d,extent,hashed", [(2, 1e4, False), (2, 1e7, True),
                                              (3, 1e2, False), (3, 1e4, True)])
