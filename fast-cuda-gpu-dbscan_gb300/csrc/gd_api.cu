@@ -165,7 +165,6 @@ struct gd_ctx {
     B.ids = sids;
     // the sort's other id and key buffers are free after the sort
     B.blist = static_cast<uint32_t*>(sids == vals0.p ? vals1.p : vals0.p);
-    B.cidm = static_cast<int*>(skeys == keys0.p ? keys1.p : keys0.p);
     B.reps = static_cast<int*>(reps.p);
     if (bits.p) gdl::set_bits(B, static_cast<uint32_t*>(bits.p), n);
     B.K = dK();

@@ -10,11 +10,12 @@
 //                   (grids up to max(2^26, 8n) cells), or, for larger (sparse)
 //                   grids, a hash of the occupied cells' 64-bit keys -> m
 //   reps[M+1] i32   sorted position of the first point of every non-empty cell
-// Per non-empty cell, indexed by its first sorted position b ("rep"):
-//   cellcore[b]  number of core points in the cell
-//   cellmin[b]   smallest original index among the cell's core points
-//   parent[b]    union-find parent (a rep position)
-//   cellcid[b]   cluster id of the cell's core points
+// Per non-empty cell, indexed by its cell index m (0..M-1, key order; the
+// walks reach it from occupancy ranks without loading reps):
+//   cellcore[m]  number of core points in the cell
+//   cellmin[m]   smallest original index among the cell's core points
+//   parent[m]    union-find parent (a cell index)
+//   cellcid[m]   cluster id of the cell's core points (INT_MAX: none)
 #pragma once
 
 #include <cuda_runtime.h>

@@ -54,11 +54,10 @@ struct Bufs {
   double* X = nullptr;          // sorted float64 coordinates, max_dim x n
   float* Xf = nullptr;          // sorted centred float32 coordinates, max_dim x n
   uint8_t* core = nullptr;      // core flag per sorted position
-  int* cellcore = nullptr;      // per rep: number of core points
-  int* cellmin = nullptr;       // per rep: smallest global index of a core point
-  int* parent = nullptr;        // per rep: union-find parent
-  int* cellcid = nullptr;       // per rep: cluster id of the cell's core points
-  int* cidm = nullptr;          // the same per cell index m (the sort's spare key buffer)
+  int* cellcore = nullptr;      // per cell m: number of core points
+  int* cellmin = nullptr;       // per cell m: smallest global index of a core point
+  int* parent = nullptr;        // per cell m: union-find parent (a cell index)
+  int* cellcid = nullptr;       // per cell m: cluster id of its core points (INT_MAX: none)
   int* lab = nullptr;           // label per sorted position
   int* asym = nullptr;          // kAsymCap (from, to) sorted-position pairs
   uint32_t* blist = nullptr;    // the current walk list (set bits of lbits in order: sorted

@@ -264,7 +264,6 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   B.keys = skeys;
   B.ids = vb[r];
   B.blist = vb[1 - r];  // the sort's other id and key buffers are free after the sort
-  B.cidm = reinterpret_cast<int*>(base + (skeys == base + kOffKeys0 ? kOffKeys1 : kOffKeys0));
   gdl::set_bits(B, reinterpret_cast<uint32_t*>(base + kOffBits), n);
   B.K = dK;
   B.X = reinterpret_cast<double*>(base + kOffX);

@@ -1107,11 +1107,6 @@ __device__ __forceinline__ uint64_t key_at(const gdl::Bufs& B, int64_t i) {
   return static_cast<const uint32_t*>(B.keys)[i];
 }
 
-// first sorted position (rep) of the cell holding sorted position i
-__device__ __forceinline__ int rep_of(const gdl::Bufs& B, int64_t i) {
-  return B.reps[cell_of(B, i)];
-}
-
 // The cell a kernel thread/warp works on: instance parameters and local key.
 struct CellCtx {
   const DevParams* P;
@@ -1475,10 +1470,10 @@ __global__ void k_core_split(const gdl::Bufs B, int64_t n) {
        i0 += (int64_t)gridDim.x * blockDim.x) {
     const int64_t i = i0 + lane;
     bool dn = false;
-    int b = 0;
+    int m = 0;
     if (i < n) {
-      const int m = cell_of(B, i);
-      b = B.reps[m];
+      m = cell_of(B, i);
+      const int b = B.reps[m];
       const int sz = B.reps[m + 1] - b;
       dn = sz >= B.Pv[ONE ? 0 : (int)(key_at<KEY64>(B, i) >> LB)].minpts;
       if (dn) {
@@ -1490,12 +1485,12 @@ __global__ void k_core_split(const gdl::Bufs B, int64_t n) {
     const unsigned wl = __ballot_sync(kFull, i < n && !dn);
     if (lane == 0) B.lbits[i0 >> 5] = wl;
     const unsigned cm = __ballot_sync(kFull, dn);
-    const unsigned grp = run_peers(cm, b);
+    const unsigned grp = run_peers(cm, m);
     if (dn) {
       const unsigned mn = __reduce_min_sync(grp, (unsigned)B.ids[i]);
       if (lane == __ffs(grp) - 1) {
-        atomicAdd(B.cellcore + b, __popc(grp));
-        atomicMin(reinterpret_cast<unsigned*>(B.cellmin) + b, mn);
+        atomicAdd(B.cellcore + m, __popc(grp));
+        atomicMin(reinterpret_cast<unsigned*>(B.cellmin) + m, mn);
       }
     }
   }
@@ -1750,12 +1745,12 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
     // per-cell core count and smallest core index, one atomic pair per cell
     // and warp
     const unsigned cm = __ballot_sync(kFull, isc);
-    const unsigned grp = run_peers(cm, b);
+    const unsigned grp = run_peers(cm, m);
     if (isc) {
       const unsigned mn = __reduce_min_sync(grp, (unsigned)B.ids[i]);
       if (lane == __ffs(grp) - 1) {
-        atomicAdd(B.cellcore + b, __popc(grp));
-        atomicMin(reinterpret_cast<unsigned*>(B.cellmin) + b, mn);
+        atomicAdd(B.cellcore + m, __popc(grp));
+        atomicMin(reinterpret_cast<unsigned*>(B.cellmin) + m, mn);
       }
     }
     // cells with an undecided point, once per warp
@@ -1857,7 +1852,7 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
         rw.init(decompose<D>(cx.local, P), P);
         float oA[D];
         if (Q.prune) cell_origin32<D>(rw.cc, P, oA);
-        int ra = uf_find(B.parent, b);
+        int ra = uf_find(B.parent, (int)m);
         for (int r = 0; r < T.n; ++r) {
           const int ox = T.o[r][0], oy = T.o[r][1];
           // rows with a negative leading offset hold no half-stencil cell
@@ -1886,25 +1881,27 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
           z0 = z0 < rw.l0 ? rw.l0 : z0;
           z1 = z1 > rw.l1 ? rw.l1 : z1;
           if (z0 > z1) continue;
-          // one non-empty cell [q, qe) at last-axis offset d; core: the cell is
-          // known to hold a core point (core occupancy bits)
-          auto visit = [&](int q, int qe, int d, bool core) {
+          // one non-empty cell (index c) at last-axis offset d; core: the cell
+          // is known to hold a core point (core occupancy bits).  Its points
+          // are looked up only when a link search is needed.
+          auto visit = [&](int c, int d, bool core) {
             const int bit = D == 3 ? half_bit<D>(pass, ox, oy, d) : half_bit<D>(pass, ox, d, 0);
-            if (bit < 0 || (!core && B.cellcore[q] <= 0)) return;
-            // ra: a root of A's set, refreshed only when q's root differs.  A
-            // parent equal to ra puts q in A's set from one load (ra stays in
+            if (bit < 0 || (!core && B.cellcore[c] <= 0)) return;
+            // ra: a root of A's set, refreshed only when c's root differs.  A
+            // parent equal to ra puts c in A's set from one load (ra stays in
             // A's set whatever is hooked later; the pass before compressed the
             // parents to roots).
-            const int pq = reinterpret_cast<volatile int*>(B.parent)[q];
-            if (pq == ra) return;
-            const int rq = pq == q ? q : uf_find(B.parent, pq);
-            if (rq == ra) return;
+            const int pc = reinterpret_cast<volatile int*>(B.parent)[c];
+            if (pc == ra) return;
+            const int rc = pc == c ? c : uf_find(B.parent, pc);
+            if (rc == ra) return;
             ra = uf_find(B.parent, ra);
-            if (rq == ra) return;
+            if (rc == ra) return;
+            const int q = B.reps[c], qe = B.reps[c + 1];
             const int res = D == 3 ? inline_link<D, F32>(B, n, b, e, q, qe, oA, ox, oy, d, Q, t)
                                    : inline_link<D, F32>(B, n, b, e, q, qe, oA, ox, d, 0, Q, t);
             if (res > 0) {
-              uf_union(B.parent, B.cellmin, b, q);
+              uf_union(B.parent, B.cellmin, (int)m, c);
               ra = uf_find(B.parent, ra);
             } else if (res < 0) {
               open |= 1ull << bit;
@@ -1921,7 +1918,7 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
               const int z = __ffs(cm) - 1;
               cm &= cm - 1;
               const int64_t r = rr + __popc(mask & ((1u << z) - 1u));
-              visit(B.reps[r], B.reps[r + 1], (int)(z0 + z - rw.cl), true);
+              visit((int)r, (int)(z0 + z - rw.cl), true);
             }
             continue;
           }
@@ -1934,14 +1931,15 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
             for (int mq = gv.zlower(rc.x, rc.y, z0); mq < rc.y; ++mq) {
               const int64_t z = gv.cellz[mq];
               if (z > z1) break;
-              visit(B.reps[mq], B.reps[mq + 1], (int)(z - rw.cl), false);
+              visit(mq, (int)(z - rw.cl), false);
             }
             continue;
           }
           const int2 sp = gv.span_row((uint64_t)rk, z0, z1);
           for (int q = sp.x; q < sp.y;) {
-            const int qe = cell_end<KEY64>(B, q);
-            visit(q, qe, (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl),
+            const int c = cell_of(B, q);
+            const int qe = B.reps[c + 1];
+            visit(c, (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl),
                   false);
             q = qe;
           }
@@ -2032,8 +2030,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
             const int z = __ffs(cm) - 1;
             cm &= cm - 1;
             const int64_t rq = gv.rank((uint64_t)rk + (uint64_t)(rw.l0 + z));
-            const int q = gv.reps[rq], qe = gv.reps[rq + 1];
-            const int cB = B.cellcid[q];
+            const int cB = B.cellcid[rq];
             if (cB >= best) continue;
             int cls = 0;
             if (prune) {
@@ -2045,6 +2042,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
             if (cls > 0) {
               best = cB;
             } else if (cls == 0) {
+              const int q = gv.reps[rq], qe = gv.reps[rq + 1];
               for (int qq = q; qq < qe; ++qq) {
                 if (!B.core[qq]) continue;
                 if (budget-- == 0) {
@@ -2063,9 +2061,10 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
           continue;
         }
         if (gv.sparse == 2 && !gv.core_row_at((uint64_t)ri)) continue;
-        // one non-empty cell [q, qe) at last-axis offset d
-        auto visitb = [&](int q, int qe, int d) {
-          const int cB = B.cellcore[q] > 0 ? B.cellcid[q] : INT_MAX;
+        // one non-empty cell (index c, points [q, qe)) at last-axis offset d;
+        // cells without core points have cluster id INT_MAX
+        auto visitb = [&](int c, int q, int qe, int d) {
+          const int cB = B.cellcid[c];
           if (cB >= best) return;
           int cls = 0;
           if (prune) {
@@ -2097,7 +2096,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
           for (int mq = gv.zlower(rc.x, rc.y, rw.l0); mq < rc.y && !over; ++mq) {
             const int64_t z = gv.cellz[mq];
             if (z > rw.l1) break;
-            visitb(B.reps[mq], B.reps[mq + 1], (int)(z - rw.cl));
+            visitb(mq, B.reps[mq], B.reps[mq + 1], (int)(z - rw.cl));
           }
           continue;
         }
@@ -2109,8 +2108,9 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
              q < rp.y && !over;) {
           const int d = (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
           if (d > dmax) break;
-          const int qe = cell_end<KEY64>(B, q);
-          visitb(q, qe, d);
+          const int c = cell_of(B, q);
+          const int qe = B.reps[c + 1];
+          visitb(c, q, qe, d);
           q = qe;
         }
       }
@@ -2163,7 +2163,7 @@ __global__ void __launch_bounds__(kCellThreads) k_core_heavy(const gdl::Bufs B, 
         mn = min(mn, (int)B.ids[i]);
       }
       mn = warp_min_i32(mn);
-      if (lane == 0) { B.cellcore[b] = sz; B.cellmin[b] = mn; ++dense; }
+      if (lane == 0) { B.cellcore[m] = sz; B.cellmin[m] = mn; ++dense; }
       continue;
     }
     const GridView gv = view_of(B, P);
@@ -2205,7 +2205,7 @@ __global__ void __launch_bounds__(kCellThreads) k_core_heavy(const gdl::Bufs B, 
       __syncwarp();
     }
     mn = warp_min_i32(mn);
-    if (lane == 0) { B.cellcore[b] = ncore; B.cellmin[b] = mn; }
+    if (lane == 0) { B.cellcore[m] = ncore; B.cellmin[m] = mn; }
   }
   flush_tally(t, B.ctr);
   if (lane == 0 && dense) atomicAdd(B.ctr + kCtrDenseCells, dense);
@@ -2227,11 +2227,10 @@ __global__ void k_parent_init(const gdl::Bufs B, int64_t n) {
     const int64_t m = m0 + lane;
     bool f = false;
     if (m < M) {
-      const int b = B.reps[m];
-      B.parent[b] = b;
-      f = B.cellcore[b] > 0;
+      B.parent[m] = (int)m;
+      f = B.cellcore[m] > 0;
       if (f && B.occ_words) {
-        const uint64_t key = key_at<KEY64>(B, b);
+        const uint64_t key = key_at<KEY64>(B, B.reps[m]);
         const DevParams& P = B.Pv[(int)(key >> LB)];
         if (P.sparse != 1) {
           const uint64_t local = key & P.kmask;
@@ -2278,14 +2277,17 @@ __global__ void __launch_bounds__(kCellThreads) k_union_heavy(const gdl::Bufs B,
     for (int t0 = 0; t0 < T.n; t0 += 32) {
       const int tt = t0 + lane;
       bool cand = false;
-      int bB = 0, eB = 0;
+      int bB = 0, eB = 0, cB = 0;
       if (tt < T.n && ((open >> tt) & 1ull)) {
         const int64_t kb = offset_key<D>(cc, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
         if (kb >= 0) {
           const int2 cb = gv.cell((uint64_t)kb);
           bB = cb.x;
           eB = cb.y;
-          cand = bB < eB && B.cellcore[bB] > 0 && uf_find(B.parent, bB) != uf_find(B.parent, b);
+          if (bB < eB) {
+            cB = cell_of(B, bB);
+            cand = B.cellcore[cB] > 0 && uf_find(B.parent, cB) != uf_find(B.parent, (int)m);
+          }
         }
       }
       unsigned mask = __ballot_sync(kFull, cand);
@@ -2294,7 +2296,8 @@ __global__ void __launch_bounds__(kCellThreads) k_union_heavy(const gdl::Bufs B,
         mask &= mask - 1;
         const int cbB = __shfl_sync(kFull, bB, src);
         const int ceB = __shfl_sync(kFull, eB, src);
-        if (uf_find(B.parent, b) == uf_find(B.parent, cbB)) continue;
+        const int ccB = __shfl_sync(kFull, cB, src);
+        if (uf_find(B.parent, (int)m) == uf_find(B.parent, ccB)) continue;
         bool found = false;
         for (int qb = cbB; qb < ceB && !found; qb += 32) {
           const int q = qb + lane;
@@ -2314,7 +2317,7 @@ __global__ void __launch_bounds__(kCellThreads) k_union_heavy(const gdl::Bufs B,
             found = __any_sync(kFull, hit);
           }
         }
-        if (found && lane == 0) uf_union(B.parent, B.cellmin, b, cbB);
+        if (found && lane == 0) uf_union(B.parent, B.cellmin, (int)m, ccB);
         __syncwarp();
       }
     }
@@ -2348,8 +2351,8 @@ __global__ void k_asym_resolve(const gdl::Bufs B) {
   int ne = 0, nv = 0;
   for (unsigned long long i = 0; i < E; ++i) {
     int a = asym_list[2 * i], b = asym_list[2 * i + 1];
-    int ra = uf_find(parent, rep_of(B, a));
-    int rb = uf_find(parent, rep_of(B, b));
+    int ra = uf_find(parent, cell_of(B, a));
+    int rb = uf_find(parent, cell_of(B, b));
     if (ra == rb) continue;
     from[ne] = ra;
     to[ne] = rb;
@@ -2397,14 +2400,13 @@ __global__ void k_asym_resolve(const gdl::Bufs B) {
     if (assigned[v] != node[v]) parent[node[v]] = assigned[v];
 }
 
-// parent[b] <- root (full path compression)
+// parent[m] <- root (full path compression)
 __global__ void k_compress(const gdl::Bufs B) {
   const int64_t M = *B.M;
   for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
        m += (int64_t)gridDim.x * blockDim.x) {
-    const int b = B.reps[m];
-    if (B.cellcore[b] == 0) continue;
-    B.parent[b] = uf_find(B.parent, b);
+    if (B.cellcore[m] == 0) continue;
+    B.parent[m] = uf_find(B.parent, (int)m);
   }
 }
 
@@ -2414,10 +2416,9 @@ __global__ void k_roots(const gdl::Bufs B) {
   const int64_t M = *B.M;
   for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
        m += (int64_t)gridDim.x * blockDim.x) {
-    const int b = B.reps[m];
-    if (B.cellcore[b] == 0) continue;
-    if (uf_find(B.parent, b) == b) {
-      const uint32_t cm = (uint32_t)B.cellmin[b];
+    if (B.cellcore[m] == 0) continue;
+    if (uf_find(B.parent, (int)m) == (int)m) {
+      const uint32_t cm = (uint32_t)B.cellmin[m];
       atomicOr(B.fbits + (cm >> 5), 1u << (cm & 31));
     }
   }
@@ -2432,16 +2433,14 @@ __global__ void k_cell_ids(const gdl::Bufs B) {
   const int64_t M = *B.M;
   for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M;
        m += (int64_t)gridDim.x * blockDim.x) {
-    const int b = B.reps[m];
     int cid = INT_MAX;
-    if (B.cellcore[b] > 0) {
-      const uint64_t key = key_at<KEY64>(B, b);
+    if (B.cellcore[m] > 0) {
+      const uint64_t key = key_at<KEY64>(B, B.reps[m]);
       const DevParams& P = B.Pv[(int)(key >> LB)];
-      const int64_t root_min = B.cellmin[uf_find(B.parent, b)];
+      const int64_t root_min = B.cellmin[uf_find(B.parent, (int)m)];
       cid = (int)(bit_rank(B.fbits, B.fpre, root_min) - bit_rank(B.fbits, B.fpre, P.pt_off));
     }
-    B.cellcid[b] = cid;
-    B.cidm[m] = cid;
+    B.cellcid[m] = cid;
   }
 }
 
@@ -2516,9 +2515,9 @@ __global__ void __launch_bounds__(kCellThreads) k_border_heavy(const gdl::Bufs B
             const int2 cb = gv.cell((uint64_t)kb);
             bB = cb.x;
             eB = cb.y;
-            if (bB < eB && B.cellcore[bB] > 0) {
-              has = true;
-              cid = B.cellcid[bB];
+            if (bB < eB) {
+              cid = B.cellcid[cell_of(B, bB)];  // INT_MAX without core points
+              has = cid != INT_MAX;
             }
           }
         }
@@ -2583,7 +2582,7 @@ __global__ void k_scatter_labels(const gdl::Bufs B, int64_t n, int* __restrict__
       const int64_t i = i0 + u * stride < n ? i0 + u * stride : n - 1;
       const int m = (int)(rp[u] + (uint32_t)__popc(rb[u] & (0xffffffffu >> (31 - (i & 31))))) - 1;
       l[u] = B.lab[i];
-      lc[u] = B.cidm[m];
+      lc[u] = B.cellcid[m];
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
