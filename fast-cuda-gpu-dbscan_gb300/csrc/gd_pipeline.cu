@@ -843,24 +843,30 @@ __device__ __forceinline__ float dist2_f32(const float* a, const float* b) {
 }
 
 // Directed test "cand is a neighbour of centre".  One side is a staged point
-// (coords in smem), the other a candidate (coords in registers / memory).
-// stage_is_centre selects which is the centre of the query box.
+// (sorted position si; float64 coordinates sx in float64 mode), the other a
+// candidate (sorted position q; coordinates in registers).  stage_is_centre
+// selects which is the centre of the query box.  In float32-band mode the
+// float64 coordinates of both are loaded only for a band re-test.
 template <int D, bool F32, class PP>
 __device__ __forceinline__ bool pair_test(const double* sx, const float* sf, const Cand<D, F32>& c,
                                           const double* __restrict__ X, int64_t n, int64_t q,
-                                          bool stage_is_centre, const PP& P, Tally& t) {
+                                          int64_t si, bool stage_is_centre, const PP& P,
+                                          Tally& t) {
   if (F32) {
     ++t.t32;
     float s = dist2_f32<D>(sf, c.f);
     if (s < P.eps2_lo32) return true;
     if (s > P.eps2_hi32) return false;
     ++t.band;
-    double qx[D];
+    double qx[D], px[D];
 #pragma unroll
-    for (int k = 0; k < D; ++k) qx[k] = X[k * n + q];
+    for (int k = 0; k < D; ++k) {
+      qx[k] = X[k * n + q];
+      px[k] = X[k * n + si];
+    }
     ++t.t64;
-    double d2 = dist2_f64<D>(sx, qx);
-    return stage_is_centre ? pred_from_d2<D>(d2, sx, qx, P) : pred_from_d2<D>(d2, qx, sx, P);
+    double d2 = dist2_f64<D>(px, qx);
+    return stage_is_centre ? pred_from_d2<D>(d2, px, qx, P) : pred_from_d2<D>(d2, qx, px, P);
   } else {
     ++t.t64;
     double d2 = dist2_f64<D>(sx, c.x);
@@ -875,19 +881,27 @@ __device__ __forceinline__ bool link_test(const double* sx, const float* sf, con
                                           const double* __restrict__ X, int64_t n, int a, int q,
                                           const PP& P, Tally& t,
                                           int* __restrict__ asym_list, unsigned long long* ctr) {
-  double qx[D];
+  double qx[D], ax[D];
   if (F32) {
     ++t.t32;
     float s = dist2_f32<D>(sf, c.f);
     if (s < P.eps2_lo32) return true;
     if (s > P.eps2_hi32) return false;
     ++t.band;
+    // float64 coordinates of both, for the band re-test only
 #pragma unroll
-    for (int k = 0; k < D; ++k) qx[k] = X[k * n + q];
+    for (int k = 0; k < D; ++k) {
+      qx[k] = X[k * n + q];
+      ax[k] = X[k * n + a];
+    }
   } else {
 #pragma unroll
-    for (int k = 0; k < D; ++k) qx[k] = c.x[k];
+    for (int k = 0; k < D; ++k) {
+      qx[k] = c.x[k];
+      ax[k] = sx[k];
+    }
   }
+  sx = ax;
   ++t.t64;
   double d2 = dist2_f64<D>(sx, qx);
   if (d2 <= P.eps2_in) return true;
@@ -1377,9 +1391,11 @@ __device__ __forceinline__ void heavy_push(const gdl::Bufs& B, int slot, bool pu
 template <int D, bool F32>
 __device__ __forceinline__ void load_point(double* x, float* f, const gdl::Bufs& B, int64_t n,
                                            int64_t i, bool prune) {
+  // float32-band mode tests from the float32 copy; the float64 coordinates
+  // are loaded by the band re-test itself
 #pragma unroll
   for (int k = 0; k < D; ++k) {
-    x[k] = B.X[k * n + i];
+    if (!F32) x[k] = B.X[k * n + i];
     if (F32 || prune) f[k] = B.Xf[k * n + i];
   }
 }
@@ -1582,7 +1598,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
             }
             Cand<D, F32> cd;
             load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
-            cnt += pair_test<D, F32>(px, pf, cd, B.X, n, qq, true, Q, t) ? 1 : 0;
+            cnt += pair_test<D, F32>(px, pf, cd, B.X, n, qq, i, true, Q, t) ? 1 : 0;
           }
         };
         auto flush = [&](void) {
@@ -1726,7 +1742,8 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
               if (qq >= 0) {
                 Cand<D, F32> cd;
                 load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
-                if (pair_test<D, F32>(S.x[ow], S.f[ow], cd, B.X, n, qq, true, Qo, t))
+                // (float64 mode only: the owner's coordinates are staged, no index needed)
+                if (pair_test<D, F32>(S.x[ow], S.f[ow], cd, B.X, n, qq, 0, true, Qo, t))
                   atomicAdd(&S.cnt[ow], 1);
               }
             }
@@ -2051,7 +2068,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
                 }
                 Cand<D, F32> cd;
                 load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
-                if (pair_test<D, F32>(px, pf, cd, B.X, n, qq, false, Q, t)) {
+                if (pair_test<D, F32>(px, pf, cd, B.X, n, qq, i, false, Q, t)) {
                   best = cB;
                   break;
                 }
@@ -2083,7 +2100,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
               }
               Cand<D, F32> cd;
               load_cand<D, F32>(cd, B.X, B.Xf, n, qq);
-              if (pair_test<D, F32>(px, pf, cd, B.X, n, qq, false, Q, t)) {
+              if (pair_test<D, F32>(px, pf, cd, B.X, n, qq, i, false, Q, t)) {
                 best = cB;
                 break;
               }
@@ -2175,7 +2192,7 @@ __global__ void __launch_bounds__(kCellThreads) k_core_heavy(const gdl::Bufs B, 
       if (lane < na) {
 #pragma unroll
         for (int k = 0; k < D; ++k) {
-          S.x[lane][k] = X[k * n + b + c0 + lane];
+          if (!F32) S.x[lane][k] = X[k * n + b + c0 + lane];
           if (F32) S.f[lane][k] = Xf[k * n + b + c0 + lane];
         }
       }
@@ -2192,7 +2209,7 @@ __global__ void __launch_bounds__(kCellThreads) k_core_heavy(const gdl::Bufs B, 
           load_cand<D, F32>(cd, X, Xf, n, q);
         }
         for (int j = 0; j < na; ++j) {
-          bool hit = valid && pair_test<D, F32>(S.x[j], S.f[j], cd, X, n, q, true, Q, t);
+          bool hit = valid && pair_test<D, F32>(S.x[j], S.f[j], cd, X, n, q, b + c0 + j, true, Q, t);
           unsigned bal = __ballot_sync(kFull, hit);
           if (lane == j) mycnt += __popc(bal);
         }
@@ -2310,7 +2327,7 @@ __global__ void __launch_bounds__(kCellThreads) k_union_heavy(const gdl::Bufs B,
             float af[D];
 #pragma unroll
             for (int k = 0; k < D; ++k) {
-              ax[k] = X[k * n + a];
+              if (!F32) ax[k] = X[k * n + a];
               if (F32) af[k] = Xf[k * n + a];
             }
             bool hit = valid && link_test<D, F32>(ax, af, c, X, n, a, q, Q, t, B.asym, B.ctr);
@@ -2499,7 +2516,7 @@ __global__ void __launch_bounds__(kCellThreads) k_border_heavy(const gdl::Bufs B
         sIdx[w][slot] = i;
 #pragma unroll
         for (int k = 0; k < D; ++k) {
-          S.x[slot][k] = X[k * n + i];
+          if (!F32) S.x[slot][k] = X[k * n + i];
           if (F32) S.f[slot][k] = Xf[k * n + i];
         }
       }
@@ -2538,7 +2555,7 @@ __global__ void __launch_bounds__(kCellThreads) k_border_heavy(const gdl::Bufs B
             while (pending) {
               const int j = __ffs(pending) - 1;
               pending &= pending - 1;
-              bool hit = valid && pair_test<D, F32>(S.x[j], S.f[j], c, X, n, q, false, Q, t);
+              bool hit = valid && pair_test<D, F32>(S.x[j], S.f[j], c, X, n, q, sIdx[w][j], false, Q, t);
               if (__any_sync(kFull, hit)) {
                 if (lane == j) best = cB;
                 wantm &= ~(1u << j);
