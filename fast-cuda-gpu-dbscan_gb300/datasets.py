@@ -129,7 +129,9 @@ def aniso3d_20m(seed: int = 0, scale: float = 1.0) -> Instance:
     centres = rng.uniform(0.0, side, size=(64, 3))
     parts = []
     for i in range(64):
-        sig = rng.uniform(0.02, 0.5, size=3)
+        # axis sigmas shrink with the domain, so a scaled-down set keeps the
+        # blob densities (and neighbour counts) of the full-size one
+        sig = rng.uniform(0.02, 0.5, size=3) * scale ** (1.0 / 3.0)
         rot = _random_rotation(rng)
         z = rng.standard_normal((int(sizes[i]), 3)) * sig
         parts.append(centres[i] + z @ rot.T)
