@@ -567,18 +567,22 @@ __device__ __forceinline__ void load_coords(const double* __restrict__ src, doub
 }
 
 // Sorted structure-of-arrays copy (+ centred float32 copy).  ONE: a single
-// instance (its parameters are Pv[0], no key is read).  Two points per thread
-// and pass, so that two random loads are in flight.
+// instance (its parameters are Pv[0], no key is read).  kGatherU points per
+// thread and pass, so that as many random loads are in flight.
+#ifndef GD_GATHER_U
+#define GD_GATHER_U 4
+#endif
+constexpr int kGatherU = GD_GATHER_U;
 template <class Key, bool XF, bool ONE>
 __global__ void k_gather(const gdl::Bufs B, int64_t n) {
   const int LB = B.Bi->LB;
   const Key* __restrict__ keys = static_cast<const Key*>(B.keys);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < n; i0 += 2 * stride) {
-    double v[2][3];
-    const DevParams* Pp[2];
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i0 < n; i0 += kGatherU * stride) {
+    double v[kGatherU][3];
+    const DevParams* Pp[kGatherU];
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
+    for (int u = 0; u < kGatherU; ++u) {
       const int64_t i = i0 + u * stride;
       Pp[u] = nullptr;
       if (i < n) {
@@ -591,7 +595,7 @@ __global__ void k_gather(const gdl::Bufs B, int64_t n) {
       }
     }
 #pragma unroll
-    for (int u = 0; u < 2; ++u) {
+    for (int u = 0; u < kGatherU; ++u) {
       const int64_t i = i0 + u * stride;
       if (i >= n) continue;
       const DevParams& P = *Pp[u];
@@ -1482,31 +1486,47 @@ __global__ void k_core_split(const gdl::Bufs B, int64_t n) {
   const int LB = B.Bi->LB;
   const int lane = threadIdx.x & 31;
   unsigned long long dense = 0;
-  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); i0 < n;
-       i0 += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = i0 + lane;
-    bool dn = false;
-    int m = 0;
-    if (i < n) {
-      m = cell_of(B, i);
-      const int b = B.reps[m];
-      const int sz = B.reps[m + 1] - b;
-      dn = sz >= B.Pv[ONE ? 0 : (int)(key_at<KEY64>(B, i) >> LB)].minpts;
+  // two groups of 32 points per warp and pass, their loads issued together
+  constexpr int U = 2;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t g0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); g0 < n;
+       g0 += U * stride) {
+    int m[U], b[U], e[U], mp[U];
+    uint32_t id[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = g0 + u * stride + lane;
+      const int64_t ic = i < n ? i : n - 1;
+      m[u] = cell_of(B, ic);
+      id[u] = B.ids[ic];
+      mp[u] = B.Pv[ONE ? 0 : (int)(key_at<KEY64>(B, ic) >> LB)].minpts;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      b[u] = B.reps[m[u]];
+      e[u] = B.reps[m[u] + 1];
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i0 = g0 + u * stride;
+      if (i0 >= n) break;  // warp-uniform
+      const int64_t i = i0 + lane;
+      const bool dn = i < n && e[u] - b[u] >= mp[u];
       if (dn) {
         B.core[i] = 1;
-        if (i == b) ++dense;
+        if (i == b[u]) ++dense;
       }
-    }
-    // the walk list: every point outside a dense cell
-    const unsigned wl = __ballot_sync(kFull, i < n && !dn);
-    if (lane == 0) B.lbits[i0 >> 5] = wl;
-    const unsigned cm = __ballot_sync(kFull, dn);
-    const unsigned grp = run_peers(cm, m);
-    if (dn) {
-      const unsigned mn = __reduce_min_sync(grp, (unsigned)B.ids[i]);
-      if (lane == __ffs(grp) - 1) {
-        atomicAdd(B.cellcore + m, __popc(grp));
-        atomicMin(reinterpret_cast<unsigned*>(B.cellmin) + m, mn);
+      // the walk list: every point outside a dense cell
+      const unsigned wl = __ballot_sync(kFull, i < n && !dn);
+      if (lane == 0) B.lbits[i0 >> 5] = wl;
+      const unsigned cm = __ballot_sync(kFull, dn);
+      const unsigned grp = run_peers(cm, m[u]);
+      if (dn) {
+        const unsigned mn = __reduce_min_sync(grp, id[u]);
+        if (lane == __ffs(grp) - 1) {
+          atomicAdd(B.cellcore + m[u], __popc(grp));
+          atomicMin(reinterpret_cast<unsigned*>(B.cellmin) + m[u], mn);
+        }
       }
     }
   }
