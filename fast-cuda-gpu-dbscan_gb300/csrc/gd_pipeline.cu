@@ -768,7 +768,7 @@ __global__ void k_row_hash(const gdl::Bufs B) {
 // ------------------------------------------------------------- cell helpers
 template <int D>
 struct CellXYZ {
-  int64_t c[3];
+  int c[3];  // per-axis cell indices (each below 2^31)
 };
 
 template <int D>
@@ -777,14 +777,14 @@ __device__ __forceinline__ CellXYZ<D> decompose(uint64_t key, const DevParams& P
   uint64_t k = key;
   if (D == 3) {
     const uint64_t k2 = udiv_by(k, P.dm[1], P.ds[1]);
-    r.c[2] = (int64_t)(k - k2 * (uint64_t)P.G[2]);
+    r.c[2] = (int)(k - k2 * (uint64_t)P.G[2]);
     k = k2;
   } else {
     r.c[2] = 0;
   }
   const uint64_t k1 = udiv_by(k, P.dm[0], P.ds[0]);
-  r.c[1] = (int64_t)(k - k1 * (uint64_t)P.G[1]);
-  r.c[0] = (int64_t)k1;
+  r.c[1] = (int)(k - k1 * (uint64_t)P.G[1]);
+  r.c[0] = (int)k1;
   return r;
 }
 
@@ -792,11 +792,11 @@ __device__ __forceinline__ CellXYZ<D> decompose(uint64_t key, const DevParams& P
 template <int D>
 __device__ __forceinline__ int64_t offset_key(const CellXYZ<D>& c, int ox, int oy, int oz,
                                               const DevParams& P) {
-  int64_t x = c.c[0] + ox, y = c.c[1] + oy;
+  int64_t x = (int64_t)c.c[0] + ox, y = (int64_t)c.c[1] + oy;
   if (x < 0 || x >= P.G[0] || y < 0 || y >= P.G[1]) return -1;
   int64_t k = x * P.G[1] + y;
   if (D == 3) {
-    int64_t z = c.c[2] + oz;
+    int64_t z = (int64_t)c.c[2] + oz;
     if (z < 0 || z >= P.G[2]) return -1;
     k = k * P.G[2] + z;
   }
@@ -975,18 +975,11 @@ __device__ __forceinline__ unsigned run_peers(unsigned act, int v) {
 // empty cells without touching the table).  Sparse grids: a hash of the
 // occupied rows (all cells sharing every coordinate but the last) gives the
 // row's point range, and a binary search on the sorted keys the cells inside
-// it.  The probe loop is bounded by the table size.
+// it.  The probe loop is bounded by the table size.  The view holds only the
+// instance's scalars; the tables' addresses are read from the kernel's
+// parameter block at each use (B is always the kernel parameter), so they
+// occupy no registers in the walks.
 struct GridView {
-  const uint32_t* start;
-  const uint32_t* cellz;   // per cell: last-axis coordinate
-  const uint32_t* occ;
-  const uint32_t* cocc;    // core occupancy (valid in the border search only)
-  const uint32_t* wpre;
-  const unsigned long long* hkeys;
-  const uint32_t* hvals;   // per slot: row begin, row end
-  const int* reps;
-  const void* keys;
-  uint32_t hmask;
   int sparse;              // DevParams::sparse
   int key64;
   uint64_t occ_off;
@@ -997,47 +990,48 @@ struct GridView {
   uint64_t glm;            // division by Gl (udiv_by)
   int32_t gls;
 
-  __device__ __forceinline__ uint64_t gkey(int64_t i) const {
-    return key64 ? static_cast<const unsigned long long*>(keys)[i]
-                 : (uint64_t) static_cast<const uint32_t*>(keys)[i];
+  __device__ __forceinline__ uint64_t gkey(const gdl::Bufs& B, int64_t i) const {
+    return key64 ? static_cast<const unsigned long long*>(B.keys)[i]
+                 : (uint64_t) static_cast<const uint32_t*>(B.keys)[i];
   }
   // cell table: index into reps of the first non-empty cell at or after
   // local key k (its rank among the occupied cells)
-  __device__ __forceinline__ int64_t rank(uint64_t k) const {
+  __device__ __forceinline__ int64_t rank(const gdl::Bufs& B, uint64_t k) const {
     const uint64_t idx = occ_off + k, w = idx >> 5;
-    return (int64_t)wpre[w] + __popc(occ[w] & ((1u << (idx & 31)) - 1u)) + rank_off;
+    return (int64_t)B.wpre[w] + __popc(B.occ[w] & ((1u << (idx & 31)) - 1u)) + rank_off;
   }
-  __device__ __forceinline__ bool occupied(uint64_t k) const {
+  __device__ __forceinline__ bool occupied(const gdl::Bufs& B, uint64_t k) const {
     const uint64_t idx = occ_off + k;
-    return (occ[idx >> 5] >> (idx & 31)) & 1u;
+    return (B.occ[idx >> 5] >> (idx & 31)) & 1u;
   }
   // row table: cells [begin, end) (indices into reps) of row ri
-  __device__ __forceinline__ int2 row_cells(uint64_t ri) const {
+  __device__ __forceinline__ int2 row_cells(const gdl::Bufs& B, uint64_t ri) const {
     const uint64_t idx = occ_off + ri;
-    if (!((occ[idx >> 5] >> (idx & 31)) & 1u)) return make_int2(0, 0);
-    return make_int2((int)start[start_off + ri], (int)start[start_off + ri + 1]);
+    if (!((B.occ[idx >> 5] >> (idx & 31)) & 1u)) return make_int2(0, 0);
+    return make_int2((int)B.start[start_off + ri], (int)B.start[start_off + ri + 1]);
   }
   // first cell in [b, e) (one row's cells) whose last-axis coordinate is >= z
-  __device__ __forceinline__ int zlower(int b, int e, int64_t z) const {
+  __device__ __forceinline__ int zlower(const gdl::Bufs& B, int b, int e, int64_t z) const {
     while (b < e) {
       const int mid = (int)(((unsigned)b + (unsigned)e) >> 1);
-      if ((int64_t)cellz[mid] < z) b = mid + 1;
+      if ((int64_t)B.cellz[mid] < z) b = mid + 1;
       else e = mid;
     }
     return b;
   }
   // row table: whether row ri holds a core point
-  __device__ __forceinline__ bool core_row_at(uint64_t ri) const {
+  __device__ __forceinline__ bool core_row_at(const gdl::Bufs& B, uint64_t ri) const {
     const uint64_t idx = occ_off + ri;
-    return (cocc[idx >> 5] >> (idx & 31)) & 1u;
+    return (B.cocc[idx >> 5] >> (idx & 31)) & 1u;
   }
   // hash: points [begin, end) of the row whose first cell is rowkey
-  __device__ __forceinline__ int2 row(uint64_t rowkey) const {
+  __device__ __forceinline__ int2 row(const gdl::Bufs& B, uint64_t rowkey) const {
     const unsigned long long k = hi | rowkey;
+    const uint32_t hmask = B.hmask;
     uint32_t h = hash_key(k) & hmask;
     for (uint32_t probe = 0; probe <= hmask; ++probe) {
-      const unsigned long long kk = hkeys[h];
-      if (kk == k) return make_int2((int)hvals[2 * h], (int)hvals[2 * h + 1]);
+      const unsigned long long kk = B.hkeys[h];
+      if (kk == k) return make_int2((int)B.hvals[2 * h], (int)B.hvals[2 * h + 1]);
       if (kk == kHashEmpty) break;
       h = (h + 1) & hmask;
     }
@@ -1046,76 +1040,77 @@ struct GridView {
   // cell table: occupancy bits of cells z0..z1 (at most 5) of the row whose
   // first cell is rowkey (bit z - z0), and the reps index of the first
   // occupied one (the others follow it in reps)
-  __device__ __forceinline__ uint32_t occ_cells(uint64_t rowkey, int64_t z0, int64_t z1,
-                                                int64_t& r0) const {
+  __device__ __forceinline__ uint32_t occ_cells(const gdl::Bufs& B, uint64_t rowkey, int64_t z0,
+                                                int64_t z1, int64_t& r0) const {
     const uint64_t i0 = occ_off + rowkey + (uint64_t)z0, w = i0 >> 5;
     const int len = (int)(z1 - z0) + 1;
     const int sh = (int)(i0 & 31);
-    const uint32_t lo = occ[w];
+    const uint32_t lo = B.occ[w];
     uint64_t bits = lo >> sh;
-    if (sh + len > 32) bits |= (uint64_t)occ[w + 1] << (32 - sh);
+    if (sh + len > 32) bits |= (uint64_t)B.occ[w + 1] << (32 - sh);
     const uint32_t mask = (uint32_t)bits & ((1u << len) - 1u);
-    if (mask) r0 = (int64_t)wpre[w] + __popc(lo & ((1u << sh) - 1u)) + rank_off;
+    if (mask) r0 = (int64_t)B.wpre[w] + __popc(lo & ((1u << sh) - 1u)) + rank_off;
     return mask;
   }
   // core occupancy bits of cells z0..z1 of a cell-table row (bit z - z0)
-  __device__ __forceinline__ uint32_t core_cells(uint64_t rowkey, int64_t z0, int64_t z1) const {
+  __device__ __forceinline__ uint32_t core_cells(const gdl::Bufs& B, uint64_t rowkey, int64_t z0,
+                                                 int64_t z1) const {
     const uint64_t i0 = occ_off + rowkey + (uint64_t)z0;
     const int len = (int)(z1 - z0) + 1;  // <= 5
     const uint64_t w = i0 >> 5;
     const int sh = (int)(i0 & 31);
-    uint64_t bits = cocc[w] >> sh;
-    if (sh + len > 32) bits |= (uint64_t)cocc[w + 1] << (32 - sh);
+    uint64_t bits = B.cocc[w] >> sh;
+    if (sh + len > 32) bits |= (uint64_t)B.cocc[w + 1] << (32 - sh);
     return (uint32_t)bits & ((1u << len) - 1u);
   }
   // first sorted position in [b, e) whose key is >= g
-  __device__ __forceinline__ int lower(int b, int e, uint64_t g) const {
+  __device__ __forceinline__ int lower(const gdl::Bufs& B, int b, int e, uint64_t g) const {
     while (b < e) {
       const int mid = (int)(((unsigned)b + (unsigned)e) >> 1);
-      if (gkey(mid) < g) b = mid + 1;
+      if (gkey(B, mid) < g) b = mid + 1;
       else e = mid;
     }
     return b;
   }
   // points of the cells z0..z1 of the row whose first cell is rowkey: one
   // contiguous range, because no other key sorts between them
-  __device__ __forceinline__ int2 span_row(uint64_t rowkey, int64_t z0, int64_t z1) const {
+  __device__ __forceinline__ int2 span_row(const gdl::Bufs& B, uint64_t rowkey, int64_t z0,
+                                           int64_t z1) const {
     if (!sparse)
-      return make_int2(reps[rank(rowkey + z0)], reps[rank(rowkey + z1 + 1)]);
+      return make_int2(B.reps[rank(B, rowkey + z0)], B.reps[rank(B, rowkey + z1 + 1)]);
     if (sparse == 2) {
-      const int2 rc = row_cells(udiv_by(rowkey, glm, gls));
+      const int2 rc = row_cells(B, udiv_by(rowkey, glm, gls));
       if (rc.x == rc.y) return make_int2(0, 0);
-      const int ma = zlower(rc.x, rc.y, z0), mb = zlower(ma, rc.y, z1 + 1);
-      return make_int2(reps[ma], reps[mb]);
+      const int ma = zlower(B, rc.x, rc.y, z0), mb = zlower(B, ma, rc.y, z1 + 1);
+      return make_int2(B.reps[ma], B.reps[mb]);
     }
-    const int2 r = row(rowkey);
+    const int2 r = row(B, rowkey);
     if (r.x == r.y) return r;
-    const int a = lower(r.x, r.y, hi | (rowkey + (uint64_t)z0));
-    const int b = lower(a, r.y, hi | (rowkey + (uint64_t)z1 + 1));
+    const int a = lower(B, r.x, r.y, hi | (rowkey + (uint64_t)z0));
+    const int b = lower(B, a, r.y, hi | (rowkey + (uint64_t)z1 + 1));
     return make_int2(a, b);
   }
   // points of the cell with local key k: [x, y)
-  __device__ __forceinline__ int2 cell(uint64_t k) const {
+  __device__ __forceinline__ int2 cell(const gdl::Bufs& B, uint64_t k) const {
     if (!sparse) {
-      if (!occupied(k)) return make_int2(0, 0);
-      const int64_t r = rank(k);
-      return make_int2(reps[r], reps[r + 1]);
+      if (!occupied(B, k)) return make_int2(0, 0);
+      const int64_t r = rank(B, k);
+      return make_int2(B.reps[r], B.reps[r + 1]);
     }
     const int64_t z = (int64_t)(k - udiv_by(k, glm, gls) * (uint64_t)Gl);
-    return span_row(k - (uint64_t)z, z, z);
+    return span_row(B, k - (uint64_t)z, z, z);
   }
   // points of the cells k0..k1 (consecutive local keys along one row)
-  __device__ __forceinline__ int2 span(uint64_t k0, uint64_t k1) const {
-    if (!sparse) return make_int2(reps[rank(k0)], reps[rank(k1 + 1)]);
+  __device__ __forceinline__ int2 span(const gdl::Bufs& B, uint64_t k0, uint64_t k1) const {
+    if (!sparse) return make_int2(B.reps[rank(B, k0)], B.reps[rank(B, k1 + 1)]);
     const int64_t z0 = (int64_t)(k0 - udiv_by(k0, glm, gls) * (uint64_t)Gl);
-    return span_row(k0 - (uint64_t)z0, z0, z0 + (int64_t)(k1 - k0));
+    return span_row(B, k0 - (uint64_t)z0, z0, z0 + (int64_t)(k1 - k0));
   }
 };
 
 __device__ __forceinline__ GridView view_of(const gdl::Bufs& B, const DevParams& P) {
   const int a = P.dim - 2;
-  return GridView{B.start, B.cellz, B.occ, B.cocc, B.wpre, B.hkeys, B.hvals, B.reps, B.keys, B.hmask,
-                  P.sparse, B.Bi->key64, P.occ_off, P.start_off, P.rank_off,
+  return GridView{P.sparse, B.Bi->key64, P.occ_off, P.start_off, P.rank_off,
                   (uint64_t)P.inst << P.LB, P.G[P.dim - 1], P.dm[a], P.ds[a]};
 }
 
@@ -1216,7 +1211,8 @@ struct RowList {
 };
 
 template <int D>
-__device__ __forceinline__ int build_rows(RowList& RL, const GridView& gv, const CellXYZ<D>& cc,
+__device__ __forceinline__ int build_rows(const gdl::Bufs& B, RowList& RL, const GridView& gv,
+                                          const CellXYZ<D>& cc,
                                           const DevParams& P, int lane) {
   const OffTab& T = kRows[D - 2];
   const int64_t Gl = P.G[D - 1];
@@ -1228,7 +1224,7 @@ __device__ __forceinline__ int build_rows(RowList& RL, const GridView& gv, const
     int64_t rowkey = offset_key<D>(cc, T.o[lane][0], T.o[lane][1], 0, P);
     if (rowkey >= 0) {
       rowkey -= cl;
-      const int2 rg = gv.span((uint64_t)(rowkey + l0), (uint64_t)(rowkey + l1));
+      const int2 rg = gv.span(B, (uint64_t)(rowkey + l0), (uint64_t)(rowkey + l1));
       lo = rg.x;
       len = rg.y - rg.x;
     }
@@ -1409,13 +1405,13 @@ __device__ __forceinline__ void load_point(double* x, float* f, const gdl::Bufs&
 template <int D>
 struct RowWalk {
   CellXYZ<D> cc;
-  int64_t cl, l0, l1;
+  int cl, l0, l1;  // the cell's last-axis index and the stencil's range on that axis
   __device__ __forceinline__ void init(const CellXYZ<D>& c, const DevParams& P) {
     cc = c;
     const int64_t Gl = P.G[D - 1];
     cl = c.c[D - 1];
     l0 = cl - 2 < 0 ? 0 : cl - 2;
-    l1 = cl + 2 >= Gl ? Gl - 1 : cl + 2;
+    l1 = (int64_t)cl + 2 >= Gl ? (int)(Gl - 1) : cl + 2;
   }
   // local key of row r's first cell, or -1 when the row is outside the grid
   __device__ __forceinline__ int64_t rowkey(const OffTab& T, int r, const DevParams& P) const {
@@ -1425,10 +1421,10 @@ struct RowWalk {
   // index of row r among the grid's rows (its first cell's key is index * G[D-1]),
   // or -1 when the row is outside the grid
   __device__ __forceinline__ int64_t rowidx(const OffTab& T, int r, const DevParams& P) const {
-    const int64_t x = cc.c[0] + T.o[r][0];
+    const int64_t x = (int64_t)cc.c[0] + T.o[r][0];
     if (x < 0 || x >= P.G[0]) return -1;
     if (D == 2) return x;
-    const int64_t y = cc.c[1] + T.o[r][1];
+    const int64_t y = (int64_t)cc.c[1] + T.o[r][1];
     if (y < 0 || y >= P.G[1]) return -1;
     return x * P.G[1] + y;
   }
@@ -1668,7 +1664,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
           if (gv.sparse == 0) {
             // cell table: the row's occupied cells from its occupancy bits
             int64_t rr = 0;
-            uint32_t mask = gv.occ_cells((uint64_t)rk, rw.l0, rw.l1, rr);
+            uint32_t mask = gv.occ_cells(B, (uint64_t)rk, rw.l0, rw.l1, rr);
             while (mask && cnt < Q.minpts && !over) {
               const int z = __ffs(mask) - 1;
               mask &= mask - 1;
@@ -1679,10 +1675,10 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
           }
           if (gv.sparse == 2) {
             // row table: the row's cells from the first at or after l0 to l1
-            const int2 rc = gv.row_cells((uint64_t)ri);
-            for (int mq = gv.zlower(rc.x, rc.y, rw.l0); mq < rc.y && cnt < Q.minpts && !over;
+            const int2 rc = gv.row_cells(B, (uint64_t)ri);
+            for (int mq = gv.zlower(B, rc.x, rc.y, rw.l0); mq < rc.y && cnt < Q.minpts && !over;
                  ++mq) {
-              const int64_t z = gv.cellz[mq];
+              const int64_t z = B.cellz[mq];
               if (z > rw.l1) break;
               visit(B.reps[mq], B.reps[mq + 1], (int)(z - rw.cl));
             }
@@ -1690,10 +1686,10 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
           }
           // hash: the row's points, from the first cell at or after l0 to the
           // first beyond l1
-          const int2 rp = gv.row((uint64_t)rk);
+          const int2 rp = gv.row(B, (uint64_t)rk);
           if (rp.x == rp.y) continue;
           const int dmax = (int)(rw.l1 - rw.cl);
-          for (int q = gv.lower(rp.x, rp.y, gv.hi | ((uint64_t)rk + (uint64_t)rw.l0));
+          for (int q = gv.lower(B, rp.x, rp.y, gv.hi | ((uint64_t)rk + (uint64_t)rw.l0));
                q < rp.y && cnt < Q.minpts && !over;) {
             const int d = (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
             if (d > dmax) break;
@@ -1905,15 +1901,15 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
           int64_t z0, z1;
           if (pass == 0) {
             if (seg) break;
-            z0 = own ? rw.cl + 1 : rw.cl - 1;
-            z1 = rw.cl + 1;
+            z0 = own ? (int64_t)rw.cl + 1 : (int64_t)rw.cl - 1;
+            z1 = (int64_t)rw.cl + 1;
           } else if (near_row) {
-            z0 = z1 = seg ? rw.cl + 2 : rw.cl - 2;
+            z0 = z1 = seg ? (int64_t)rw.cl + 2 : (int64_t)rw.cl - 2;
             if (own && !seg) continue;
           } else {
             if (seg) break;
-            z0 = rw.cl - 2;
-            z1 = rw.cl + 2;
+            z0 = (int64_t)rw.cl - 2;
+            z1 = (int64_t)rw.cl + 2;
           }
           z0 = z0 < rw.l0 ? rw.l0 : z0;
           z1 = z1 > rw.l1 ? rw.l1 : z1;
@@ -1949,8 +1945,8 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
             // core occupancy bits (a cell's index into reps: the rank of the
             // first occupied one plus the occupied cells before it)
             int64_t rr = 0;
-            const uint32_t mask = gv.occ_cells((uint64_t)rk, z0, z1, rr);
-            uint32_t cm = mask ? mask & gv.core_cells((uint64_t)rk, z0, z1) : 0u;
+            const uint32_t mask = gv.occ_cells(B, (uint64_t)rk, z0, z1, rr);
+            uint32_t cm = mask ? mask & gv.core_cells(B, (uint64_t)rk, z0, z1) : 0u;
             while (cm) {
               const int z = __ffs(cm) - 1;
               cm &= cm - 1;
@@ -1963,16 +1959,16 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
             // row table: the row's cells with last-axis coordinate in [z0, z1],
             // rows without a core point skipped
             const uint64_t ri = udiv_by((uint64_t)rk, gv.glm, gv.gls);
-            if (!gv.core_row_at(ri)) continue;
-            const int2 rc = gv.row_cells(ri);
-            for (int mq = gv.zlower(rc.x, rc.y, z0); mq < rc.y; ++mq) {
-              const int64_t z = gv.cellz[mq];
+            if (!gv.core_row_at(B, ri)) continue;
+            const int2 rc = gv.row_cells(B, ri);
+            for (int mq = gv.zlower(B, rc.x, rc.y, z0); mq < rc.y; ++mq) {
+              const int64_t z = B.cellz[mq];
               if (z > z1) break;
               visit(mq, (int)(z - rw.cl), false);
             }
             continue;
           }
-          const int2 sp = gv.span_row((uint64_t)rk, z0, z1);
+          const int2 sp = gv.span_row(B, (uint64_t)rk, z0, z1);
           for (int q = sp.x; q < sp.y;) {
             const int c = cell_of(B, q);
             const int qe = B.reps[c + 1];
@@ -2062,11 +2058,11 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
         const int64_t rk = ri * P.G[D - 1];  // key of the row's first cell
         if (gv.sparse == 0) {
           // cell table: visit only the cells holding a core point
-          uint32_t cm = gv.core_cells((uint64_t)rk, rw.l0, rw.l1);
+          uint32_t cm = gv.core_cells(B, (uint64_t)rk, rw.l0, rw.l1);
           while (cm && !over) {
             const int z = __ffs(cm) - 1;
             cm &= cm - 1;
-            const int64_t rq = gv.rank((uint64_t)rk + (uint64_t)(rw.l0 + z));
+            const int64_t rq = gv.rank(B, (uint64_t)rk + (uint64_t)(rw.l0 + z));
             const int cB = B.cellcid[rq];
             if (cB >= best) continue;
             int cls = 0;
@@ -2079,7 +2075,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
             if (cls > 0) {
               best = cB;
             } else if (cls == 0) {
-              const int q = gv.reps[rq], qe = gv.reps[rq + 1];
+              const int q = B.reps[rq], qe = B.reps[rq + 1];
               for (int qq = q; qq < qe; ++qq) {
                 if (!B.core[qq]) continue;
                 if (budget-- == 0) {
@@ -2097,7 +2093,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
           }
           continue;
         }
-        if (gv.sparse == 2 && !gv.core_row_at((uint64_t)ri)) continue;
+        if (gv.sparse == 2 && !gv.core_row_at(B, (uint64_t)ri)) continue;
         // one non-empty cell (index c, points [q, qe)) at last-axis offset d;
         // cells without core points have cluster id INT_MAX
         auto visitb = [&](int c, int q, int qe, int d) {
@@ -2129,19 +2125,19 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
         };
         if (gv.sparse == 2) {
           // row table: the row's cells from the first at or after l0 to l1
-          const int2 rc = gv.row_cells((uint64_t)ri);
-          for (int mq = gv.zlower(rc.x, rc.y, rw.l0); mq < rc.y && !over; ++mq) {
-            const int64_t z = gv.cellz[mq];
+          const int2 rc = gv.row_cells(B, (uint64_t)ri);
+          for (int mq = gv.zlower(B, rc.x, rc.y, rw.l0); mq < rc.y && !over; ++mq) {
+            const int64_t z = B.cellz[mq];
             if (z > rw.l1) break;
             visitb(mq, B.reps[mq], B.reps[mq + 1], (int)(z - rw.cl));
           }
           continue;
         }
         // hash: the row's points from the first cell at or after l0
-        const int2 rp = gv.row((uint64_t)rk);
+        const int2 rp = gv.row(B, (uint64_t)rk);
         if (rp.x == rp.y) continue;
         const int dmax = (int)(rw.l1 - rw.cl);
-        for (int q = gv.lower(rp.x, rp.y, gv.hi | ((uint64_t)rk + (uint64_t)rw.l0));
+        for (int q = gv.lower(B, rp.x, rp.y, gv.hi | ((uint64_t)rk + (uint64_t)rw.l0));
              q < rp.y && !over;) {
           const int d = (int)((int64_t)((key_at<KEY64>(B, q) & P.kmask) - (uint64_t)rk) - rw.cl);
           if (d > dmax) break;
@@ -2205,7 +2201,7 @@ __global__ void __launch_bounds__(kCellThreads) k_core_heavy(const gdl::Bufs B, 
     }
     const GridView gv = view_of(B, P);
     const CellXYZ<D> cc = decompose<D>(cx.local, P);
-    const int total = build_rows<D>(RL, gv, cc, P, lane);
+    const int total = build_rows<D>(B, RL, gv, cc, P, lane);
     int ncore = 0, mn = INT_MAX;
     for (int c0 = 0; c0 < sz; c0 += 32) {
       const int na = min(32, sz - c0);
@@ -2318,7 +2314,7 @@ __global__ void __launch_bounds__(kCellThreads) k_union_heavy(const gdl::Bufs B,
       if (tt < T.n && ((open >> tt) & 1ull)) {
         const int64_t kb = offset_key<D>(cc, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
         if (kb >= 0) {
-          const int2 cb = gv.cell((uint64_t)kb);
+          const int2 cb = gv.cell(B, (uint64_t)kb);
           bB = cb.x;
           eB = cb.y;
           if (bB < eB) {
@@ -2549,7 +2545,7 @@ __global__ void __launch_bounds__(kCellThreads) k_border_heavy(const gdl::Bufs B
         if (tt < T.n) {
           const int64_t kb = offset_key<D>(cc, T.o[tt][0], T.o[tt][1], T.o[tt][2], P);
           if (kb >= 0) {
-            const int2 cb = gv.cell((uint64_t)kb);
+            const int2 cb = gv.cell(B, (uint64_t)kb);
             bB = cb.x;
             eB = cb.y;
             if (bB < eB) {
