@@ -631,14 +631,28 @@ __device__ __forceinline__ int cell_of(const gdl::Bufs& B, int64_t i) {
 template <class Key>
 __global__ void k_run_bits(const Key* __restrict__ keys, int64_t n, uint32_t* __restrict__ bits) {
   const int lane = threadIdx.x & 31;
-  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); i0 < n;
-       i0 += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = i0 + lane;
-    const Key k = i < n ? keys[i] : (Key)0;
-    Key prev = __shfl_up_sync(kFull, k, 1);
-    if (lane == 0 && i > 0) prev = keys[i - 1];
-    const unsigned b = __ballot_sync(kFull, i < n && (i == 0 || k != prev));
-    if (lane == 0) bits[i0 >> 5] = b;
+  // four groups of 32 positions per warp and pass, their loads issued together
+  constexpr int U = 4;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t g0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); g0 < n;
+       g0 += U * stride) {
+    Key k[U], p[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = g0 + u * stride + lane;
+      k[u] = i < n ? keys[i] : (Key)0;
+      p[u] = lane == 0 && i > 0 && i <= n ? keys[i - 1] : (Key)0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i0 = g0 + u * stride;
+      if (i0 >= n) break;  // warp-uniform
+      const int64_t i = i0 + lane;
+      Key prev = __shfl_up_sync(kFull, k[u], 1);
+      if (lane == 0) prev = p[u];
+      const unsigned b = __ballot_sync(kFull, i < n && (i == 0 || k[u] != prev));
+      if (lane == 0) bits[i0 >> 5] = b;
+    }
   }
 }
 
@@ -2255,7 +2269,8 @@ __global__ void k_parent_init(const gdl::Bufs B, int64_t n) {
   const int64_t M = *B.M;
   const int lane = threadIdx.x & 31;
   const int LB = B.Bi->LB;
-  for (int64_t m0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); m0 < n;
+  // words of the mask beyond the cells are cleared before the launch
+  for (int64_t m0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); m0 < M;
        m0 += (int64_t)gridDim.x * blockDim.x) {
     const int64_t m = m0 + lane;
     bool f = false;
@@ -2482,11 +2497,24 @@ __global__ void k_cell_ids(const gdl::Bufs B) {
 // instances' first), a word per warp.
 __global__ void k_label(const gdl::Bufs B, int64_t n) {
   const int lane = threadIdx.x & 31;
-  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); i0 < n;
-       i0 += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = i0 + lane;
-    const unsigned nc = __ballot_sync(kFull, i < n && !B.core[i]);
-    if (lane == 0) B.lbits[i0 >> 5] = nc;
+  // four groups of 32 points per warp and pass, their loads issued together
+  constexpr int U = 4;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t g0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); g0 < n;
+       g0 += U * stride) {
+    uint8_t c[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i = g0 + u * stride + lane;
+      c[u] = i < n ? B.core[i] : (uint8_t)1;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t i0 = g0 + u * stride;
+      if (i0 >= n) break;  // warp-uniform
+      const unsigned nc = __ballot_sync(kFull, !c[u]);
+      if (lane == 0) B.lbits[i0 >> 5] = nc;
+    }
   }
 }
 
@@ -2793,6 +2821,7 @@ int core(const Bufs& B, int64_t n, int dims, bool f32, bool key64, bool one, int
 int unite(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, void* scan_temp,
           cudaStream_t s) {
   if (B.occ_words) cudaMemsetAsync(B.cocc, 0, B.occ_words * 4, s);
+  cudaMemsetAsync(B.lbits, 0, (size_t)B.nw * 4, s);
   if (key64) k_parent_init<true><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
   else k_parent_init<false><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B, n);
   int L = 1 + list_bits(B, n, sms, scan_temp, s);
