@@ -12,6 +12,14 @@
                   (test-results/cluster-check.cpp) into the executable
                   oracle/_ref/ref_cluster_check through ref_check_harness.cpp.
                   Skipped (returns None) when the checkout is absent.
+  build_ref_multicore() compiles the reference's multicore CPU DBSCAN
+                  (multicore-cpu/) into oracle/_ref/libref_multicore.so through
+                  ref_multicore_harness.cpp, for timing only.  Skipped (returns
+                  None) when the checkout is absent.
+
+REF_ROOT is where the reference checkout lies on the machine that builds these
+checkers (GD_REFERENCE_ROOT overrides it); this recipe reads the reference's
+sources there and copies none of them.
 """
 from __future__ import annotations
 
@@ -25,6 +33,7 @@ REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD_DIR, "libgd_oracle.so")
 REF_RTREE_SO = os.path.join(REF_DIR, "libref_rtree.so")
 REF_CHECK_EXE = os.path.join(REF_DIR, "ref_cluster_check")
+REF_MULTICORE_SO = os.path.join(REF_DIR, "libref_multicore.so")
 REF_ROOT = os.environ.get("GD_REFERENCE_ROOT", "/root/reference")
 
 _COMMON = ["-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off"]
@@ -81,7 +90,29 @@ def build_ref_check(force: bool = False) -> str | None:
     return REF_CHECK_EXE
 
 
+def build_ref_multicore(force: bool = False) -> str | None:
+    """The reference's multicore CPU DBSCAN (multicore-cpu/dbscan.cpp, report.c,
+    read_dataset.c) into oracle/_ref/libref_multicore.so through
+    ref_multicore_harness.cpp; None when the checkout is absent."""
+    src_dir = os.path.join(REF_ROOT, "multicore-cpu")
+    srcs = [os.path.join(src_dir, f) for f in ("dbscan.cpp", "report.c", "read_dataset.c")]
+    if not all(os.path.exists(s) for s in srcs):
+        return None
+    harness = os.path.join(HERE, "ref_multicore_harness.cpp")
+    if not force and _newer(REF_MULTICORE_SO, [harness, *srcs]):
+        return REF_MULTICORE_SO
+    os.makedirs(REF_DIR, exist_ok=True)
+    tmp = REF_MULTICORE_SO + f".tmp{os.getpid()}"
+    # the two .c files are C++ (they include <fstream>)
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-w", "-I", src_dir,
+           harness, "-x", "c++", srcs[1], srcs[2], "-o", tmp]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, REF_MULTICORE_SO)
+    return REF_MULTICORE_SO
+
+
 if __name__ == "__main__":
     print(build_oracle(force="-f" in sys.argv))
     print(build_ref(force="-f" in sys.argv))
     print(build_ref_check(force="-f" in sys.argv))
+    print(build_ref_multicore(force="-f" in sys.argv))

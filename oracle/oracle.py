@@ -79,3 +79,28 @@ def ref_rtree_dbscan(points: np.ndarray, eps: float, minpts: int):
     k = _ref.gd_ref_rtree_dbscan(pts.ctypes.data, n, float(eps), int(minpts), raw.ctypes.data)
     lab = np.where(raw == -1, -2, raw - 1).astype(np.int32)
     return lab, int(k)
+
+
+_mc = None
+
+
+def ref_multicore_dbscan(points: np.ndarray, eps: float, minpts: int, threads: int = 16) -> int:
+    """The reference's multicore CPU DBSCAN (2D, O(n^2) brute force, float32
+    sqrt test, self excluded from the count) on these points; returns the
+    number of clusters it reports.  For timing: its semantics differ from the
+    exact DBSCAN, so its clusters are not compared with anything."""
+    global _mc
+    if _mc is None:
+        path = (_build.REF_MULTICORE_SO if os.path.exists(_build.REF_MULTICORE_SO)
+                else _build.build_ref_multicore())
+        if path is None:
+            raise RuntimeError("reference multicore build unavailable")
+        lib = ctypes.CDLL(path)
+        lib.gd_ref_multicore_dbscan.restype = ctypes.c_int
+        lib.gd_ref_multicore_dbscan.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
+                                                ctypes.c_int, ctypes.c_int]
+        _mc = lib
+    pts = np.ascontiguousarray(points, dtype=np.float64)
+    assert pts.shape[1] == 2, "the reference multicore DBSCAN is 2D only"
+    return int(_mc.gd_ref_multicore_dbscan(pts.ctypes.data, pts.shape[0], float(eps),
+                                           int(minpts), int(threads)))

@@ -71,3 +71,18 @@ def test_oracle_vs_live_reference(oracle):
         lab, _, _ = oracle.oracle_dbscan(pts, eps, mp)
         ref, _ = oracle.ref_rtree_dbscan(pts, eps, mp)
         assert np.array_equal(lab, ref)
+
+
+def test_reference_multicore_baseline_runs(oracle):
+    """The reference's multicore CPU DBSCAN (a timed baseline only: it counts
+    neighbours without the point itself and tests float32 sqrt(d2) <= eps, so
+    its clusters are not compared with the exact ones) builds from the checkout
+    and gives the same cluster count on repeated runs and thread counts."""
+    from oracle import build as obuild
+    if obuild.build_ref_multicore() is None:
+        pytest.skip("reference checkout not present")
+    rng = np.random.default_rng(5)
+    pts = np.concatenate([rng.normal(c, 0.3, (400, 2)) for c in ((0, 0), (5, 5), (0, 5))])
+    k1 = oracle.ref_multicore_dbscan(pts, 0.3, 5, threads=1)
+    k4 = oracle.ref_multicore_dbscan(pts, 0.3, 5, threads=4)
+    assert k1 == k4 >= 3
