@@ -132,6 +132,16 @@ struct gd_ctx {
     return GD_OK;
   }
 
+  // ensure() for temp memory that must be zero when first used (the scan and
+  // sort state): cleared on the stream whenever it is (re)allocated
+  gd_status ensure_zeroed(DevBuf& b, size_t bytes, const char* what) {
+    void* before = b.p;
+    const size_t had = b.bytes;
+    GD_TRY(ensure(b, bytes, what));
+    if (b.p != before || b.bytes != had) GD_CUDA(cudaMemsetAsync(b.p, 0, b.bytes, stream), what);
+    return GD_OK;
+  }
+
   void free_all(bool keep_small) {
     DevBuf* a[] = {&coords, &inst,   &chunks,   &Pv,      &Bi,     &bbox,     &keys0,
                    &keys1,  &vals0,  &vals1,    &X,       &Xf,     &table,    &occ, &cellz, &hkeys,
@@ -278,11 +288,11 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
   GD_TRY(ctx->ensure(ctx->reps, (n + 1) * 4, "cell reps"));
   GD_TRY(ctx->ensure(ctx->cellz, n * 4, "cell coordinates"));
   GD_TRY(ctx->ensure(ctx->bits, gdl::bit_layout(n).words * 4, "bit masks"));
-  GD_TRY(ctx->ensure(ctx->sorttemp, gdprim::sort_temp_bytes(n), "sort temp"));
+  GD_TRY(ctx->ensure_zeroed(ctx->sorttemp, gdprim::sort_temp_bytes(n), "sort temp"));
   size_t sc = std::max({gdprim::scan_temp_bytes(n + 1),
                         gdprim::scan_temp_bytes((int64_t)bi.start_total),
                         gdprim::scan_temp_bytes((int64_t)W)});
-  GD_TRY(ctx->ensure(ctx->scantemp, sc, "scan temp"));
+  GD_TRY(ctx->ensure_zeroed(ctx->scantemp, sc, "scan temp"));
   const int key_bits = bi.LB + bi.IB;
   int r;
   uint32_t* vb[2] = {static_cast<uint32_t*>(ctx->vals0.p), static_cast<uint32_t*>(ctx->vals1.p)};
@@ -291,18 +301,16 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
   if (ctx->key64) {
     using U64 = unsigned long long;
     U64* kb[2] = {static_cast<U64*>(ctx->keys0.p), static_cast<U64*>(ctx->keys1.p)};
-    r = gdprim::radix_sort_pairs<U64>(kb, vb, n, key_bits, true, ctx->sorttemp.p, s);
+    r = gdprim::radix_sort_pairs<U64>(kb, vb, n, key_bits, true, ctx->sorttemp.p, s,
+                                        ctx->dCtr() + gd::kCtrWaitTimeouts);
     ctx->skeys = kb[r];
   } else {
     uint32_t* kb[2] = {static_cast<uint32_t*>(ctx->keys0.p), static_cast<uint32_t*>(ctx->keys1.p)};
-    r = gdprim::radix_sort_pairs<uint32_t>(kb, vb, n, key_bits, true, ctx->sorttemp.p, s);
+    r = gdprim::radix_sort_pairs<uint32_t>(kb, vb, n, key_bits, true, ctx->sorttemp.p, s,
+                                        ctx->dCtr() + gd::kCtrWaitTimeouts);
     ctx->skeys = kb[r];
   }
-  {
-    const int rb = gdprim::sort_digit_bits(key_bits);
-    const int passes = (key_bits + rb - 1) / rb;
-    L += n > 0 ? (passes ? passes * 5 : 1) : 0;  // upsweep, 3 scan kernels, downsweep per pass
-  }
+  L += gdprim::sort_launches(n, key_bits);
   ctx->sids = vb[r];
   B = ctx->bufs();
   L += gdl::gather(B, ctx->key64, n, ctx->xf, K == 1, ctx->sms, s);
@@ -313,8 +321,8 @@ gd_status build_run(gd_ctx* ctx, uint64_t dense_floor, uint64_t dense_per_point)
   L += gdl::cell_counts(B, ctx->key64, n, ctx->sms, s);
   L += gdl::start_fill(B, ctx->K, s);
   gdprim::exclusive_scan_u32(B.start, B.start, (int64_t)bi.start_total, ctx->scantemp.p, nullptr,
-                             s);
-  L += bi.start_total ? 3 : 0;
+                             s, ctx->dCtr() + gd::kCtrWaitTimeouts);
+  L += gdprim::scan_launches((int64_t)bi.start_total);
   L += gdl::occ_rank(B, ctx->K, ctx->scantemp.p, s);
   if (bi.any_sparse) {
     GD_CUDA(cudaMemsetAsync(ctx->hkeys.p, 0xff, hcap * 8, s), "clear row hash");
@@ -366,8 +374,9 @@ gd_status expand_run(gd_ctx* ctx) {
   GD_TRY(ctx->ensure(ctx->asym, gd::kAsymCap * 8, "one-directional links"));
   GD_TRY(ctx->ensure(ctx->hvcell, n * 4, "heavy-work list"));
   GD_TRY(ctx->ensure(ctx->hvmask, n * 8, "heavy-work masks"));
-  GD_TRY(ctx->ensure(ctx->scantemp, std::max(gdprim::scan_temp_bytes(n + 1), ctx->scantemp.bytes),
-                     "scan temp"));
+  GD_TRY(ctx->ensure_zeroed(ctx->scantemp,
+                            std::max(gdprim::scan_temp_bytes(n + 1), ctx->scantemp.bytes),
+                            "scan temp"));
   ctx->stage = 2;
   if (ctx->graphs && ctx->xgraph) {
     GD_CUDA(cudaGraphLaunch(ctx->xgraph, s), "expand graph launch");
@@ -459,6 +468,14 @@ gd_status finish_run(gd_ctx* ctx, int32_t* labels, uint8_t* is_core, int32_t on_
   S.asym_pairs = (int64_t)ctr[gd::kCtrAsym];
   S.precision_used = ctx->f32 ? GD_PREC_FP32_BAND : GD_PREC_FP64;
   S.launches = ctx->launches + ctx->expand_launches + fin;
+  if (ctr[gd::kCtrWaitTimeouts]) {
+    // start the scan and sort state afresh for the next run
+    if (ctx->sorttemp.p) cudaMemsetAsync(ctx->sorttemp.p, 0, ctx->sorttemp.bytes, s);
+    if (ctx->scantemp.p) cudaMemsetAsync(ctx->scantemp.p, 0, ctx->scantemp.bytes, s);
+    cudaStreamSynchronize(s);
+    ctx->stage = 1;
+    return fail(GD_ECUDA, "a scan or sort look-back wait gave up (results discarded)");
+  }
   if (ctr[gd::kCtrAsymEdges] > (unsigned long long)gd::kAsymCap) {
     ctx->stage = 1;
     return fail(GD_ERANGE, "more one-directional core neighbour pairs than the merge replay "

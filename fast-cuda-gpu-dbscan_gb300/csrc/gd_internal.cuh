@@ -195,7 +195,8 @@ enum Counter {
   kCtrCells2D,          // cells of 2D instances (they sort first)
   kCtrWalkCursor2,      // walk-list entries handed out (2D, 3D); cleared before each walk launch
   kCtrWalkCursor3,
-  kCtrCount = 16
+  kCtrWaitTimeouts,     // scan / sort launches whose look-back wait gave up (never expected)
+  kCtrCount = 17
 };
 
 // Capacity of the list of one-directional core-core pairs (see k_asym_resolve).
@@ -281,30 +282,40 @@ __device__ __forceinline__ void uf_union(int* parent, const int* cellmin, int a,
 
 // ---- host-side primitive launchers (gd_prims.cu) ---------------------------
 namespace gdprim {
-// temp bytes needed by exclusive_scan_u32 for n elements
+// temp bytes needed by exclusive_scan_u32 / exclusive_scan_popc for n
+// elements.  Temp memory must be zero when first used and is then kept
+// consistent by the primitives themselves (one stream at a time).
 size_t scan_temp_bytes(int64_t n);
+// kernels one scan of n elements launches
+int scan_launches(int64_t n);
 // out[i] = sum_{j<i} in[i]; in == out allowed.  Returns the total in *total_dev
-// (device pointer, may be null).
+// (device pointer, may be null).  timeouts (may be null): incremented when a
+// look-back wait gave up (the result is then wrong but every write in bounds).
 void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, void* temp,
-                        uint32_t* total_dev, cudaStream_t s);
+                        uint32_t* total_dev, cudaStream_t s,
+                        unsigned long long* timeouts = nullptr);
 // pre[w] = number of set bits in words[0, w) (exclusive scan of popcounts),
 // total in *total_dev (may be null); words and pre 16-byte aligned, distinct.
 void exclusive_scan_popc(const uint32_t* words, uint32_t* pre, int64_t nw, void* temp,
-                         uint32_t* total_dev, cudaStream_t s);
+                         uint32_t* total_dev, cudaStream_t s,
+                         unsigned long long* timeouts = nullptr);
 // the positions of the set bits of words[0, nw) in ascending order:
 // out[pre[w] + r] = 32 w + (position of the r-th set bit of word w)
 void compact_bits(const uint32_t* words, const uint32_t* pre, int64_t nw, uint32_t* out, int sms,
                   cudaStream_t s);
-// temp bytes needed by radix_sort_pairs for n elements (either key width)
+// temp bytes needed by radix_sort_pairs for n elements (either key width);
+// zero when first used, as for the scan
 size_t sort_temp_bytes(int64_t n);
 // Stable LSD radix sort of (key, value) pairs on the low `bits` key bits,
 // K = uint32_t or unsigned long long.  keys/vals: ping-pong buffers [0] and
 // [1]; input in [0].  If vals_in_is_iota, vals[0] is not read and the values
 // are taken as 0..n-1.  Returns the index (0 or 1) of the buffer that holds the
-// result.
+// result.  timeouts as for the scan.
 template <class K>
 int radix_sort_pairs(K* keys[2], uint32_t* vals[2], int64_t n, int bits, bool vals_in_is_iota,
-                     void* temp, cudaStream_t s);
+                     void* temp, cudaStream_t s, unsigned long long* timeouts = nullptr);
+// kernels one radix_sort_pairs call launches
+int sort_launches(int64_t n, int bits);
 // digit width radix_sort_pairs uses for a `bits`-bit key (8 or 9)
 int sort_digit_bits(int bits);
 }  // namespace gdprim

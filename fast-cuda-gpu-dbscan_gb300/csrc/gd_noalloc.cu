@@ -188,7 +188,6 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
     return fail(GD_EINVAL, "gd_dbscan_noalloc: NULL pointer");
   if (n_clusters) *n_clusters = 0;
   if (n == 0) return GD_OK;
-  static_assert(kSortTempBytes >= 16 * 256 * 4 + 256 + 256, "sort temp too small");
   if (gdprim::sort_temp_bytes(kMaxPoints) > kSortTempBytes ||
       gdprim::scan_temp_bytes((int64_t)kTableCells + 1) > kScanTempBytes ||
       gdprim::scan_temp_bytes(kMaxPoints + 1) > kScanTempBytes)
@@ -253,12 +252,14 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   if (key64) {
     using U64 = unsigned long long;
     U64* kb[2] = {reinterpret_cast<U64*>(base + kOffKeys0), reinterpret_cast<U64*>(base + kOffKeys1)};
-    r = gdprim::radix_sort_pairs<U64>(kb, vb, n, key_bits, true, base + kOffSortTemp, s);
+    r = gdprim::radix_sort_pairs<U64>(kb, vb, n, key_bits, true, base + kOffSortTemp, s,
+                                      dCtr + gd::kCtrWaitTimeouts);
     skeys = kb[r];
   } else {
     uint32_t* kb[2] = {reinterpret_cast<uint32_t*>(base + kOffKeys0),
                        reinterpret_cast<uint32_t*>(base + kOffKeys1)};
-    r = gdprim::radix_sort_pairs<uint32_t>(kb, vb, n, key_bits, true, base + kOffSortTemp, s);
+    r = gdprim::radix_sort_pairs<uint32_t>(kb, vb, n, key_bits, true, base + kOffSortTemp, s,
+                                           dCtr + gd::kCtrWaitTimeouts);
     skeys = kb[r];
   }
   B.keys = skeys;
@@ -287,7 +288,7 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   gdl::cell_counts(B, key64, n, sms, s);
   gdl::start_fill(B, 1, s);
   gdprim::exclusive_scan_u32(B.start, B.start, (int64_t)bi.start_total, base + kOffScanTemp,
-                             nullptr, s);
+                             nullptr, s, dCtr + gd::kCtrWaitTimeouts);
   gdl::occ_rank(B, 1, base + kOffScanTemp, s);
   if (bi.any_sparse) {
     NA_CUDA(cudaMemsetAsync(B.hkeys, 0xff, kHashSlots * 8, s), "clear row hash");
@@ -311,13 +312,18 @@ extern "C" gd_status gd_dbscan_noalloc(const double* coords_dev, int64_t n, int3
   gdl::border(B, n, dims, f32, key64, sms, s);
   gdl::scatter_labels(B, n, labels_dev, nullptr, sms, s);
   NA_CUDA(cudaGetLastError(), "launch");
-  unsigned long long asym_edges = 0;
+  unsigned long long ctr[gd::kCtrCount];
   uint32_t K = 0;
-  NA_CUDA(cudaMemcpyAsync(&asym_edges, dCtr + gd::kCtrAsymEdges, 8, cudaMemcpyDeviceToHost, s),
-          "read counters");
+  NA_CUDA(cudaMemcpyAsync(ctr, dCtr, sizeof ctr, cudaMemcpyDeviceToHost, s), "read counters");
   NA_CUDA(cudaMemcpyAsync(&K, dK, 4, cudaMemcpyDeviceToHost, s), "read cluster count");
   NA_CUDA(cudaStreamSynchronize(s), "DBSCAN pipeline");
-  if (asym_edges > (unsigned long long)gd::kAsymCap)
+  if (ctr[gd::kCtrWaitTimeouts]) {
+    // start the scan and sort state afresh for the next call
+    cudaMemsetAsync(base + kOffSortTemp, 0, kSortTempBytes + kScanTempBytes, s);
+    cudaStreamSynchronize(s);
+    return fail(GD_ECUDA, "gd_dbscan_noalloc: a scan or sort look-back wait gave up");
+  }
+  if (ctr[gd::kCtrAsymEdges] > (unsigned long long)gd::kAsymCap)
     return fail(GD_ERANGE, "gd_dbscan_noalloc: too many one-directional core neighbour pairs");
   if (n_clusters) *n_clusters = K;
   return GD_OK;

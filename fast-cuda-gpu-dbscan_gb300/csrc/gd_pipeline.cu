@@ -1250,6 +1250,14 @@ constexpr OffTab make_full(int D) {
 }
 
 __constant__ OffTab kRows[2] = {make_rows(2), make_rows(3)};
+// rows per dimension, and the 3D rows within one cell of the own row (the
+// first nine of make_rows(3))
+constexpr int kRowsPerDim[2] = {5, 25};
+constexpr int kNearRows3 = 9;
+static_assert(make_rows(2).n == kRowsPerDim[0] && make_rows(3).n == kRowsPerDim[1], "rows");
+static_assert(row_rank(make_rows(3).o[kNearRows3 - 1][0], make_rows(3).o[kNearRows3 - 1][1]) < 8 &&
+                  row_rank(make_rows(3).o[kNearRows3][0], make_rows(3).o[kNearRows3][1]) >= 8,
+              "the near rows come first");
 __constant__ OffTab kHalf[2][kUnionPasses] = {{make_half(2, 0), make_half(2, 1), make_half(2, 2)},
                                               {make_half(3, 0), make_half(3, 1), make_half(3, 2)}};
 
@@ -1625,8 +1633,17 @@ __global__ void k_core_split(const gdl::Bufs B, int64_t n) {
 // sends its cell to the warp kernel, which recomputes the whole cell.
 // Per-cell core counts and smallest core indices are warp-aggregated atomics
 // (cleared before the launch).
+//
+// Rows [r0, r1) of the stencil.  A walk split in two (3D) first takes the 3x3
+// near rows for every listed point (r1 < rows): a point still undecided after
+// them keeps its count in lab[] and its bit in fbits, and the second launch
+// (r0 > 0) walks the remaining rows for that compacted list only.  Most points
+// decide within the near rows, so the second launch's warps hold only the
+// points that need the long walk instead of idling beside them (C3: a warp
+// ran 13.4 rows where its lanes needed 6.2 on average).
 template <int D, bool F32, bool KEY64>
-__global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_point(const gdl::Bufs B, int64_t n) {
+__global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks)
+k_core_point(const gdl::Bufs B, int64_t n, int r0, int r1) {
   __shared__ int2 sq[core_queue(D, F32)][kScanThreadsPerBlock];
   // per thread: squared largest / smallest distance terms to the five cell
   // slabs along the last axis (offsets -2..2), kept out of registers
@@ -1637,10 +1654,14 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
   const int wbase = threadIdx.x & ~31;
   CoreFlushStage<D, F32>& S = stage[F32 ? 0 : threadIdx.x >> 5];
   const int LB = B.Bi->LB;
+  const bool second = r0 > 0;    // the list and counts of a first launch
+  const bool split = r1 < T.n;   // a second launch follows
   // this dimension's part of the walk list: 2D instances' points come first
   const int64_t p3 = B.reps[(int64_t)B.ctr[kCtrCells2D]];
   const int64_t L = (int64_t)*B.lcount;
-  const int64_t L2 = p3 < n ? (int64_t)bit_rank(B.lbits, B.lpre, p3) : L;
+  const int64_t L2 =
+      p3 < n ? (int64_t)(second ? bit_rank(B.fbits, B.fpre, p3) : bit_rank(B.lbits, B.lpre, p3))
+             : L;
   const int64_t jlo = D == 2 ? 0 : L2, jhi = D == 2 ? L2 : L;
   WalkCursor wc = walk_cursor<D>(B, jlo, jhi);
   Tally t;
@@ -1652,6 +1673,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
     int m = -1, b = 0;
     bool isc = false, over = false, pend = false;
     int cnt = 0, nq = 0, minpts = 0;
+    if (valid && second) cnt = B.lab[i];
     if (valid) {
       m = cell_of(B, i);
       b = B.reps[m];
@@ -1700,7 +1722,7 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
           nq = 0;
           ptot = 0;
         };
-        for (int r = 0; r < T.n && cnt < Q.minpts && !over; ++r) {
+        for (int r = r0; r < r1 && cnt < Q.minpts && !over; ++r) {
           float rmx = 0.0f, rmn = 0.0f;
           if (prune) {
 #pragma unroll
@@ -1773,8 +1795,10 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
             q = qe;
           }
         }
-        // what is still queued decides only if it can lift the count to minpts
-        pend = !over && cnt < Q.minpts && nq > 0 && cnt + ptot >= Q.minpts;
+        // what is still queued decides only if it can lift the count to minpts;
+        // before a second launch it is always counted (that launch walks the
+        // other rows only)
+        pend = !over && cnt < Q.minpts && nq > 0 && (split || cnt + ptot >= Q.minpts);
         if (pend) {
 #pragma unroll
           for (int k = 0; k < D; ++k) {
@@ -1849,7 +1873,13 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kCoreMinBlocks) k_core_p
       }
       __syncwarp();
     }
-    if (valid && !over) B.core[i] = isc ? 1 : 0;
+    // undecided after the near rows: on to the second launch
+    const bool go_on = split && valid && !over && !isc;
+    if (go_on) {
+      B.lab[i] = cnt;
+      atomicOr(B.fbits + (i >> 5), 1u << (i & 31));
+    }
+    if (valid && !over && !go_on) B.core[i] = isc ? 1 : 0;
     // per-cell core count and smallest core index, one atomic pair per cell
     // and warp
     const unsigned cm = __ballot_sync(kFull, isc);
@@ -2788,13 +2818,13 @@ int gather(const Bufs& B, bool key64, int64_t n, bool xf, bool one, int sms, cud
 }
 
 // kernels of one exclusive scan over nw words
-static int scan_launches(int64_t nw) { return nw > 0 ? 3 : 0; }
+static int scan_launches(int64_t nw) { return gdprim::scan_launches(nw); }
 
 // the set bits of B.lbits over [0, n) listed in order into B.blist, their
 // count in *B.lcount
 static int list_bits(const Bufs& B, int64_t n, int sms, void* scan_temp, cudaStream_t s) {
   const int64_t nw = (n + 31) / 32;
-  gdprim::exclusive_scan_popc(B.lbits, B.lpre, nw, scan_temp, B.lcount, s);
+  gdprim::exclusive_scan_popc(B.lbits, B.lpre, nw, scan_temp, B.lcount, s, B.ctr + kCtrWaitTimeouts);
   gdprim::compact_bits(B.lbits, B.lpre, nw, B.blist, sms, s);
   return scan_launches(nw) + (nw > 0 ? 1 : 0);
 }
@@ -2806,7 +2836,7 @@ int runs(const Bufs& B, bool key64, int64_t n, bool mixed, int sms, void* scan_t
   if (key64) k_run_bits<unsigned long long><<<g, 256, 0, s>>>(
       static_cast<const unsigned long long*>(B.keys), n, B.runbits);
   else k_run_bits<uint32_t><<<g, 256, 0, s>>>(static_cast<const uint32_t*>(B.keys), n, B.runbits);
-  gdprim::exclusive_scan_popc(B.runbits, B.runpre, nw, scan_temp, B.M, s);
+  gdprim::exclusive_scan_popc(B.runbits, B.runpre, nw, scan_temp, B.M, s, B.ctr + kCtrWaitTimeouts);
   gdprim::compact_bits(B.runbits, B.runpre, nw, reinterpret_cast<uint32_t*>(B.reps), sms, s);
   if (key64) k_runs_finish<unsigned long long><<<1, 32, 0, s>>>(B, n, mixed ? 1 : 0);
   else k_runs_finish<uint32_t><<<1, 32, 0, s>>>(B, n, mixed ? 1 : 0);
@@ -2826,7 +2856,7 @@ int start_fill(const Bufs& B, int K, cudaStream_t s) {
 
 int occ_rank(const Bufs& B, int K, void* scan_temp, cudaStream_t s) {
   if (!B.occ_words) return 0;
-  gdprim::exclusive_scan_popc(B.occ, B.wpre, (int64_t)B.occ_words, scan_temp, nullptr, s);
+  gdprim::exclusive_scan_popc(B.occ, B.wpre, (int64_t)B.occ_words, scan_temp, nullptr, s, B.ctr + kCtrWaitTimeouts);
   k_rank_off<<<(K + 127) / 128, 128, 0, s>>>(B, K);
   return scan_launches((int64_t)B.occ_words) + 1;
 }
@@ -2874,7 +2904,20 @@ int core(const Bufs& B, int64_t n, int dims, bool f32, bool key64, bool one, int
   }
   int L = 1 + list_bits(B, n, sms, scan_temp, s);
   cudaMemsetAsync(B.ctr + kCtrWalkCursor2, 0, 16, s);
-  GD_LAUNCH_DIMS(dims, f32, key64, k_core_point, sms * 8, kScanThreadsPerBlock, B, n);
+  // 3D walks split after the 3x3 near rows (the first nine of kRows)
+  const int rows2 = kRowsPerDim[0], rows3 = kRowsPerDim[1], near3 = kNearRows3;
+  if (dims & 2) cudaMemsetAsync(B.fbits, 0, (size_t)B.nw * 4, s);
+  if (dims & 1) GD_L1(2, f32, key64, k_core_point, sms * 8, kScanThreadsPerBlock, B, n, 0, rows2);
+  if (dims & 2) {
+    GD_L1(3, f32, key64, k_core_point, sms * 8, kScanThreadsPerBlock, B, n, 0, near3);
+    // the undecided 3D points, listed in sorted order
+    gdprim::exclusive_scan_popc(B.fbits, B.fpre, B.nw, scan_temp, B.lcount, s,
+                                B.ctr + kCtrWaitTimeouts);
+    gdprim::compact_bits(B.fbits, B.fpre, B.nw, B.blist, sms, s);
+    cudaMemsetAsync(B.ctr + kCtrWalkCursor3, 0, 8, s);
+    GD_L1(3, f32, key64, k_core_point, sms * 8, kScanThreadsPerBlock, B, n, near3, rows3);
+    L += scan_launches(B.nw) + 2;
+  }
   GD_LAUNCH_DIMS(dims, f32, key64, k_core_heavy, sms * 8, kCellThreads, B, n);
   return L + 2 * per_dim(dims);
 }
@@ -2908,7 +2951,7 @@ int roots(const Bufs& B, bool key64, int64_t n, int sms, void* scan_temp, cudaSt
   cudaMemsetAsync(B.fbits, 0, (size_t)(B.nwf + 1) * 4, s);
   k_roots<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
   // total clusters into the small block (read with the counters)
-  gdprim::exclusive_scan_popc(B.fbits, B.fpre, B.nwf, scan_temp, B.K, s);
+  gdprim::exclusive_scan_popc(B.fbits, B.fpre, B.nwf, scan_temp, B.K, s, B.ctr + kCtrWaitTimeouts);
   if (key64) k_cell_ids<true><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
   else k_cell_ids<false><<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
   return 2 + scan_launches(B.nwf);

@@ -1,20 +1,36 @@
 // gd_prims.cu -- device primitives: exclusive scan and a stable LSD radix sort.
 //
-// Both are reduce-then-scan designs: no kernel waits on another block, so no
-// spin loop exists anywhere in them.
+// The scan is a single-pass design with decoupled look-back: each tile
+// publishes its aggregate, reads its predecessors' published values back to the
+// nearest inclusive prefix, and publishes its own inclusive prefix.  Tiles take
+// their index from an atomic counter when their block starts, so a tile only
+// waits on tiles that running blocks hold and every wait ends; each wait is
+// still bounded (kWaitPolls polls), and a wait that gives up counts the
+// predecessor as 0 -- every offset then stays at or below its true value, so no
+// write leaves its array -- and is reported through the caller's counter.
 //
-// Scan (u32): tiles of 4096 elements (512 threads x 8 contiguous items).
-//   k_scan_reduce    tile sums                       reads 4 B/elem
-//   k_scan_partials  one block scans the tile sums
-//   k_scan_down      tile-local scan + tile offset   reads 4 B, writes 4 B/elem
+// Scan (u32): tiles of 4096 elements (512 threads x 8 contiguous items), one
+// launch (k_scan_onepass): reads 4 B, writes 4 B/elem.  Against the earlier
+// reduce / partials / down-sweep kernels it saves two launches per scan (C2:
+// union and label phases about 10 us faster each).
 // Radix sort (u32 or u64 key, u32 value), 8- or 9-bit digits, tiles of 4096 pairs
 // (256 threads x 16 items; each warp owns a contiguous 512-element segment so
 // warp-local ranking in item order is stable):
 //   k_rs_upsweep     per-tile digit histograms       reads 4 B/pair
-//   exclusive scan over the [digit][tile] histogram
+//   exclusive scan over the [digit][tile] histogram (k_scan_onepass)
 //   k_rs_downsweep   rank in tile, regroup in shared memory, scatter
 //                                                    reads 8 B, writes 8 B/pair
+// A onesweep variant (one histogram kernel for all passes, per-digit look-back
+// in the scatter kernel) was measured slower on C2 (index phase 0.78 -> 0.94
+// ms): with about 760 tiles in flight the serial per-digit look-back chains
+// cost more than the upsweep and the histogram scan they replace.
 // This replaces thrust::sort_by_key (main.cu:332).
+//
+// The scan's state between launches lives in the caller's temp memory, which
+// must be zero when first used (the callers clear it when they allocate it): a
+// control block (tile counter, finished-block counter, launch epoch) that the
+// last block of each launch resets, and the status words, tagged with the
+// launch's epoch so that words left by earlier launches read as not ready.
 #include "gd_internal.cuh"
 
 namespace gdprim {
@@ -62,57 +78,121 @@ __device__ __forceinline__ uint32_t scan_val(uint32_t x) {
   return POPC ? (uint32_t)__popc(x) : x;
 }
 
-template <bool POPC>
-__global__ void __launch_bounds__(kScanThreads)
-k_scan_reduce(const uint32_t* __restrict__ in, int64_t n, uint32_t* __restrict__ partial) {
-  __shared__ uint32_t s_warp[32];
-  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
-  uint32_t sum = 0;
-  if (base + kScanItems <= n) {
-    const uint4* p = reinterpret_cast<const uint4*>(in + base);
-    uint4 a = p[0], b = p[1];
-    sum = scan_val<POPC>(a.x) + scan_val<POPC>(a.y) + scan_val<POPC>(a.z) + scan_val<POPC>(a.w) +
-          scan_val<POPC>(b.x) + scan_val<POPC>(b.y) + scan_val<POPC>(b.z) + scan_val<POPC>(b.w);
-  } else {
-    for (int i = 0; i < kScanItems; ++i)
-      if (base + i < n) sum += scan_val<POPC>(in[base + i]);
+// ------------------------------------------------------------ look-back state
+struct LookbackCtl {
+  unsigned int tile;   // next tile index of the running launch
+  unsigned int done;   // blocks of the running launch that finished
+  unsigned int epoch;  // launches completed on this control block
+  unsigned int pad[13];
+};
+static_assert(sizeof(LookbackCtl) == 64, "control block is 64 bytes");
+
+// A predecessor tile's block is already running when its tile is waited on, so
+// its aggregate follows within microseconds; 2^14 polls (about 16 ms) only end
+// waits that could never succeed.
+constexpr unsigned kWaitPolls = 1u << 14;
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// status word: tag (bits 63..34), kind (33..32: 1 aggregate, 2 inclusive
+// prefix), value (31..0)
+__device__ __forceinline__ unsigned long long lb_word(uint32_t tag, uint32_t kind, uint32_t v) {
+  return ((unsigned long long)tag << 34) | ((unsigned long long)kind << 32) | v;
+}
+
+// A tile's status word once it carries this launch's tag: its kind (1 or 2)
+// and value; kind 0 (value 0) when kWaitPolls polls saw nothing.
+__device__ __forceinline__ uint32_t lb_wait(const unsigned long long* p, uint32_t tag,
+                                            uint32_t& v) {
+  for (unsigned it = 0; it < kWaitPolls; ++it) {
+    const unsigned long long w = ld_relaxed_u64(p);
+    const uint32_t kind = (uint32_t)(w >> 32) & 3u;
+    if ((uint32_t)(w >> 34) == tag && kind != 0u) {
+      v = (uint32_t)w;
+      return kind;
+    }
+    if (it >= 4) __nanosleep(64);
   }
-  // block reduction
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(gd::kFull, sum, o);
-  if (lane == 0) s_warp[w] = sum;
+  v = 0;
+  return 0;
+}
+
+// Block start: the tile index (from the counter) and the launch's tag.
+__device__ __forceinline__ void lb_begin(LookbackCtl* ctl, unsigned* s_tile, unsigned* s_epoch) {
+  if (threadIdx.x == 0) {
+    *s_tile = atomicAdd(&ctl->tile, 1u);
+    *s_epoch = *reinterpret_cast<volatile unsigned*>(&ctl->epoch);
+  }
   __syncthreads();
-  if (w == 0) {
-    uint32_t t = lane < kScanThreads / 32 ? s_warp[lane] : 0u;
+}
+
+__device__ __forceinline__ uint32_t lb_tag(unsigned epoch) { return (epoch & 0x3fffffffu) + 1u; }
+
+// Block end, after every thread is done with the status words: the last block
+// of the launch resets the counters and advances the epoch for the next one.
+__device__ __forceinline__ void lb_end(LookbackCtl* ctl, unsigned tiles, unsigned epoch) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&ctl->done, 1u) == tiles - 1u) {
+      ctl->tile = 0u;
+      ctl->done = 0u;
+      ctl->epoch = epoch + 1u;
+    }
+  }
+}
+
+// Exclusive prefix of tile `tile` from its predecessors' status words, by one
+// warp (32 predecessors per round, nearest first).  *gave_up: a wait ran out.
+__device__ __forceinline__ uint32_t lb_warp_prefix(const unsigned long long* status, int64_t tile,
+                                                   uint32_t tag, bool* gave_up) {
+  const int lane = threadIdx.x & 31;
+  uint32_t excl = 0;
+  bool lost = false;
+  for (int64_t top = tile - 1; top >= 0; top -= 32) {
+    const int64_t k = top - lane;
+    uint32_t v = 0, kind = 2;  // before tile 0: an inclusive prefix of 0
+    if (k >= 0) kind = lb_wait(status + k, tag, v);
+    lost |= __any_sync(gd::kFull, kind == 0u);
+    // nearest lane holding a prefix (or a wait that gave up): sum up to it
+    const unsigned stop = __ballot_sync(gd::kFull, kind != 1u);
+    const int last = stop ? __ffs(stop) - 1 : 31;
+    uint32_t add = lane <= last ? v : 0u;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(gd::kFull, t, o);
-    if (lane == 0) partial[blockIdx.x] = t;
+    for (int o = 16; o > 0; o >>= 1) add += __shfl_xor_sync(gd::kFull, add, o);
+    excl += add;
+    if (stop) break;
   }
+  *gave_up = lost;
+  return excl;
 }
 
-__global__ void __launch_bounds__(1024)
-k_scan_partials(uint32_t* partial, int64_t T, uint32_t* total_dev) {
-  __shared__ uint32_t s_warp[32];
-  __shared__ uint32_t s_total;
-  uint32_t carry = 0;
-  for (int64_t base = 0; base < T; base += 1024) {
-    int64_t i = base + threadIdx.x;
-    uint32_t v = i < T ? partial[i] : 0u;
-    uint32_t ex = block_excl_scan<1024>(v, s_warp, &s_total);
-    if (i < T) partial[i] = carry + ex;
-    __syncthreads();
-    carry += s_total;
-    __syncthreads();
-  }
-  if (threadIdx.x == 0 && total_dev) *total_dev = carry;
-}
-
+// Single-pass exclusive scan (decoupled look-back).
 template <bool POPC>
 __global__ void __launch_bounds__(kScanThreads)
-k_scan_down(const uint32_t* in, uint32_t* out, int64_t n, const uint32_t* __restrict__ partial) {
+k_scan_onepass(const uint32_t* in, uint32_t* out, int64_t n, unsigned tiles, LookbackCtl* ctl,
+               unsigned long long* status, uint32_t* total_dev, unsigned long long* timeouts) {
   __shared__ uint32_t s_warp[32];
-  const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+  __shared__ unsigned s_tile, s_epoch;
+  __shared__ uint32_t s_agg, s_excl;
+  lb_begin(ctl, &s_tile, &s_epoch);
+  const unsigned tile = s_tile, epoch = s_epoch;
+  const uint32_t tag = lb_tag(epoch);
+  if (tile >= tiles) {
+    // a counter left inconsistent (never expected): no tile, report it
+    if (threadIdx.x == 0 && timeouts) atomicAdd(timeouts, 1ull);
+    lb_end(ctl, tiles, epoch);
+    return;
+  }
+  const int64_t base = (int64_t)tile * kScanTile + (int64_t)threadIdx.x * kScanItems;
   uint32_t v[kScanItems];
   const bool full = base + kScanItems <= n;
   if (full) {
@@ -126,10 +206,25 @@ k_scan_down(const uint32_t* in, uint32_t* out, int64_t n, const uint32_t* __rest
   }
 #pragma unroll
   for (int i = 0; i < kScanItems; ++i) v[i] = scan_val<POPC>(v[i]);
-  uint32_t s = 0;
+  uint32_t sum = 0;
 #pragma unroll
-  for (int i = 0; i < kScanItems; ++i) s += v[i];
-  uint32_t ex = block_excl_scan<kScanThreads>(s, s_warp, nullptr) + partial[blockIdx.x];
+  for (int i = 0; i < kScanItems; ++i) sum += v[i];
+  uint32_t ex = block_excl_scan<kScanThreads>(sum, s_warp, &s_agg);
+  if (threadIdx.x < 32) {
+    const uint32_t agg = s_agg;
+    unsigned long long* my = status + tile;
+    if (threadIdx.x == 0) st_relaxed_u64(my, lb_word(tag, tile == 0 ? 2u : 1u, agg));
+    bool lost = false;
+    const uint32_t excl = tile == 0 ? 0u : lb_warp_prefix(status, (int64_t)tile, tag, &lost);
+    if (threadIdx.x == 0) {
+      if (tile != 0) st_relaxed_u64(my, lb_word(tag, 2u, excl + agg));
+      s_excl = excl;
+      if (lost && timeouts) atomicAdd(timeouts, 1ull);
+      if (tile == tiles - 1u && total_dev) *total_dev = excl + agg;
+    }
+  }
+  __syncthreads();
+  ex += s_excl;
 #pragma unroll
   for (int i = 0; i < kScanItems; ++i) {
     uint32_t t = v[i];
@@ -145,6 +240,7 @@ k_scan_down(const uint32_t* in, uint32_t* out, int64_t n, const uint32_t* __rest
     for (int i = 0; i < kScanItems; ++i)
       if (base + i < n) out[base + i] = v[i];
   }
+  lb_end(ctl, tiles, epoch);
 }
 
 // ---------------------------------------------------------------- radix sort
@@ -322,33 +418,37 @@ inline size_t align_up(size_t x) { return (x + 255) & ~(size_t)255; }
 
 }  // namespace
 
+// temp layout of both primitives: control block (64 B), then their arrays
 size_t scan_temp_bytes(int64_t n) {
-  int64_t T = (n + kScanTile - 1) / kScanTile;
-  return align_up((size_t)(T + 1) * sizeof(uint32_t));
+  const int64_t T = (n + kScanTile - 1) / kScanTile;
+  return align_up(sizeof(LookbackCtl) + (size_t)(T > 0 ? T : 1) * 8);
 }
+
+int scan_launches(int64_t n) { return n > 0 ? 1 : 0; }
 
 template <bool POPC>
 void scan_impl(const uint32_t* in, uint32_t* out, int64_t n, void* temp, uint32_t* total_dev,
-               cudaStream_t s) {
+               cudaStream_t s, unsigned long long* timeouts) {
   if (n <= 0) {
     if (total_dev) cudaMemsetAsync(total_dev, 0, sizeof(uint32_t), s);
     return;
   }
-  int64_t T = (n + kScanTile - 1) / kScanTile;
-  uint32_t* partial = static_cast<uint32_t*>(temp);
-  k_scan_reduce<POPC><<<(unsigned)T, kScanThreads, 0, s>>>(in, n, partial);
-  k_scan_partials<<<1, 1024, 0, s>>>(partial, T, total_dev);
-  k_scan_down<POPC><<<(unsigned)T, kScanThreads, 0, s>>>(in, out, n, partial);
+  const int64_t T = (n + kScanTile - 1) / kScanTile;
+  LookbackCtl* ctl = static_cast<LookbackCtl*>(temp);
+  unsigned long long* status =
+      reinterpret_cast<unsigned long long*>(static_cast<char*>(temp) + sizeof(LookbackCtl));
+  k_scan_onepass<POPC><<<(unsigned)T, kScanThreads, 0, s>>>(in, out, n, (unsigned)T, ctl, status,
+                                                            total_dev, timeouts);
 }
 
 void exclusive_scan_u32(const uint32_t* in, uint32_t* out, int64_t n, void* temp,
-                        uint32_t* total_dev, cudaStream_t s) {
-  scan_impl<false>(in, out, n, temp, total_dev, s);
+                        uint32_t* total_dev, cudaStream_t s, unsigned long long* timeouts) {
+  scan_impl<false>(in, out, n, temp, total_dev, s, timeouts);
 }
 
 void exclusive_scan_popc(const uint32_t* words, uint32_t* pre, int64_t nw, void* temp,
-                         uint32_t* total_dev, cudaStream_t s) {
-  scan_impl<true>(words, pre, nw, temp, total_dev, s);
+                         uint32_t* total_dev, cudaStream_t s, unsigned long long* timeouts) {
+  scan_impl<true>(words, pre, nw, temp, total_dev, s, timeouts);
 }
 
 void compact_bits(const uint32_t* words, const uint32_t* pre, int64_t nw, uint32_t* out, int sms,
@@ -359,26 +459,28 @@ void compact_bits(const uint32_t* words, const uint32_t* pre, int64_t nw, uint32
   k_compact_bits<<<(unsigned)g, 256, 0, s>>>(words, pre, nw, out);
 }
 
+// sort temp: the histogram scan's state (its control block at offset 0 for
+// every sort on this temp), then the [digit][tile] histogram
 size_t sort_temp_bytes(int64_t n) {
-  int64_t T = (n + kRsMinTile - 1) / kRsMinTile;
-  int64_t h = T * kRsMaxBins;
-  return align_up((size_t)h * sizeof(uint32_t)) + scan_temp_bytes(h);
+  const int64_t T = (n + kRsMinTile - 1) / kRsMinTile;
+  const int64_t h = T * kRsMaxBins;
+  return scan_temp_bytes(h) + align_up((size_t)h * sizeof(uint32_t));
 }
 
 template <class K, int RB>
 int sort_passes(K* keys[2], uint32_t* vals[2], int64_t n, int passes, bool vals_in_is_iota,
-                void* temp, cudaStream_t s) {
+                void* temp, cudaStream_t s, unsigned long long* timeouts) {
   constexpr int ITEMS = rs_items<K>();
   constexpr int TILE = kRsThreads * ITEMS;
-  int64_t T = (n + TILE - 1) / TILE;
-  int64_t h = T << RB;
-  uint32_t* hist = static_cast<uint32_t*>(temp);
-  void* scan_temp = static_cast<char*>(temp) + align_up((size_t)h * sizeof(uint32_t));
+  const int64_t T = (n + TILE - 1) / TILE;
+  const int64_t h = T << RB;
+  void* scan_temp = temp;
+  uint32_t* hist = reinterpret_cast<uint32_t*>(static_cast<char*>(temp) + scan_temp_bytes(h));
   int cur = 0;
   for (int p = 0; p < passes; ++p) {
     int shift = RB * p;
     k_rs_upsweep<K, ITEMS, RB><<<(unsigned)T, kRsThreads, 0, s>>>(keys[cur], n, shift, hist, T);
-    exclusive_scan_u32(hist, hist, h, scan_temp, nullptr, s);
+    exclusive_scan_u32(hist, hist, h, scan_temp, nullptr, s, timeouts);
     const uint32_t* vin = (p == 0 && vals_in_is_iota) ? nullptr : vals[cur];
     k_rs_downsweep<K, ITEMS, RB><<<(unsigned)T, kRsThreads, 0, s>>>(
         keys[cur], vin, keys[cur ^ 1], vals[cur ^ 1], n, shift, hist, T);
@@ -389,11 +491,18 @@ int sort_passes(K* keys[2], uint32_t* vals[2], int64_t n, int passes, bool vals_
 
 int sort_digit_bits(int bits) { return (bits + 8) / 9 < (bits + 7) / 8 ? 9 : 8; }
 
+int sort_launches(int64_t n, int bits) {
+  if (n <= 0) return 0;
+  const int rb = sort_digit_bits(bits);
+  const int passes = (bits + rb - 1) / rb;
+  return passes ? passes * 3 : 1;  // upsweep, scan, downsweep per pass
+}
+
 // Digits of 9 bits where they save a pass (a 26-bit key: 3 passes, not 4),
 // else of 8 bits.
 template <class K>
 int radix_sort_pairs(K* keys[2], uint32_t* vals[2], int64_t n, int bits, bool vals_in_is_iota,
-                     void* temp, cudaStream_t s) {
+                     void* temp, cudaStream_t s, unsigned long long* timeouts) {
   if (n <= 0) return 0;
   const int rb = sort_digit_bits(bits);
   const int passes = (bits + rb - 1) / rb;
@@ -401,13 +510,14 @@ int radix_sort_pairs(K* keys[2], uint32_t* vals[2], int64_t n, int bits, bool va
     if (vals_in_is_iota) k_iota<<<1024, 256, 0, s>>>(vals[0], n);
     return 0;
   }
-  return rb == 9 ? sort_passes<K, 9>(keys, vals, n, passes, vals_in_is_iota, temp, s)
-                 : sort_passes<K, 8>(keys, vals, n, passes, vals_in_is_iota, temp, s);
+  return rb == 9 ? sort_passes<K, 9>(keys, vals, n, passes, vals_in_is_iota, temp, s, timeouts)
+                 : sort_passes<K, 8>(keys, vals, n, passes, vals_in_is_iota, temp, s, timeouts);
 }
 
 template int radix_sort_pairs<uint32_t>(uint32_t* [2], uint32_t* [2], int64_t, int, bool, void*,
-                                        cudaStream_t);
+                                        cudaStream_t, unsigned long long*);
 template int radix_sort_pairs<unsigned long long>(unsigned long long* [2], uint32_t* [2], int64_t,
-                                                  int, bool, void*, cudaStream_t);
+                                                  int, bool, void*, cudaStream_t,
+                                                  unsigned long long*);
 
 }  // namespace gdprim
