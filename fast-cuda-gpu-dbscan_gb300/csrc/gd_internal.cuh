@@ -238,12 +238,21 @@ __device__ __forceinline__ bool box_f64(const double* p, const double* q, double
   return true;
 }
 
+// d2 <= t for a squared distance d2 (a sum of squares of finite values: +0 or
+// positive, never -0 or NaN) and any t other than NaN, from the bit patterns:
+// non-negative doubles order as their bits do as signed integers, and a
+// negative t has a negative pattern, below every d2.  An integer compare keeps
+// the test off this GPU's narrow float64 pipe.
+__device__ __forceinline__ bool d2_le(double d2, double t) {
+  return __double_as_longlong(d2) <= __double_as_longlong(t);
+}
+
 // Full predicate given d2 = dist2_f64(p, q).
 template <int D, class PP>
 __device__ __forceinline__ bool pred_from_d2(double d2, const double* p, const double* q,
                                              const PP& P) {
-  if (d2 <= P.eps2_in) return true;
-  if (!(d2 <= P.eps2)) return false;
+  if (d2_le(d2, P.eps2_in)) return true;
+  if (!d2_le(d2, P.eps2)) return false;
   return box_f64<D>(p, q, P.eps);
 }
 

@@ -922,8 +922,8 @@ __device__ __forceinline__ bool link_test(const double* sx, const float* sf, con
   sx = ax;
   ++t.t64;
   double d2 = dist2_f64<D>(sx, qx);
-  if (d2 <= P.eps2_in) return true;
-  if (!(d2 <= P.eps2)) return false;
+  if (d2_le(d2, P.eps2_in)) return true;
+  if (!d2_le(d2, P.eps2)) return false;
   bool f = box_f64<D>(sx, qx, P.eps), b = box_f64<D>(qx, sx, P.eps);
   if (f != b) {
     // q is a neighbour of a but not a of q (f), or the reverse: a directed
@@ -1990,6 +1990,12 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
         rw.init(decompose<D>(cx.local, P), P);
         float oA[D];
         if (Q.prune) cell_origin32<D>(rw.cc, P, oA);
+        // A's parent as the compression before this pass left it: A's root at
+        // the start of the pass.  Neighbours' parents were compressed at the
+        // same time, so one equal to it puts the cell in A's set however the
+        // pass's unions have moved the root since (ra, the current root, is
+        // checked too).
+        const int ra0 = reinterpret_cast<volatile int*>(B.parent)[m];
         int ra = uf_find(B.parent, (int)m);
         for (int r = 0; r < T.n; ++r) {
           const int ox = T.o[r][0], oy = T.o[r][1];
@@ -2013,7 +2019,7 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
             // A's set whatever is hooked later; the pass before compressed the
             // parents to roots).
             const int pc = reinterpret_cast<volatile int*>(B.parent)[c];
-            if (pc == ra) return;
+            if (pc == ra || pc == ra0) return;
             const int rc = pc == c ? c : uf_find(B.parent, pc);
             if (rc == ra) return;
             ra = uf_find(B.parent, ra);
@@ -2050,7 +2056,8 @@ k_union_scan(const gdl::Bufs B, int64_t n, int pass) {
             for (int z = 0; z < 5; ++z) {
               if ((cm >> z) & 1u) {
                 const int64_t r = rr + __popc(mask & ((1u << z) - 1u));
-                if (B.parent[r] != ra) slow |= 1u << z;
+                const int pr = B.parent[r];
+                if (pr != ra && pr != ra0) slow |= 1u << z;
               }
             }
             while (slow) {
@@ -2162,12 +2169,22 @@ __global__ void __launch_bounds__(kScanThreadsPerBlock, kBorderMinBlocks) k_bord
         if (ri < 0) continue;
         const int64_t rk = ri * P.G[D - 1];  // key of the row's first cell
         if (gv.sparse == 0) {
-          // cell table: visit only the cells holding a core point
-          uint32_t cm = gv.core_cells(B, (uint64_t)rk, rw.l0, rw.l1);
+          // cell table: visit only the cells holding a core point.  The
+          // occupancy, core occupancy and prefix words load together; then the
+          // row's cluster ids, together: a row none of whose ids is below best
+          // is done without looking at its cells.
+          int64_t rr = 0;
+          const uint32_t mask = gv.occ_cells(B, (uint64_t)rk, rw.l0, rw.l1, rr);
+          uint32_t cm = mask & gv.core_cells(B, (uint64_t)rk, rw.l0, rw.l1);
+          int rowmin = INT_MAX;
+#pragma unroll
+          for (int z = 0; z < 5; ++z)
+            if ((cm >> z) & 1u) rowmin = min(rowmin, B.cellcid[rr + __popc(mask & ((1u << z) - 1u))]);
+          if (rowmin >= best) continue;
           while (cm && !over) {
             const int z = __ffs(cm) - 1;
             cm &= cm - 1;
-            const int64_t rq = gv.rank(B, (uint64_t)rk + (uint64_t)(rw.l0 + z));
+            const int64_t rq = rr + __popc(mask & ((1u << z) - 1u));
             const int cB = B.cellcid[rq];
             if (cB >= best) continue;
             int cls = 0;
