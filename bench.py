@@ -63,13 +63,16 @@ METRIC = "points/sec at exact labels"
 
 # kernels of each timed phase (the library records CUDA events between phases)
 PHASE_KERNELS = {
-    "ms_index": "k_bbox_chunk, k_params_inst, k_layout, k_keys, radix sort, k_gather, "
-                "k_run_flags, scan, k_run_scatter, k_cell_counts, k_start_fill, scan, "
-                "k_occ_popc, scan, k_rank_off, k_row_hash",
-    "ms_core": "k_core_point + k_core_heavy",
-    "ms_union": "k_parent_init, k_union_scan x2, k_union_heavy x2, k_asym_resolve, k_compress",
-    "ms_label": "k_roots, scan, k_label, k_core_occ, k_border_point, k_border_heavy, "
-                "k_scatter_labels",
+    "ms_index": "k_bbox_init, k_bbox_chunk, k_params_inst, k_layout, k_keys, radix sort "
+                "(k_rs_upsweep, k_scan_onepass, k_rs_downsweep per pass), k_gather, k_run_bits, "
+                "k_scan_onepass, k_compact_bits, k_runs_finish, k_cell_counts, k_start_fill, "
+                "k_scan_onepass, k_rank_off (k_row_hash for hashed grids)",
+    "ms_core": "k_core_split, k_scan_onepass, k_compact_bits, k_core_point (3D: near rows, "
+               "k_scan_onepass, k_compact_bits, far rows), k_core_heavy",
+    "ms_union": "k_parent_init, k_scan_onepass, k_compact_bits, k_union_scan + k_union_heavy + "
+                "k_compress per pass (2D: 2 passes, 3D: 3), k_asym_resolve",
+    "ms_label": "k_roots, k_scan_onepass, k_cell_ids, k_label, k_scan_onepass, k_compact_bits, "
+                "k_border_point, k_border_heavy, k_scatter_labels",
 }
 
 
