@@ -2956,9 +2956,13 @@ int unite(const Bufs& B, int64_t n, int dims, bool f32, bool key64, int sms, voi
     GD_LAUNCH_DIMS(pd, f32, key64, k_union_scan, sms * 8, kScanThreadsPerBlock, B, n, pass);
     GD_LAUNCH_DIMS(pd, f32, key64, k_union_heavy, sms * 8, kCellThreads, B, n, pass);
     // every parent to its root: the next pass then finds most neighbours in
-    // A's set from one load (parent[q] == A's root)
-    k_compress<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
-    launched += 2 * per_dim(pd) + 1;
+    // A's set from one load (parent[q] == A's root).  After the last pass the
+    // root marks and cluster ids find their roots themselves.
+    const bool last = pass == kUnionPasses - 1 ||
+                      !(dims & ((pass + 1 < union_passes(2) ? 1 : 0) |
+                                (pass + 1 < union_passes(3) ? 2 : 0)));
+    if (!last) k_compress<<<grid_for(n, 256, sms, 8), 256, 0, s>>>(B);
+    launched += 2 * per_dim(pd) + (last ? 0 : 1);
   }
   k_asym_resolve<<<1, 32, 0, s>>>(B);
   return L + launched + 1;

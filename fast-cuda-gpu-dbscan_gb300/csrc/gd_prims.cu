@@ -9,7 +9,7 @@
 // predecessor as 0 -- every offset then stays at or below its true value, so no
 // write leaves its array -- and is reported through the caller's counter.
 //
-// Scan (u32): tiles of 4096 elements (512 threads x 8 contiguous items), one
+// Scan (u32): tiles of 8192 elements (512 threads x 16 contiguous items), one
 // launch (k_scan_onepass): reads 4 B, writes 4 B/elem.  Against the earlier
 // reduce / partials / down-sweep kernels it saves two launches per scan (C2:
 // union and label phases about 10 us faster each).
@@ -38,7 +38,7 @@ namespace gdprim {
 namespace {
 
 constexpr int kScanThreads = 512;
-constexpr int kScanItems = 8;
+constexpr int kScanItems = 16;
 constexpr int kScanTile = kScanThreads * kScanItems;
 
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
@@ -197,9 +197,11 @@ k_scan_onepass(const uint32_t* in, uint32_t* out, int64_t n, unsigned tiles, Loo
   const bool full = base + kScanItems <= n;
   if (full) {
     const uint4* p = reinterpret_cast<const uint4*>(in + base);
-    uint4 a = p[0], b = p[1];
-    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+#pragma unroll
+    for (int q = 0; q < kScanItems / 4; ++q) {
+      const uint4 a = p[q];
+      v[4 * q] = a.x; v[4 * q + 1] = a.y; v[4 * q + 2] = a.z; v[4 * q + 3] = a.w;
+    }
   } else {
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i) v[i] = base + i < n ? in[base + i] : 0u;
@@ -233,8 +235,9 @@ k_scan_onepass(const uint32_t* in, uint32_t* out, int64_t n, unsigned tiles, Loo
   }
   if (full) {
     uint4* p = reinterpret_cast<uint4*>(out + base);
-    p[0] = make_uint4(v[0], v[1], v[2], v[3]);
-    p[1] = make_uint4(v[4], v[5], v[6], v[7]);
+#pragma unroll
+    for (int q = 0; q < kScanItems / 4; ++q)
+      p[q] = make_uint4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
   } else {
 #pragma unroll
     for (int i = 0; i < kScanItems; ++i)
