@@ -67,6 +67,11 @@ constexpr uint64_t kCellsPerPoint = 64;
 // largest multipliers allowed: cell diagonal below eps (1 - 2^-20)
 constexpr double kMaxCellMult2 = 0.70710678118654752 * (1.0 - 1.0 / 1048576.0);
 constexpr double kMaxCellMult3 = 0.57735026918962576 * (1.0 - 1.0 / 1048576.0);
+// default multipliers: the smallest cells in 2D (larger 2D cells measured
+// slower: more float64 tests per walk), the largest in 3D (C3: 6.84 -> 6.33 ms,
+// 27-bit keys and three sort passes instead of four, fewer link searches)
+constexpr double kDefaultCellMult2 = kDefaultCellMult;
+constexpr double kDefaultCellMult3 = kMaxCellMult3;
 
 size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -82,7 +87,7 @@ struct gd_ctx {
   cudaStream_t own = nullptr;
   cudaStream_t stream = nullptr;
   int precision = GD_PREC_FP64;
-  double mult2 = kDefaultCellMult, mult3 = kDefaultCellMult;
+  double mult2 = kDefaultCellMult2, mult3 = kDefaultCellMult3;
   int tn_core = kDefaultCoreTests, tn_link = kDefaultLinkTests, tn_border = kDefaultBorderTests;
 
   DevBuf coords, inst, chunks, Pv, Bi, bbox, keys0, keys1, vals0, vals1, X, Xf, table, occ, cellz,
@@ -606,8 +611,8 @@ gd_status gd_ctx_set_cell_mults(gd_ctx* ctx, double mult2d, double mult3d) {
     return fail(GD_EINVAL, "2D cell multiplier must lie in (0.5, 1/sqrt(2)) or be 0");
   if (mult3d != 0.0 && !(mult3d > 0.5 && mult3d <= kMaxCellMult3))
     return fail(GD_EINVAL, "3D cell multiplier must lie in (0.5, 1/sqrt(3)) or be 0");
-  ctx->mult2 = mult2d != 0.0 ? mult2d : kDefaultCellMult;
-  ctx->mult3 = mult3d != 0.0 ? mult3d : kDefaultCellMult;
+  ctx->mult2 = mult2d != 0.0 ? mult2d : kDefaultCellMult2;
+  ctx->mult3 = mult3d != 0.0 ? mult3d : kDefaultCellMult3;
   return GD_OK;
 }
 

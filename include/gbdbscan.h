@@ -102,7 +102,8 @@ void gd_ctx_destroy(gd_ctx* ctx);
 /* stream: a cudaStream_t of the context's device; NULL restores the context's own */
 gd_status gd_ctx_set_stream(gd_ctx* ctx, void* stream);
 gd_status gd_ctx_set_precision(gd_ctx* ctx, int32_t precision);
-/* grid cell side = eps * mult; 0 restores the default 0.5*(1+2^-16).
+/* grid cell side = eps * mult; 0 restores the defaults: 0.5*(1+2^-16) in 2D,
+   the largest allowed, (1/sqrt(3))*(1-2^-20), in 3D.
    Allowed range: (0.5, 1/sqrt(dim)) -- cells stay smaller than eps/sqrt(dim) so
    a cell's points are mutual neighbours, and larger than eps/2 so neighbours
    stay within +-2 cells. */
