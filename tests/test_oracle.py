@@ -86,3 +86,20 @@ def test_reference_multicore_baseline_runs(oracle):
     k1 = oracle.ref_multicore_dbscan(pts, 0.3, 5, threads=1)
     k4 = oracle.ref_multicore_dbscan(pts, 0.3, 5, threads=4)
     assert k1 == k4 >= 3
+
+
+@pytest.mark.parametrize("spacing,offset", [(0.1, 0.0), (0.3, 1000.0), (0.001, 12.3)])
+def test_quantised_inputs_stay_below_the_one_directional_pair_cap(oracle, spacing, offset):
+    # A pair is a neighbour one way only when the query box and the distance test
+    # disagree in the last bit (the case above: a coordinate near 0 beside one at
+    # eps).  Lattices with spacing equal to eps, and data rounded to a decimal
+    # step, produce none, far from the 2,048 pairs the device's merge replay holds.
+    xs = np.arange(100) * spacing + offset
+    g = np.stack(np.meshgrid(xs, xs, indexing="ij"), -1).reshape(-1, 2)
+    _, _, c = oracle.oracle_dbscan(g, spacing, 4)
+    assert c["asym_pairs"] == 0
+    rng = np.random.default_rng(7)
+    dec = int(round(-np.log10(spacing)))
+    r = np.round(rng.uniform(0, 500 * spacing, size=(20000, 2)), dec) + offset
+    _, _, c = oracle.oracle_dbscan(r, spacing, 4)
+    assert c["asym_pairs"] == 0
